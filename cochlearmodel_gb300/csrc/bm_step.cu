@@ -1,0 +1,377 @@
+// BM/OHC adaptive-step solver (reference kernel 17,
+// include/cochlea.cuh:13573-14245, launched by BMOHCNewKernel,
+// src/cochlea.cu:1436-1493).
+//
+// GB300 layout: one WARP owns one unit (one time block of one signal); lane l
+// holds sections 8l..8l+7 of every state vector in registers.  A Jacobi sweep
+// is 8 FADD + 8 FFMA per lane plus two shuffles for the halo (sections 8l-1
+// and 8l+8) -- no shared-memory round trip and no block barrier, where the
+// reference spends two __syncthreads per sweep across 256 threads.  The
+// Lipschitz/fault reductions are xor-butterflies, so every lane holds the
+// full result and takes the same step decision (the reference's warp-0
+// reduction leaves the full value only in lane 0; its other lanes race on
+// the shared decision slots -- this kernel takes the lane-0 semantics).
+// Units come from a device work queue, so a persistent grid of warps drains
+// batches of uneven-length signals.
+//
+// Floating-point order is fixed (compiled with --fmad=false; explicit
+// __fmaf_rn where an FMA is intended) and matches the CPU oracle, which
+// evaluates the same sequence, bit for bit.  The simulated-time accumulator
+// is double.
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+
+#include "cgb_device.cuh"
+#include "cgb_internal.h"
+
+namespace cgb {
+
+constexpr int kSPL = 8;  // sections per lane
+
+struct BMArgs {
+  const float* secp;   // [8][256]: 1/M, 1/m, R, S, Q, S_ohc, S_tm, R_tm
+  const float* gamma;  // [P][256]
+  const cgb_unit* units;
+  int n_units;
+  const float* in;
+  float* out;
+  int32_t* failed;
+  cgb_unit_stats* stats;
+  int32_t* work;
+  float ratio, nas, al, e1, e2, nw, ar, dx2, dxa0, na1, na2, gme, sow;
+  float dt0, dtmin, dtmax;
+  int jfast, jslow, max_outer, max_sub;
+  double tout, invts;
+};
+
+__device__ __forceinline__ void load8(const float* p, float (&r)[kSPL]) {
+  const float4 a = reinterpret_cast<const float4*>(p)[0];
+  const float4 b = reinterpret_cast<const float4*>(p)[1];
+  r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+  r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+}
+
+// One unit, executed by one full warp.  sp: shared [8][256] section
+// parameters; sg / sgs: shared gamma and gamma*S_ohc of the unit's profile.
+__device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
+                                         const float* __restrict__ sp,
+                                         const float* __restrict__ sg,
+                                         const float* __restrict__ sgs, int lane,
+                                         cgb_unit_stats* st) {
+  const int base = lane * kSPL;
+  float rm[kSPL];
+  load8(sp + 1 * 256 + base, rm);
+
+  float x0[kSPL], v0[kSPL], a0[kSPL], y0[kSPL], u0[kSPL], ps0[kSPL], dp0[kSPL];
+  float x[kSPL], v[kSPL], a[kSPL], y[kSPL], u[kSPL], ps[kSPL], dp[kSPL];
+  float Ptm[kSPL], p[kSPL], G[kSPL], Yrm[kSPL];
+#pragma unroll
+  for (int k = 0; k < kSPL; ++k) {
+    x0[k] = v0[k] = a0[k] = y0[k] = u0[k] = ps0[k] = dp0[k] = 0.0f;
+    x[k] = v[k] = a[k] = y[k] = u[k] = ps[k] = dp[k] = 0.0f;
+    Ptm[k] = p[k] = G[k] = Yrm[k] = 0.0f;
+  }
+  float w0 = 0.f, wd0 = 0.f, wdd0 = 0.f, w = 0.f, wd = 0.f, wdd = 0.f;
+
+  const float mtt = un.mtt, mmspt = un.mmspt;
+  const float* inb = A.in + un.in_base;
+  float* outb = A.out + un.out_base * 256;
+  int32_t* fb = A.failed ? A.failed + un.out_base : nullptr;
+
+  float dt = A.dt0;
+  double tau = 0.0;
+  int n = un.start;
+  float sx0 = inb[n], sx1 = inb[n + 1];
+  int fail_flag = 0;
+  long long n_sub = 0, n_it = 0, n_sw = 0;
+  int n_failed = 0, n_written = 0, status = 0, sub_in_sample = 0;
+
+  while (n < un.end) {
+    if (++sub_in_sample > A.max_sub) {  // dt collapsed: stop this unit, flag it
+      status = 1;
+      break;
+    }
+    int out_loop = 0, reset = 1, another = 1;
+    const float delta = (float)(tau * A.invts);
+    const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
+    do {
+      float evp = 0.0f, fp = 0.0f;
+      if (out_loop == 0 || reset) {
+        out_loop = 0;
+#pragma unroll
+        for (int k = 0; k < kSPL; ++k) {
+          y[k] = __fmaf_rn(u0[k], dt, y0[k]);
+          const float vn = __fmaf_rn(a0[k], dt, v0[k]);
+          const float dv = fabsf(__fsub_rn(vn, v[k]));
+          v[k] = vn;
+          x[k] = __fmaf_rn(__fmul_rn(__fadd_rn(v0[k], vn), 0.5f), dt, x0[k]);
+          ps[k] = __fmaf_rn(dp0[k], dt, ps0[k]);
+          evp = __fadd_rn(evp, dv);
+          fp = __fadd_rn(fp, __fsub_rn(dv, fmaxf(mtt, __fmul_rn(vn, dt))));
+        }
+        w = __fmaf_rn(wd0, dt, w0);
+        wd = __fmaf_rn(wdd0, dt, wd0);
+      } else {
+#pragma unroll
+        for (int k = 0; k < kSPL; ++k) {
+          const float vn = __fmaf_rn(__fmul_rn(__fadd_rn(a0[k], a[k]), 0.5f), dt, v0[k]);
+          const float dv = fabsf(__fsub_rn(vn, v[k]));
+          v[k] = vn;
+          x[k] = __fmaf_rn(__fmul_rn(__fadd_rn(v0[k], vn), 0.5f), dt, x0[k]);
+          y[k] = __fmaf_rn(__fmul_rn(__fadd_rn(u0[k], u[k]), 0.5f), dt, y0[k]);
+          ps[k] = __fmaf_rn(__fmul_rn(__fadd_rn(dp0[k], dp[k]), 0.5f), dt, ps0[k]);
+          evp = __fadd_rn(evp, dv);
+          fp = __fadd_rn(fp, __fsub_rn(dv, fmaxf(mtt, __fmul_rn(vn, dt))));
+        }
+        w = __fmaf_rn(__fmul_rn(__fadd_rn(wd0, wd), 0.5f), dt, w0);
+        wd = __fmaf_rn(__fmul_rn(__fadd_rn(wdd0, wdd), 0.5f), dt, wd0);
+      }
+
+      // OHC / TM coupling, G and the right-hand side Y (scaled by 1/m).
+      const bool tm_update = out_loop < 2;
+#pragma unroll
+      for (int k = 0; k < kSPL; ++k) {
+        const int s = base + k;
+        const float d = __fsub_rn(y[k], x[k]);
+        const float Pohc = __fmul_rn(sgs[s], d);
+        const float Stm = sp[6 * 256 + s], Rtm = sp[7 * 256 + s];
+        if (tm_update) {
+          const float gm = sg[s];
+          const float t = own_tanhf(__fmul_rn(A.ratio, ps[k]));
+          const float dL = __fmul_rn(A.nas, t);
+          const float Aa = __fmul_rn(A.al, __fmaf_rn(t, t, -1.0f));
+          const float N1 = __fmaf_rn(A.e1, d, __fmaf_rn(A.e2, v[k], __fmul_rn(A.nw, ps[k])));
+          const float N = __fmaf_rn(Stm, dL, __fmul_rn(__fmul_rn(N1, Rtm), Aa));
+          const float Pp = __fmaf_rn(Stm, y[k], Pohc);
+          const float num = __fmaf_rn(-gm, N, Pp);
+          const float den = __fmul_rn(Rtm, __fmaf_rn(__fmul_rn(gm, Aa), A.e2, -1.0f));
+          u[k] = __fdiv_rn(num, den);
+          Ptm[k] = __fmaf_rn(Rtm, u[k], __fmul_rn(Stm, y[k]));
+        }
+        float g = __fmul_rn(sp[2 * 256 + s], __fmaf_rn(A.ar, __fmul_rn(v[k], v[k]), 1.0f));
+        g = __fmaf_rn(g, v[k], __fmul_rn(sp[3 * 256 + s], x[k]));
+        G[k] = __fsub_rn(-g, Ptm[k]);
+        float Yk = __fmul_rn(__fmul_rn(A.dx2, G[k]), sp[4 * 256 + s]);
+        if (k == 0 && lane == 0)
+          Yk = __fmul_rn(A.dxa0, __fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmul_rn(A.gme, smp))));
+        if (k == kSPL - 1 && lane == 31) Yk = 0.0f;
+        Yrm[k] = __fmul_rn(Yk, rm[k]);
+      }
+
+      // Jacobi sweeps on the pressure; p persists across iterations and steps.
+      const int J = tm_update ? A.jslow : A.jfast;
+      for (int it = 0; it < J; ++it) {
+        float left = __shfl_up_sync(kFull, p[kSPL - 1], 1);
+        float right = __shfl_down_sync(kFull, p[0], 1);
+        if (lane == 0) left = 0.0f;
+        if (lane == 31) right = 0.0f;
+        float t[kSPL];
+        t[0] = __fadd_rn(left, p[1]);
+#pragma unroll
+        for (int k = 1; k < kSPL - 1; ++k) t[k] = __fadd_rn(p[k - 1], p[k + 1]);
+        t[kSPL - 1] = __fadd_rn(p[kSPL - 2], right);
+        if (lane == 31) {  // rows 254, 255 carry no lower coefficient
+          t[kSPL - 2] = p[kSPL - 1];
+          t[kSPL - 1] = right;
+        }
+#pragma unroll
+        for (int k = 0; k < kSPL; ++k) p[k] = __fmaf_rn(-t[k], rm[k], Yrm[k]);
+      }
+      n_sw += J;
+
+      const float p0 = __shfl_sync(kFull, p[0], 0);
+      float eap = 0.0f;
+#pragma unroll
+      for (int k = 0; k < kSPL; ++k) {
+        const int s = base + k;
+        const float an = __fmul_rn(__fadd_rn(p[k], G[k]), sp[0 * 256 + s]);
+        eap = fmaxf(eap, fabsf(__fsub_rn(a[k], an)));
+        a[k] = an;
+        const float d = __fsub_rn(y[k], x[k]);
+        dp[k] = __fmaf_rn(A.e1, d, __fmaf_rn(A.e2, __fsub_rn(u[k], v[k]), __fmul_rn(A.nw, ps[k])));
+      }
+      wdd = __fdiv_rn(__fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmaf_rn(A.gme, smp, p0))), A.sow);
+
+      if (reset == 0) {
+        const float ea = warp_max_xor(eap);
+        const float ev = warp_sum_xor(evp);
+        const float F = warp_sum_xor(fp);
+        const float L = ev > mmspt ? __fdiv_rn(__fmul_rn(ea, dt), ev) : 0.0f;
+        if (L > 6.0f) {
+          dt = __fmul_rn(dt, 0.5f);
+          if (dt < A.dtmin) dt = A.dtmin;
+          another = 0;
+          reset = 1;
+        } else if (F > 0.0f) {
+          another = 1;
+          reset = 0;
+        } else if (L < 0.5f) {
+          dt = __fmul_rn(dt, 2.0f);
+          if (dt > A.dtmax) dt = A.dtmax;
+          another = 0;
+          reset = 1;
+        } else {
+          another = 1;
+          reset = 0;
+        }
+      } else {
+        another = 1;
+        reset = 0;
+      }
+      ++out_loop;
+      if (out_loop >= A.max_outer) {
+        another = 0;
+        reset = 1;
+        fail_flag = 1;
+      }
+    } while (another);
+    ++n_sub;
+    n_it += out_loop;
+
+    if (tau > A.tout) {
+      tau -= A.tout;
+      sx0 = sx1;
+      sx1 = inb[n + 2];
+      if (n >= un.out_first) {
+        float4* o = reinterpret_cast<float4*>(outb + (int64_t)n * 256 + base);
+        o[0] = make_float4(v[0], v[1], v[2], v[3]);
+        o[1] = make_float4(v[4], v[5], v[6], v[7]);
+        if (fb && lane == 0) fb[n] = fail_flag;
+        ++n_written;
+        n_failed += fail_flag;
+      }
+      fail_flag = 0;
+      sub_in_sample = 0;
+      ++n;
+    }
+#pragma unroll
+    for (int k = 0; k < kSPL; ++k) {
+      x0[k] = x[k];
+      v0[k] = v[k];
+      a0[k] = a[k];
+      ps0[k] = ps[k];
+      dp0[k] = dp[k];
+      u0[k] = u[k];
+      y0[k] = y[k];
+    }
+    w0 = w;
+    wd0 = wd;
+    wdd0 = wdd;
+    tau += (double)dt;
+  }
+  if (st && lane == 0) {
+    st->substeps = n_sub;
+    st->iterations = n_it;
+    st->sweeps = n_sw;
+    st->failed_samples = n_failed;
+    st->written_samples = n_written;
+    st->status = status;
+  }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) bm_warp_kernel(const BMArgs A) {
+  __shared__ __align__(16) float s_par[8 * 256];
+  __shared__ __align__(16) float s_gam[WARPS][2][256];
+  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) s_par[i] = A.secp[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    int uid = 0;
+    if (lane == 0) uid = atomicAdd(A.work, 1);
+    uid = __shfl_sync(kFull, uid, 0);
+    if (uid >= A.n_units) break;
+    const cgb_unit un = A.units[uid];
+    const float* g = A.gamma + (int64_t)un.profile * 256;
+#pragma unroll
+    for (int k = 0; k < kSPL; ++k) {
+      const int s = lane * kSPL + k;
+      const float gm = g[s];
+      s_gam[warp][0][s] = gm;
+      s_gam[warp][1][s] = __fmul_rn(gm, s_par[5 * 256 + s]);
+    }
+    __syncwarp();
+    run_unit(A, un, s_par, s_gam[warp][0], s_gam[warp][1], lane,
+             A.stats ? A.stats + uid : nullptr);
+    __syncwarp();
+  }
+}
+
+constexpr int kWarpsPerCta = 4;
+
+}  // namespace cgb
+
+extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
+                              const cgb_bm_scalars* sc, const cgb_unit* d_units, int n_units,
+                              const float* d_in, int64_t in_len, float* d_out,
+                              int64_t out_rows, int32_t* d_failed, cgb_unit_stats* d_stats,
+                              int32_t* d_work, void* stream) {
+  using namespace cgb;
+  if (!d_secp || !d_gamma || !sc || !d_units || !d_in || !d_out || !d_work)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: null pointer argument");
+  if (n_units < 0 || n_profiles <= 0 || in_len <= 0 || out_rows <= 0)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: bad sizes");
+  if (sc->red_lanes != 32 || sc->jacobi_mode != 0)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: only red_lanes=32, jacobi_mode=0 are built");
+  if (sc->jacobi_fast < 0 || sc->jacobi_slow < 0 || sc->max_outer < 1 ||
+      sc->max_substeps_per_sample < 1)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: bad loop counts");
+  if ((reinterpret_cast<uintptr_t>(d_out) & 15) || (reinterpret_cast<uintptr_t>(d_secp) & 15))
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: d_out and d_secp must be 16-byte aligned");
+  if (n_units == 0) return CGB_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  BMArgs A;
+  A.secp = d_secp;
+  A.gamma = d_gamma;
+  A.units = d_units;
+  A.n_units = n_units;
+  A.in = d_in;
+  A.out = d_out;
+  A.failed = d_failed;
+  A.stats = d_stats;
+  A.work = d_work;
+  A.ratio = sc->alpha_l / sc->alpha_s;
+  A.nas = -sc->alpha_s;
+  A.al = sc->alpha_l;
+  A.e1 = sc->eta_1;
+  A.e2 = sc->eta_2;
+  A.nw = -sc->w_ohc;
+  A.ar = sc->alpha_r;
+  A.dx2 = sc->delta_x * sc->delta_x;
+  A.dxa0 = sc->delta_x * sc->a0;
+  A.na1 = -sc->a1;
+  A.na2 = -sc->a2;
+  A.gme = sc->Gme;
+  A.sow = sc->sigma_ow;
+  A.dt0 = sc->time_step;
+  A.dtmin = sc->dt_min;
+  A.dtmax = sc->dt_max;
+  A.jfast = sc->jacobi_fast;
+  A.jslow = sc->jacobi_slow;
+  A.max_outer = sc->max_outer;
+  A.max_sub = sc->max_substeps_per_sample;
+  A.tout = (double)sc->time_step_out;
+  A.invts = 1.0 / (double)sc->Ts;
+
+  int dev = 0, n_sm = 0, per_sm = 0;
+  CGB_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  CGB_TRY_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev),
+               "cudaDeviceGetAttribute");
+  CGB_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &per_sm, bm_warp_kernel<kWarpsPerCta>, kWarpsPerCta * 32, 0),
+               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+  if (per_sm < 1) per_sm = 1;
+  long long want = (n_units + kWarpsPerCta - 1) / kWarpsPerCta;
+  long long grid = (long long)n_sm * per_sm;
+  if (grid > want) grid = want;
+  CGB_TRY_CUDA(cudaMemsetAsync(d_work, 0, sizeof(int32_t), st), "cudaMemsetAsync(work)");
+  bm_warp_kernel<kWarpsPerCta><<<(unsigned)grid, kWarpsPerCta * 32, 0, st>>>(A);
+  CGB_TRY_CUDA(cudaGetLastError(), "bm_warp_kernel launch");
+  note_launch();
+  (void)in_len;
+  (void)out_rows;
+  return CGB_OK;
+}

@@ -1,0 +1,75 @@
+// Device helpers shared by the solver kernels.
+#pragma once
+
+#include <cstdint>
+
+namespace cgb {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// e^y for y >= 0 by Cody-Waite reduction y = k ln2 + r and a degree-8 Taylor
+// polynomial of e^r; 2^k is assembled in the exponent field.  The order of
+// every float operation is fixed (explicit fma, no contraction) so the CPU
+// oracle, which evaluates the same sequence, rounds identically.
+__device__ __forceinline__ float own_expf_pos(float y) {
+  const float log2e = 1.44269504088896341f;
+  const float ln2_hi = 0.693145751953125f;
+  const float ln2_lo = 1.42860682030941723e-06f;
+  float k = rintf(__fmul_rn(y, log2e));
+  float r = __fmaf_rn(-k, ln2_hi, y);
+  r = __fmaf_rn(-k, ln2_lo, r);
+  float p = 1.0f / 40320.0f;
+  p = __fmaf_rn(p, r, 1.0f / 5040.0f);
+  p = __fmaf_rn(p, r, 1.0f / 720.0f);
+  p = __fmaf_rn(p, r, 1.0f / 120.0f);
+  p = __fmaf_rn(p, r, 1.0f / 24.0f);
+  p = __fmaf_rn(p, r, 1.0f / 6.0f);
+  p = __fmaf_rn(p, r, 0.5f);
+  p = __fmaf_rn(p, r, 1.0f);
+  p = __fmaf_rn(p, r, 1.0f);
+  int ki = (int)k;
+  float scale = __int_as_float((ki + 127) << 23);
+  return __fmul_rn(p, scale);
+}
+
+// tanh(x): odd Taylor series to x^21 below |x| = 0.55, 1 - 2/(e^{2|x|}+1)
+// up to |x| = 20, +-1 beyond.
+__device__ __forceinline__ float own_tanhf(float x) {
+  float ax = fabsf(x);
+  float r;
+  if (ax < 0.55f) {
+    float x2 = __fmul_rn(x, x);
+    float p = (float)(18888466084.0 / 194896477400625.0);
+    p = __fmaf_rn(p, x2, (float)(-443861162.0 / 1856156927625.0));
+    p = __fmaf_rn(p, x2, (float)(6404582.0 / 10854718875.0));
+    p = __fmaf_rn(p, x2, (float)(-929569.0 / 638512875.0));
+    p = __fmaf_rn(p, x2, (float)(21844.0 / 6081075.0));
+    p = __fmaf_rn(p, x2, (float)(-1382.0 / 155925.0));
+    p = __fmaf_rn(p, x2, (float)(62.0 / 2835.0));
+    p = __fmaf_rn(p, x2, (float)(-17.0 / 315.0));
+    p = __fmaf_rn(p, x2, (float)(2.0 / 15.0));
+    p = __fmaf_rn(p, x2, (float)(-1.0 / 3.0));
+    p = __fmul_rn(p, x2);
+    return __fmaf_rn(p, x, x);
+  } else if (ax < 20.0f) {
+    float e = own_expf_pos(__fmul_rn(2.0f, ax));
+    r = __fsub_rn(1.0f, __fdiv_rn(2.0f, __fadd_rn(e, 1.0f)));
+  } else {
+    r = 1.0f;
+  }
+  return x < 0.0f ? -r : r;
+}
+
+__device__ __forceinline__ float warp_sum_xor(float v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+__device__ __forceinline__ float warp_max_xor(float v) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+}  // namespace cgb

@@ -1,0 +1,141 @@
+/*
+ * cochlea_gb300.h -- plain C ABI of the GB300-native cochlear solver.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (CGB_OK == 0); the message of the last failure is in cgb_last_error().
+ * Functions whose name ends in _dev take DEVICE pointers and a CUDA stream
+ * (passed as void*), enqueue work and return without synchronising.  The
+ * reference-named drop-in layer (include/cochlea_common.h) is built on top of
+ * this ABI.
+ *
+ * Reference interfaces replaced (YonatanKoral/CochlearModel):
+ *   cgb_model_setup        CModel ctor + CSolver::Init_Tri_Matrix
+ *                          (src/model.cpp:18-86, src/solver.cpp:155-176)
+ *   cgb_block_partition    the per-block start/output/end table built inside
+ *                          BMOHCNewKernel (src/cochlea.cu:1148-1176)
+ *   cgb_bm_run_dev         the kernel launch of BMOHCNewKernel, variant 17
+ *                          (src/cochlea.cu:1436-1493,
+ *                           include/cochlea.cuh:13573-14245)
+ *   cgb_ihc_lambda_dev     RunIHCKernel: CudaUnifiedCalcIHC + CudaCalcLambda
+ *                          (src/cochlea.cu:3573-3644, 3431-3506, 3365-3408)
+ *   cgb_jnd_dev            CudaCalculateJND: GlobalCalculateMeanRate +
+ *                          GlobalCalculateJND (src/cochlea.cu:3946-4065)
+ *   cgb_input_gen_dev      generateInputFromProfile's kernel
+ *                          CudaGenerateInputFromProfile (src/cochlea.cu:4070-4103)
+ *   cgb_noise_normalization calculateDCANDNornalizationFactor /
+ *                          ...PureTone (src/cochlea.cu:4165-4254)
+ */
+#ifndef COCHLEA_GB300_H
+#define COCHLEA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CGB_SECTIONS 256
+#define CGB_LAMBDA_COUNT 3
+
+enum {
+  CGB_OK = 0,
+  CGB_ERR_ARG = 1,    /* invalid argument (null pointer, bad size)        */
+  CGB_ERR_CUDA = 2,   /* a CUDA runtime call failed                       */
+  CGB_ERR_RANGE = 3,  /* a size beyond a documented maximum               */
+  CGB_ERR_STATE = 4   /* call out of order (drop-in layer)                */
+};
+
+/* One unit of BM work: one time block of one signal, simulated from zero
+ * state (reference: one CUDA block of BMOHCNewKernel).  Coordinates are in
+ * samples of the unit's frame; the frame's sample 0 sits at input index
+ * in_base and at output row out_base (rows of 256 floats). */
+typedef struct cgb_unit {
+  int64_t in_base;
+  int64_t out_base;
+  int32_t start;      /* first input sample simulated                     */
+  int32_t out_first;  /* first sample whose velocity row is written       */
+  int32_t end;        /* one past the last sample simulated               */
+  int32_t profile;    /* OHC (gamma) profile row                          */
+  float mtt;          /* throw tolerance   (Max_Tolerance)                */
+  float mmspt;        /* m1_sp tolerance   (Max_M1_SP_Error)              */
+} cgb_unit;
+
+/* Per-unit counters written by the BM kernel. */
+typedef struct cgb_unit_stats {
+  int64_t substeps;        /* accepted + rejected time steps               */
+  int64_t iterations;      /* outer (predictor/corrector) iterations       */
+  int64_t sweeps;          /* Jacobi sweeps                                */
+  int32_t failed_samples;  /* written samples with a non-converged step    */
+  int32_t written_samples;
+  int32_t status;          /* 0 ok; 1 stopped: a sample needed more than
+                              max_substeps_per_sample steps (dt collapsed) */
+  int32_t pad_;
+} cgb_unit_stats;
+
+/* Scalars of the BM/OHC step (the float arguments of BMOHCNewKernel). */
+typedef struct cgb_bm_scalars {
+  float w_ohc, time_step, time_step_out, delta_x, alpha_r, Ts;
+  float alpha_l, alpha_s, Gme, a0, a1, a2, sigma_ow, eta_1, eta_2;
+  float dt_min, dt_max;
+  int32_t jacobi_fast;  /* sweeps on outer iterations >= 2 (JACOBBY_Loops_Fast) */
+  int32_t jacobi_slow;  /* sweeps on outer iterations 0-1 (JACOBBY_Loops_Slow)  */
+  int32_t max_outer;    /* Cuda_Outern_Loops                                   */
+  int32_t red_lanes;    /* reduction tree width; must be 32                    */
+  int32_t jacobi_mode;  /* must be 0 (fixed sweeps, reference semantics)       */
+  int32_t max_substeps_per_sample; /* guard against a collapsed dt (>= 1)       */
+} cgb_bm_scalars;
+
+const char* cgb_last_error(void);
+int cgb_abi_version(void);
+
+/* Model vectors.  Outputs (double, 256 each): M, R, S, Q, S_ohc, S_tm, R_tm and
+ * the pressure-system diagonals m, l, u.  scal (double[16]): w_ohc, dx,
+ * alpha_r, alpha_L, alpha_s, Gme, a0, a1, a2, sigma_ow, eta_1, eta_2, w_ow,
+ * Cme, ratio_K, psi0. */
+int cgb_model_setup(double* M, double* R, double* S, double* Q, double* S_ohc,
+                    double* S_tm, double* R_tm, double* diag_m, double* diag_l,
+                    double* diag_u, double* scal);
+
+/* Packs the float section parameters the BM kernel reads:
+ * secp = float[8][256]: 1/M, 1/m, R, S, Q, S_ohc, S_tm, R_tm, from the float
+ * casts the reference host makes (src/solver.cpp:357-376). */
+int cgb_pack_sections(const double* M, const double* diag_m, const double* R,
+                      const double* S, const double* Q, const double* S_ohc,
+                      const double* S_tm, const double* R_tm, float* secp);
+
+/* Fills the reference block partition for one run of `time_blocks` blocks
+ * over a buffer of samples_p1 samples (totalTimeNodesP1). */
+int cgb_block_partition(int time_blocks, int64_t samples_p1, int overlap, int decouple,
+                        int32_t* start, int32_t* out_first, int32_t* end);
+
+/* BM/OHC solver over n_units units (device pointers).
+ *   d_secp   float[8][256]     section parameters (cgb_pack_sections)
+ *   d_gamma  float[P][256]     OHC profiles
+ *   d_units  cgb_unit[n_units]
+ *   d_in     float[in_len]     input samples; each unit reads up to
+ *                              in_base+end+1
+ *   d_out    float[out_rows][256] velocity rows
+ *   d_failed int32[out_rows]   1 where a written sample had a step that hit
+ *                              max_outer (may be null)
+ *   d_stats  cgb_unit_stats[n_units] (may be null)
+ *   d_work   int32[1] scratch: the work-queue counter (reset in-stream)
+ * Units are taken from a device work queue by a persistent grid of warps. */
+int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
+                   const cgb_bm_scalars* sc, const cgb_unit* d_units, int n_units,
+                   const float* d_in, int64_t in_len, float* d_out, int64_t out_rows,
+                   int32_t* d_failed, cgb_unit_stats* d_stats, int32_t* d_work,
+                   void* stream);
+
+/* Host-side validation of a unit table against buffer sizes (the checks
+ * cgb_bm_run_dev relies on); returns CGB_ERR_RANGE on the first bad unit. */
+int cgb_check_units(const cgb_unit* units, int n_units, int n_profiles, int64_t in_len,
+                    int64_t out_rows);
+
+/* Number of BM kernel launches enqueued by this process (for accounting). */
+int64_t cgb_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COCHLEA_GB300_H */

@@ -1,0 +1,730 @@
+// Test infrastructure: the CPU oracle of the cochlear-solver hot path.
+//
+// This file is NOT part of the product.  Only tests/, __graft_entry__.smoke()
+// and bench.py's CPU-baseline / reference arm may load it, and only as the
+// checker or as the timed CPU implementation -- never as the thing shipped.
+//
+// It restates, in plain C++, the arithmetic of the reference path
+// (YonatanKoral/CochlearModel):
+//   * model vectors            src/model.cpp:72-86, include/const.h:216-297
+//   * tridiagonal diagonals    src/solver.cpp:155-176
+//   * Thomas solve             src/tridiag.cpp:67-106
+//   * block partition          src/cochlea.cu:1148-1176
+//   * BM/OHC adaptive step     include/cochlea.cuh:13573-14245 (kernel 17)
+//   * IHC + lambda             src/cochlea.cu:2712-2730, 2980-2988, 3291-3317,
+//                              3365-3408, 3431-3506
+//   * JND (Eq. 17-24)          src/cochlea.cu:3741-3944,
+//                              src/AudioGramCreator.cpp:454-508
+//   * input generation         src/cochlea.cu:4070-4103, 4165-4254
+//
+// Parity pinning: the reference publishes no tests, fixtures or golden
+// vectors, and its own path cannot be built here (Windows/MFC/MATLAB host,
+// GPU-only kernels).  Its Thomas solve (src/tridiag.cpp) and constants
+// header (include/const.h) DO compile on their own; oracle/build_ref.sh
+// builds them into oracle/_ref/ and tests/test_oracle_pins.py checks this
+// restatement against them.  The BM step, IHC, lambda and JND stages are
+// pinned only by this restatement ("parity pinned for the model constants
+// and the tridiagonal solve; restatement-only for the time stepping").
+//
+// FP32 mode fixes the order of every floating-point operation (explicit
+// fmaf, IEEE division, a fixed reduction tree) so that the CUDA kernels,
+// which follow the same order, agree with it bit for bit.  FP64 mode runs the
+// same algorithm in double and is the accuracy yardstick.
+//
+// Build: oracle/build.sh (g++ -O2 -ffp-contract=off, no fast-math).
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <algorithm>
+#include <atomic>
+#include <thread>
+#include <type_traits>
+#include <vector>
+
+namespace {
+
+constexpr int NS = 256;  // cochlear sections (include/const.h:19)
+
+// ---------------------------------------------------------------------------
+// tanh in float.  The reference calls CUDA's tanhf; this project uses its own
+// tanh on both sides so the GPU and the oracle round identically:
+//   |x| < 0.55 : odd Taylor series of tanh to x^21 (coefficients
+//                2^{2n}(2^{2n}-1)B_{2n}/(2n)!), Horner in x^2;
+//   |x| < 20   : 1 - 2/(e^{2|x|}+1), e^y by Cody-Waite reduction
+//                y = k ln2 + r and a degree-8 Taylor polynomial of e^r;
+//   else       : +-1.
+// ---------------------------------------------------------------------------
+float own_expf_pos(float y) {
+  const float log2e = 1.44269504088896341f;
+  const float ln2_hi = 0.693145751953125f;
+  const float ln2_lo = 1.42860682030941723e-06f;
+  float k = rintf(y * log2e);
+  float r = fmaf(-k, ln2_hi, y);
+  r = fmaf(-k, ln2_lo, r);
+  float p = 1.0f / 40320.0f;
+  p = fmaf(p, r, 1.0f / 5040.0f);
+  p = fmaf(p, r, 1.0f / 720.0f);
+  p = fmaf(p, r, 1.0f / 120.0f);
+  p = fmaf(p, r, 1.0f / 24.0f);
+  p = fmaf(p, r, 1.0f / 6.0f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  int ki = (int)k;
+  uint32_t bits = (uint32_t)(ki + 127) << 23;
+  float scale;
+  std::memcpy(&scale, &bits, 4);
+  return p * scale;
+}
+
+float own_tanhf(float x) {
+  float ax = fabsf(x);
+  float r;
+  if (ax < 0.55f) {
+    float x2 = x * x;
+    float p = (float)(18888466084.0 / 194896477400625.0);
+    p = fmaf(p, x2, (float)(-443861162.0 / 1856156927625.0));
+    p = fmaf(p, x2, (float)(6404582.0 / 10854718875.0));
+    p = fmaf(p, x2, (float)(-929569.0 / 638512875.0));
+    p = fmaf(p, x2, (float)(21844.0 / 6081075.0));
+    p = fmaf(p, x2, (float)(-1382.0 / 155925.0));
+    p = fmaf(p, x2, (float)(62.0 / 2835.0));
+    p = fmaf(p, x2, (float)(-17.0 / 315.0));
+    p = fmaf(p, x2, (float)(2.0 / 15.0));
+    p = fmaf(p, x2, (float)(-1.0 / 3.0));
+    p = p * x2;
+    return fmaf(p, x, x);
+  } else if (ax < 20.0f) {
+    float e = own_expf_pos(2.0f * ax);
+    r = 1.0f - 2.0f / (e + 1.0f);
+  } else {
+    r = 1.0f;
+  }
+  return x < 0.0f ? -r : r;
+}
+
+template <typename T> struct Ar;
+template <> struct Ar<float> {
+  static float fma(float a, float b, float c) { return fmaf(a, b, c); }
+  static float tanh(float x) { return own_tanhf(x); }
+  static float abs(float x) { return fabsf(x); }
+  static float max(float a, float b) { return fmaxf(a, b); }
+  static float min(float a, float b) { return fminf(a, b); }
+};
+template <> struct Ar<double> {
+  static double fma(double a, double b, double c) { return std::fma(a, b, c); }
+  static double tanh(double x) { return std::tanh(x); }
+  static double abs(double x) { return std::fabs(x); }
+  static double max(double a, double b) { return std::fmax(a, b); }
+  static double min(double a, double b) { return std::fmin(a, b); }
+};
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// Shared record layouts (the product declares identical ones in
+// include/cochlea_gb300.h).
+// ---------------------------------------------------------------------------
+typedef struct {
+  int64_t in_base;    // input index of frame sample 0
+  int64_t out_base;   // output row of frame sample 0
+  int32_t start;      // first input sample simulated (frame coords)
+  int32_t out_first;  // first sample whose velocity row is written
+  int32_t end;        // one past the last sample simulated
+  int32_t profile;    // OHC (gamma) profile index
+  float mtt;          // throw tolerance  (Max_Tolerance)
+  float mmspt;        // m1_sp tolerance  (Max_M1_SP_Error)
+} orc_unit;
+
+typedef struct {
+  int64_t substeps;
+  int64_t iterations;
+  int64_t sweeps;
+  int32_t failed_samples;
+  int32_t written_samples;
+  int32_t status;
+  int32_t pad_;
+} orc_unit_stats;
+
+typedef struct {
+  float w_ohc, time_step, time_step_out, delta_x, alpha_r, Ts;
+  float alpha_l, alpha_s, Gme, a0, a1, a2, sigma_ow, eta_1, eta_2;
+  float dt_min, dt_max;
+  int32_t jacobi_fast, jacobi_slow, max_outer;
+  int32_t red_lanes;   // reduction tree width (sections per lane = 256/red_lanes)
+  int32_t jacobi_mode; // 0 fixed sweeps (reference), 1 exact tridiagonal solve
+  int32_t max_substeps_per_sample;  // a unit stops (status 1) past this many steps in a sample
+} orc_bm_scalars;
+
+float orc_tanhf(float x) { return own_tanhf(x); }
+
+// ---------------------------------------------------------------------------
+// Model vectors in FP64 from the reference's float-valued constants
+// (src/model.cpp:18-86, include/const.h:216-297) and the pressure system's
+// diagonals (src/solver.cpp:155-176).  Outputs are 256-long arrays.
+// scal_out (double[16]): w_ohc, dx, alpha_r, alpha_L, alpha_s, Gme, a0, a1,
+// a2, sigma_ow, eta_1, eta_2, w_ow, Cme, ratio_K, psi0.
+// ---------------------------------------------------------------------------
+void orc_model_setup(double* M, double* R, double* S, double* Q, double* S_ohc,
+                     double* S_tm, double* R_tm, double* diag_m, double* diag_l,
+                     double* diag_u, double* scal_out) {
+  const float PIf = 3.141592653589793f;
+  // macro expansions evaluated in float, left to right, as the C++ compiler
+  // does for the reference's #defines.
+  float w_ohc_f = 2 * PIf * 1000.0f;                        // W_OHC
+  float eta1_f = (1.0f) / (2e-6f) * 2 * PIf * 1000.0f;      // ETA_1
+  float w_ow_f = 2 * PIf * 1500;                             // W_OW
+  float cme_f = (2 * PIf * 1340) * (2 * PIf * 1340) * 0.059f / (0.49f * 1.4f);  // C_ME
+  float bc0_f = ((2.0f * (1.0f) * (6e-3f)) / (0.5f));
+  float bc1_f = ((0.5f) * (2 * PIf * 1500 * 2 * PIf * 1500) +
+                 (2 * PIf * 1340) * (2 * PIf * 1340) * 0.059f / (0.49f * 1.4f) * (21.4f));
+  float bc2_f = (0.5f) * (20e3f);
+  float dx_f = (3.5f) / NS;
+
+  const double dx = dx_f, area = 0.5f, rho = 1.0f, beta = 0.003f;
+  const double w_ohc = w_ohc_f, ratio_K = 1e-3f;
+  const double M0 = 1.286e-6f, M1 = 1.5f, R0 = 0.25f, R1 = -0.06f, S0 = 1.282e4f,
+               S1 = -1.5f;
+  const double a0 = bc0_f;
+  for (int i = 0; i < NS; ++i) {
+    M[i] = M0 * std::exp(M1 * dx * i);
+    R[i] = R0 * std::exp(R1 * dx * i);
+    S[i] = S0 * std::exp(S1 * dx * i);
+    double wcf2 = S[i] / M[i];
+    R_tm[i] = R[i];
+    S_tm[i] = R[i] * wcf2 / w_ohc;
+    S_ohc[i] = ratio_K * S_tm[i];
+    Q[i] = 2 * rho * beta / (area * M[i]);
+  }
+  double dx2 = dx * dx;
+  for (int i = 0; i < NS; ++i) {
+    diag_u[i] = 1.0;
+    diag_l[i] = 1.0;
+    diag_m[i] = -1.0 * (2.0 + dx2 * Q[i]);
+  }
+  diag_m[0] = -1.0 * (1.0 + dx * a0);
+  diag_m[NS - 1] = 1.0;
+  diag_l[NS - 1] = 0.0;
+  diag_l[NS - 2] = 0.0;
+  double sc[16] = {w_ohc, dx, 0.0f /*BM_ALPHA_R*/, 2e-6f, 1e-6f, 21.4f, a0, bc1_f, bc2_f,
+                   0.5f, eta1_f, 0.0 /*ETA_2*/, w_ow_f, cme_f, ratio_K, 70e-3f};
+  std::memcpy(scal_out, sc, sizeof(sc));
+}
+
+// Thomas solve restated from src/tridiag.cpp:67-106: row i uses sub-diagonal
+// l[i-1], diagonal m[i], super-diagonal u[i].
+void orc_thomas(const double* m, const double* l, const double* u, const double* v,
+                double* res, int n) {
+  std::vector<double> k(n), h(n), p(n);
+  k[0] = m[0];
+  h[0] = u[0] / k[0];
+  for (int i = 1; i < n; ++i) {
+    k[i] = m[i] - l[i - 1] * h[i - 1];
+    h[i] = u[i] / k[i];
+  }
+  p[0] = v[0] / m[0];
+  for (int i = 1; i < n; ++i) p[i] = (v[i] - l[i - 1] * p[i - 1]) / k[i];
+  res[n - 1] = p[n - 1];
+  for (int j = n - 2; j >= 0; --j) res[j] = p[j] - res[j + 1] * h[j];
+}
+
+// Block partition of one run (src/cochlea.cu:1148-1176).  Writes
+// start/out_first/end for each of `time_blocks` blocks.  out_first is the
+// first sample the block owns; the reference also writes sample
+// out_first-1, which the previous block owns (a cross-block write race).
+void orc_block_partition(int time_blocks, int64_t samples_p1, int overlap, int decouple,
+                         int32_t* start, int32_t* out_first, int32_t* end) {
+  int64_t N = (samples_p1 - overlap) / (time_blocks + 1);
+  for (int b = 0; b < time_blocks; ++b) {
+    int transient_offset = (b > 0 && (decouple == 0 || (decouple != 1 && b % decouple != 0)));
+    int pre = decouple > 0 && (decouple == 1 || ((b + 1) % decouple == 0)) && b != time_blocks - 1;
+    int post = decouple > 0 && (b % decouple == 0);
+    int64_t s = b * N;
+    int64_t of = s + std::max(1 - transient_offset - post, 0) * (int64_t)overlap;
+    int64_t len = N + (1 - pre) * (int64_t)overlap;
+    int64_t e = s + len;
+    if (b > 0) of = std::max<int64_t>(of, end[b - 1]);
+    start[b] = (int32_t)s;
+    out_first[b] = (int32_t)of;
+    end[b] = (int32_t)e;
+  }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// BM/OHC adaptive step of one unit (kernel 17 semantics, reference
+// include/cochlea.cuh:13573-14245).  Decisions taken on the full block
+// reduction (the reference's warp-0 lane-0 value; its other lanes race).
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+struct BMModel {
+  T invM[NS], rm[NS], R[NS], S[NS], Q[NS], S_ohc[NS], S_tm[NS], R_tm[NS];
+};
+
+template <typename T>
+T tree_sum(const T* term, int lanes) {
+  int chunk = NS / lanes;
+  T part[NS];
+  for (int l = 0; l < lanes; ++l) {
+    T acc = T(0);
+    for (int c = 0; c < chunk; ++c) acc = acc + term[l * chunk + c];
+    part[l] = acc;
+  }
+  for (int o = lanes / 2; o >= 1; o /= 2) {
+    T nxt[NS];
+    for (int l = 0; l < lanes; ++l) nxt[l] = part[l] + part[l ^ o];
+    for (int l = 0; l < lanes; ++l) part[l] = nxt[l];
+  }
+  return part[0];
+}
+
+template <typename T>
+void exact_solve(const T* Y, const T* rm, T* p) {
+  // kernel matrix: row s: l_s p_{s-1} + m_s p_s + p_{s+1} = Y_s,
+  // l_s = 1 for s < 254 else 0 (reference include/cochlea.cuh:13736).
+  double m[NS], l[NS], u[NS], v[NS], r[NS];
+  for (int s = 0; s < NS; ++s) {
+    m[s] = 1.0 / (double)rm[s];
+    u[s] = 1.0;
+    v[s] = (double)Y[s];
+  }
+  // tridiag.cpp convention: row i uses l[i-1]
+  for (int s = 0; s < NS; ++s) l[s] = (s + 1 < NS - 2) ? 1.0 : 0.0;
+  orc_thomas(m, l, u, v, r, NS);
+  for (int s = 0; s < NS; ++s) p[s] = (T)r[s];
+}
+
+template <typename T, typename TO>
+void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scalars& sc,
+             const orc_unit& un, const float* in, TO* out, int32_t* failed,
+             orc_unit_stats* st) {
+  using A = Ar<T>;
+  T x0[NS] = {}, v0[NS] = {}, a0[NS] = {}, y0[NS] = {}, u0[NS] = {}, ps0[NS] = {}, dp0[NS] = {};
+  T x[NS] = {}, v[NS] = {}, a[NS] = {}, y[NS] = {}, u[NS] = {}, ps[NS] = {}, dp[NS] = {};
+  T Ptm[NS] = {}, p[NS] = {}, Y[NS] = {}, G[NS] = {}, aref[NS] = {}, dv[NS] = {},
+    flt[NS] = {}, tmp[NS] = {}, Yrm[NS] = {};
+  T w0 = 0, wd0 = 0, wdd0 = 0, w = 0, wd = 0, wdd = 0;
+  const T ratio = (T)(sc.alpha_l / sc.alpha_s);  // float division as the host does it
+  const T nas = -(T)sc.alpha_s, al = (T)sc.alpha_l;
+  const T e1 = (T)sc.eta_1, e2 = (T)sc.eta_2, nw = -(T)sc.w_ohc;
+  const T ar = (T)sc.alpha_r;
+  const T dx = (T)sc.delta_x;
+  const T dx2 = dx * dx, dxa0 = dx * (T)sc.a0;
+  const T na1 = -(T)sc.a1, na2 = -(T)sc.a2, Gme = (T)sc.Gme, sow = (T)sc.sigma_ow;
+  const T mtt = (T)un.mtt, mmspt = (T)un.mmspt;
+  const T dtmin = (T)sc.dt_min, dtmax = (T)sc.dt_max;
+  const double Tout = (double)sc.time_step_out;
+  const double invTs = 1.0 / (double)sc.Ts;
+  const float* inb = in + un.in_base;
+  TO* outb = out ? out + un.out_base * (int64_t)NS : nullptr;
+  int32_t* fb = failed ? failed + un.out_base : nullptr;
+
+  T dt = (T)sc.time_step;
+  double tau = 0.0;
+  int64_t n = un.start;
+  T sx0 = (T)inb[n], sx1 = (T)inb[n + 1];
+  int fail_flag = 0;
+  int64_t sub_in_sample = 0;
+  orc_unit_stats S = {};
+  while (n < un.end) {
+    if (++sub_in_sample > sc.max_substeps_per_sample) {
+      S.status = 1;
+      break;
+    }
+    int out_loop = 0, reset = 1, another = 1;
+    const T delta = std::is_same<T, float>::value ? (T)(float)(tau * invTs) : (T)(tau * invTs);
+    const T smp = A::fma(sx1, delta, sx0 * ((T)1 - delta));
+    while (another) {
+      for (int s = 0; s < NS; ++s) aref[s] = a[s];
+      if (out_loop == 0 || reset) {
+        out_loop = 0;
+        for (int s = 0; s < NS; ++s) {
+          y[s] = A::fma(u0[s], dt, y0[s]);
+          T vn = A::fma(a0[s], dt, v0[s]);
+          dv[s] = A::abs(vn - v[s]);
+          v[s] = vn;
+          x[s] = A::fma((v0[s] + vn) * (T)0.5, dt, x0[s]);
+          ps[s] = A::fma(dp0[s], dt, ps0[s]);
+        }
+        w = A::fma(wd0, dt, w0);
+        wd = A::fma(wdd0, dt, wd0);
+      } else {
+        for (int s = 0; s < NS; ++s) {
+          T vn = A::fma((a0[s] + a[s]) * (T)0.5, dt, v0[s]);
+          dv[s] = A::abs(vn - v[s]);
+          v[s] = vn;
+          x[s] = A::fma((v0[s] + vn) * (T)0.5, dt, x0[s]);
+          y[s] = A::fma((u0[s] + u[s]) * (T)0.5, dt, y0[s]);
+          ps[s] = A::fma((dp0[s] + dp[s]) * (T)0.5, dt, ps0[s]);
+        }
+        w = A::fma((wd0 + wd) * (T)0.5, dt, w0);
+        wd = A::fma((wdd0 + wdd) * (T)0.5, dt, wd0);
+      }
+      for (int s = 0; s < NS; ++s) {
+        T d = y[s] - x[s];
+        T Pohc = gs[s] * d;
+        if (out_loop < 2) {
+          T t = A::tanh(ratio * ps[s]);
+          T dL = nas * t;
+          T Aa = al * A::fma(t, t, (T)-1);
+          T N1 = A::fma(e1, d, A::fma(e2, v[s], nw * ps[s]));
+          T N = A::fma(md.S_tm[s], dL, (N1 * md.R_tm[s]) * Aa);
+          T Pp = A::fma(md.S_tm[s], y[s], Pohc);
+          T num = A::fma(-gam[s], N, Pp);
+          T den = md.R_tm[s] * A::fma(gam[s] * Aa, e2, (T)-1);
+          u[s] = num / den;
+          Ptm[s] = A::fma(md.R_tm[s], u[s], md.S_tm[s] * y[s]);
+        }
+        T g = md.R[s] * A::fma(ar, v[s] * v[s], (T)1);
+        g = A::fma(g, v[s], md.S[s] * x[s]);
+        G[s] = -g - Ptm[s];
+        if (s == 0) {
+          Y[s] = dxa0 * A::fma(na1, w, A::fma(na2, wd, Gme * smp));
+        } else if (s == NS - 1) {
+          Y[s] = 0;
+        } else {
+          Y[s] = (dx2 * G[s]) * md.Q[s];
+        }
+      }
+      int J = out_loop < 2 ? sc.jacobi_slow : sc.jacobi_fast;
+      if (sc.jacobi_mode == 1) {
+        exact_solve<T>(Y, md.rm, p);
+      } else {
+        // p_s <- (Y_s - (l_s p_{s-1} + p_{s+1})) / m_s, evaluated as
+        // fma(-t, 1/m_s, Y_s/m_s) with Y_s/m_s formed once per iteration.
+        for (int s = 0; s < NS; ++s) Yrm[s] = Y[s] * md.rm[s];
+        for (int it = 0; it < J; ++it) {
+          for (int s = 0; s < NS; ++s) {
+            T pm1 = s > 0 ? p[s - 1] : (T)0;
+            T pp1 = s < NS - 1 ? p[s + 1] : (T)0;
+            T t = s < NS - 2 ? pm1 + pp1 : pp1;
+            tmp[s] = A::fma(-t, md.rm[s], Yrm[s]);
+          }
+          for (int s = 0; s < NS; ++s) p[s] = tmp[s];
+        }
+        S.sweeps += J;
+      }
+      for (int s = 0; s < NS; ++s) {
+        a[s] = (p[s] + G[s]) * md.invM[s];
+        T d = y[s] - x[s];
+        dp[s] = A::fma(e1, d, A::fma(e2, u[s] - v[s], nw * ps[s]));
+      }
+      wdd = A::fma(na1, w, A::fma(na2, wd, A::fma(Gme, smp, p[0]))) / sow;
+      if (reset == 0) {
+        T ea = 0;
+        for (int s = 0; s < NS; ++s) {
+          ea = A::max(ea, A::abs(aref[s] - a[s]));
+          flt[s] = dv[s] - A::max(mtt, v[s] * dt);
+        }
+        T ev = tree_sum<T>(dv, sc.red_lanes);
+        T F = tree_sum<T>(flt, sc.red_lanes);
+        T L = ev > mmspt ? (ea * dt) / ev : (T)0;
+        if (L > (T)6) {
+          dt = dt * (T)0.5;
+          if (dt < dtmin) dt = dtmin;
+          another = 0;
+          reset = 1;
+        } else if (F > (T)0) {
+          another = 1;
+          reset = 0;
+        } else if (L < (T)0.5) {
+          dt = dt * (T)2;
+          if (dt > dtmax) dt = dtmax;
+          another = 0;
+          reset = 1;
+        } else {
+          another = 1;
+          reset = 0;
+        }
+      } else {
+        another = 1;
+        reset = 0;
+      }
+      ++out_loop;
+      if (out_loop >= sc.max_outer) {
+        another = 0;
+        reset = 1;
+        fail_flag = 1;
+      }
+    }
+    S.substeps += 1;
+    S.iterations += out_loop;
+    if (tau > Tout) {
+      tau -= Tout;
+      sx0 = sx1;
+      sx1 = (T)inb[n + 2];
+      if (n >= un.out_first) {
+        if (outb)
+          for (int s = 0; s < NS; ++s) outb[n * NS + s] = (TO)v[s];
+        if (fb) fb[n] = fail_flag;
+        S.written_samples += 1;
+        S.failed_samples += fail_flag;
+      }
+      fail_flag = 0;
+      sub_in_sample = 0;
+      ++n;
+    }
+    for (int s = 0; s < NS; ++s) {
+      x0[s] = x[s];
+      v0[s] = v[s];
+      a0[s] = a[s];
+      ps0[s] = ps[s];
+      dp0[s] = dp[s];
+      u0[s] = u[s];
+      y0[s] = y[s];
+    }
+    w0 = w;
+    wd0 = wd;
+    wdd0 = wdd;
+    tau += (double)dt;
+  }
+  if (st) *st = S;
+}
+
+template <typename T, typename TO>
+void bm_run(const float* secp, const float* gamma, const orc_bm_scalars* sc,
+            const orc_unit* units, int n_units, const float* in, TO* out, int32_t* failed,
+            orc_unit_stats* stats, int n_threads) {
+  // secp: float[8][256] = invM, rm, R, S, Q, S_ohc, S_tm, R_tm
+  BMModel<T> md;
+  for (int s = 0; s < NS; ++s) {
+    md.invM[s] = (T)secp[0 * NS + s];
+    md.rm[s] = (T)secp[1 * NS + s];
+    md.R[s] = (T)secp[2 * NS + s];
+    md.S[s] = (T)secp[3 * NS + s];
+    md.Q[s] = (T)secp[4 * NS + s];
+    md.S_ohc[s] = (T)secp[5 * NS + s];
+    md.S_tm[s] = (T)secp[6 * NS + s];
+    md.R_tm[s] = (T)secp[7 * NS + s];
+  }
+  std::atomic<int> next(0);
+  auto worker = [&]() {
+    T gam[NS], gs[NS];
+    for (;;) {
+      int i = next.fetch_add(1);
+      if (i >= n_units) break;
+      const orc_unit& un = units[i];
+      for (int s = 0; s < NS; ++s) {
+        gam[s] = (T)gamma[(int64_t)un.profile * NS + s];
+        gs[s] = gam[s] * md.S_ohc[s];
+      }
+      bm_unit<T, TO>(md, gam, gs, *sc, un, in, out, failed, stats ? stats + i : nullptr);
+    }
+  };
+  n_threads = std::max(1, n_threads);
+  if (n_threads == 1) {
+    worker();
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t) th.emplace_back(worker);
+    for (auto& t : th) t.join();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_bm_run_f32(const float* secp, const float* gamma, const orc_bm_scalars* sc,
+                    const orc_unit* units, int n_units, const float* in, float* out,
+                    int32_t* failed, orc_unit_stats* stats, int n_threads) {
+  bm_run<float, float>(secp, gamma, sc, units, n_units, in, out, failed, stats, n_threads);
+}
+
+void orc_bm_run_f64(const float* secp, const float* gamma, const orc_bm_scalars* sc,
+                    const orc_unit* units, int n_units, const float* in, double* out,
+                    int32_t* failed, orc_unit_stats* stats, int n_threads) {
+  bm_run<double, double>(secp, gamma, sc, units, n_units, in, out, failed, stats, n_threads);
+}
+
+// ---------------------------------------------------------------------------
+// IHC + lambda of one frame, reference mixed precision (double taps and
+// accumulators, float buffers): src/cochlea.cu:2712-2730 (FIR with the
+// decoupled look-back limit), 2980-2988 (dS), 3291-3317 (IHC log),
+// 3365-3408 (lambda).
+//   v       : float [rows][256] BM velocity of the frame
+//   seg     : decoupled interval length (Time_Block_Length nodes x Decouple_Filter)
+//   frdp    : Time_Block_Length nodes x Time_Blocks (final_regular_division_position)
+//   total   : rows rounded up to 64 (calcTime)
+//   lam_rows: rows for which lambda is produced (Time_Block_Length nodes x Time_Blocks)
+//   ihc     : float [rows][256] IHC output; lam: float [3][lam_stride][256]
+// ---------------------------------------------------------------------------
+static inline int fir_taps_used(int k, int seg, int frdp, int total, int taps) {
+  int sg = k / (frdp - 1);
+  sg = sg * total + (1 - sg) * seg;
+  int lim = (k + 1) % sg;
+  return lim < taps ? lim : taps;
+}
+
+void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int lam_rows,
+                    const double* ac_taps, int n_ac, const double* dc_taps, int n_dc,
+                    double scale, double eta_ac, double eta_dc, const double* ihc_damage,
+                    const float* aihc /*[3][256]*/, const float* spont /*[3]*/,
+                    double lambda_sat, float* ihc, float* lam, int64_t lam_stride,
+                    int fp64 /*0: reference mixed precision, 1: all double*/) {
+  std::vector<double> ac((size_t)rows * NS), ds((size_t)rows * NS);
+  for (int k = 0; k < rows; ++k) {
+    int tu = fir_taps_used(k, seg, frdp, total, n_ac);
+    for (int s = 0; s < NS; ++s) {
+      double acc = 0.0;
+      for (int i = 0; i < tu; ++i) acc = acc + ac_taps[i] * (double)v[(size_t)(k - i) * NS + s];
+      if (fp64) {
+        ac[(size_t)k * NS + s] = acc;
+        double ms = (double)v[(size_t)k * NS + s] * scale - acc;
+        ds[(size_t)k * NS + s] = ms * ms;
+      } else {
+        float acf = (float)acc;
+        ac[(size_t)k * NS + s] = acf;
+        float ms = fmaf(v[(size_t)k * NS + s], (float)scale, -acf);
+        ds[(size_t)k * NS + s] = (double)(ms * ms);
+      }
+    }
+  }
+  for (int k = 0; k < rows; ++k) {
+    int tu = fir_taps_used(k, seg, frdp, total, n_dc);
+    for (int s = 0; s < NS; ++s) {
+      double acc = 0.0;
+      for (int i = 0; i < tu; ++i) acc = acc + dc_taps[i] * ds[(size_t)(k - i) * NS + s];
+      double pre;
+      if (fp64) {
+        pre = ac[(size_t)k * NS + s] * eta_ac + acc * eta_dc;
+      } else {
+        float dcf = (float)acc;
+        pre = (double)fmaf((float)ac[(size_t)k * NS + s], (float)eta_ac,
+                           (float)((double)dcf * eta_dc));
+      }
+      ihc[(size_t)k * NS + s] = (float)std::log10(std::fmax(ihc_damage[s] * pre, 0.0) + 1e-20);
+    }
+  }
+  for (int j = 0; j < 3; ++j) {
+    double sp = (double)spont[j];
+    for (int k = 0; k < lam_rows; ++k) {
+      for (int s = 0; s < NS; ++s) {
+        double A = (double)aihc[j * NS + s];
+        double base = std::fmin(lambda_sat, std::fmax(A * (double)ihc[(size_t)k * NS + s], sp));
+        double val = s != 0 ? base : sp;
+        lam[(size_t)j * lam_stride * NS + (size_t)k * NS + s] = (float)val;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// JND (Eq. 17-24): src/cochlea.cu:3741-3944 and
+// src/AudioGramCreator.cpp:454-508.  lam: float [3][lam_stride][256] with
+// interval i starting at row i*interval_nodes.  ref_of[i] is the reference
+// interval of i (== i for a reference interval).  Outputs (double) F_RA and
+// FisherAI_sum [3][n_int].  mode 0: reference float arithmetic; 1: FP64 sums.
+// ---------------------------------------------------------------------------
+void orc_jnd(const float* lam, int64_t lam_stride, int n_int, int interval_nodes, int head,
+             int len, const double* dA, const int32_t* ref_of, const double* nIHC,
+             const float* W, double Fs, double delta_alpha_len_factor, double* F_RA,
+             double* F_AI, int mode) {
+  std::vector<double> MR((size_t)3 * n_int * NS);
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < n_int; ++i)
+      for (int s = 0; s < NS; ++s) {
+        const float* base = lam + (size_t)j * lam_stride * NS +
+                            ((size_t)i * interval_nodes + head) * NS + s;
+        double acc = base[0];
+        for (int t = 1; t < len; ++t) acc = acc + base[(size_t)t * NS];
+        if (mode == 0)
+          MR[((size_t)j * n_int + i) * NS + s] = (double)((float)acc / (float)len);
+        else
+          MR[((size_t)j * n_int + i) * NS + s] = acc / (double)len;
+      }
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < n_int; ++i) {
+      int r = ref_of[i];
+      if (mode == 0) {
+        float T = (float)(delta_alpha_len_factor / Fs);
+        float Tl = (float)((double)(float)len / Fs);
+        float dAf = (float)dA[i];
+        float ai[NS], ra[NS];
+        for (int s = 0; s < NS; ++s) {
+          float mr = (float)MR[((size_t)j * n_int + i) * NS + s];
+          float mrr = (float)MR[((size_t)j * n_int + r) * NS + s];
+          float dMR = (mr - mrr) / dAf;
+          const float* c = lam + (size_t)j * lam_stride * NS + ((size_t)i * interval_nodes + head) * NS + s;
+          const float* rf = lam + (size_t)j * lam_stride * NS + ((size_t)r * interval_nodes + head) * NS + s;
+          float acc = 0.0f;
+          for (int t = 0; t < len; ++t) {
+            float rl = rf[(size_t)t * NS], cl = c[(size_t)t * NS];
+            float dl = dAf > 0 ? (cl - rl) / dAf : 0.0f;
+            float pre = (float)((double)(dl * dl) / (Fs * (double)rl));
+            acc += pre;
+          }
+          float rs = 1.0f / sqrtf(acc);
+          ai[s] = (float)((double)(T / Tl) * nIHC[s] / (double)(rs * rs));
+          float crlb = 1.0f / sqrtf(((T / mrr) * dMR) * dMR);
+          ra[s] = (float)(nIHC[s] / (double)(crlb * crlb));
+        }
+        for (int t = NS / 2; t >= 1; t >>= 1)
+          for (int s = 0; s < t; ++s) {
+            ai[s] = ai[s] + ai[s + t];
+            ra[s] = ra[s] + ra[s + t];
+          }
+        F_AI[(size_t)j * n_int + i] = (double)(ai[0] * W[j]);
+        F_RA[(size_t)j * n_int + i] = (double)(ra[0] * W[j]);
+      } else {
+        double T = delta_alpha_len_factor / Fs;
+        double Tl = (double)len / Fs;
+        double dAd = dA[i];
+        double sai = 0.0, sra = 0.0;
+        for (int s = 0; s < NS; ++s) {
+          double mr = MR[((size_t)j * n_int + i) * NS + s];
+          double mrr = MR[((size_t)j * n_int + r) * NS + s];
+          double dMR = (mr - mrr) / dAd;
+          const float* c = lam + (size_t)j * lam_stride * NS + ((size_t)i * interval_nodes + head) * NS + s;
+          const float* rf = lam + (size_t)j * lam_stride * NS + ((size_t)r * interval_nodes + head) * NS + s;
+          double acc = 0.0;
+          for (int t = 0; t < len; ++t) {
+            double rl = rf[(size_t)t * NS], cl = c[(size_t)t * NS];
+            double dl = dAd > 0 ? (cl - rl) / dAd : 0.0;
+            acc += dl * dl / (Fs * rl);
+          }
+          sai += (T / Tl) * nIHC[s] * acc;
+          sra += nIHC[s] * (T / mrr) * dMR * dMR;
+        }
+        F_AI[(size_t)j * n_int + i] = sai * (double)W[j];
+        F_RA[(size_t)j * n_int + i] = sra * (double)W[j];
+      }
+    }
+}
+
+// Final JND in dB (src/AudioGramCreator.cpp:478-504, include/params.h:328-331).
+double orc_jnd_db(double fisher_sum, double spl_ref, double max_db) {
+  double pa = 1.0 / std::sqrt(fisher_sum);
+  double max_pa = std::pow(10.0, max_db / 20.0) * spl_ref;
+  if (std::isinf(pa) || pa > max_pa) return max_db;
+  return 20.0 * std::log10(pa / spl_ref);
+}
+
+// ---------------------------------------------------------------------------
+// Input generation (src/cochlea.cu:4070-4103): x[p][n] for n < interval_len.
+// prof: double[n_prof][3] = dA, Wn, frequency.
+// ---------------------------------------------------------------------------
+void orc_input_gen(const double* prof, int n_prof, const float* wn, int interval_len,
+                   int head, float Fs, double wn_dc, double wn_norm, double sig_norm,
+                   float* out) {
+  const float PIf = 3.141592653589793f;
+  const float two_pi = 2 * PIf;
+  for (int p = 0; p < n_prof; ++p) {
+    double dA = prof[p * 3 + 0], Wn = prof[p * 3 + 1], f = prof[p * 3 + 2];
+    for (int n = 0; n < interval_len; ++n) {
+      double t = (double)(n - head) / (double)Fs;
+      double cut = (double)two_pi * f * t;
+      double sum = dA * std::cos(cut) / sig_norm;
+      sum = sum + Wn * ((double)wn[n] - wn_dc) / wn_norm;
+      out[(size_t)p * interval_len + n] = (float)sum;
+    }
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,177 @@
+"""Test infrastructure: ctypes binding of the CPU oracle (oracle/cochlea_oracle.cpp).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+arm may import this module.  It builds the oracle library on first use.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libcochlea_oracle.so"
+
+UNIT_DTYPE = np.dtype([
+    ("in_base", "<i8"), ("out_base", "<i8"), ("start", "<i4"), ("out_first", "<i4"),
+    ("end", "<i4"), ("profile", "<i4"), ("mtt", "<f4"), ("mmspt", "<f4"),
+])
+STATS_DTYPE = np.dtype([
+    ("substeps", "<i8"), ("iterations", "<i8"), ("sweeps", "<i8"),
+    ("failed_samples", "<i4"), ("written_samples", "<i4"), ("status", "<i4"), ("pad_", "<i4"),
+])
+
+
+class OrcScalars(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "w_ohc", "time_step", "time_step_out", "delta_x", "alpha_r", "Ts",
+        "alpha_l", "alpha_s", "Gme", "a0", "a1", "a2", "sigma_ow", "eta_1", "eta_2",
+        "dt_min", "dt_max")] + [(n, C.c_int32) for n in (
+            "jacobi_fast", "jacobi_slow", "max_outer", "red_lanes", "jacobi_mode",
+            "max_substeps_per_sample")]
+
+
+_lib = None
+_p = C.c_void_p
+
+
+def build(force: bool = False) -> Path:
+    src = HERE / "cochlea_oracle.cpp"
+    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["sh", str(HERE / "build.sh")], check=True)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        lib.orc_tanhf.restype = C.c_float
+        lib.orc_tanhf.argtypes = [C.c_float]
+        lib.orc_model_setup.argtypes = [_p] * 11
+        lib.orc_thomas.argtypes = [_p, _p, _p, _p, _p, C.c_int]
+        lib.orc_block_partition.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, _p, _p, _p]
+        for nm in ("orc_bm_run_f32", "orc_bm_run_f64"):
+            getattr(lib, nm).argtypes = [_p, _p, C.POINTER(OrcScalars), _p, C.c_int, _p, _p,
+                                         _p, _p, C.c_int]
+        lib.orc_ihc_lambda.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       _p, C.c_int, _p, C.c_int, C.c_double, C.c_double,
+                                       C.c_double, _p, _p, _p, C.c_double, _p, _p, C.c_int64,
+                                       C.c_int]
+        lib.orc_jnd.argtypes = [_p, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _p, _p, _p,
+                                _p, C.c_double, C.c_double, _p, _p, C.c_int]
+        lib.orc_jnd_db.restype = C.c_double
+        lib.orc_jnd_db.argtypes = [C.c_double, C.c_double, C.c_double]
+        lib.orc_input_gen.argtypes = [_p, C.c_int, _p, C.c_int, C.c_int, C.c_float,
+                                      C.c_double, C.c_double, C.c_double, _p]
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def scalars_from(sc) -> OrcScalars:
+    """Copies a product BMScalars (same field list) into the oracle's struct."""
+    o = OrcScalars()
+    for name, _ in OrcScalars._fields_:
+        setattr(o, name, getattr(sc, name))
+    return o
+
+
+def tanhf(x: float) -> float:
+    return load().orc_tanhf(x)
+
+
+def model_setup():
+    arrs = [np.zeros(256, np.float64) for _ in range(10)]
+    scal = np.zeros(16, np.float64)
+    load().orc_model_setup(*[_ptr(a) for a in arrs], _ptr(scal))
+    names = ["M", "R", "S", "Q", "S_ohc", "S_tm", "R_tm", "diag_m", "diag_l", "diag_u"]
+    d = dict(zip(names, arrs))
+    d["scal"] = scal
+    return d
+
+
+def thomas(m, l, u, v):
+    n = len(v)
+    res = np.zeros(n, np.float64)
+    load().orc_thomas(*[_ptr(np.ascontiguousarray(a, np.float64)) for a in (m, l, u, v)],
+                      _ptr(res), n)
+    return res
+
+
+def block_partition(time_blocks, samples_p1, overlap, decouple):
+    st = np.zeros(time_blocks, np.int32)
+    of = np.zeros(time_blocks, np.int32)
+    en = np.zeros(time_blocks, np.int32)
+    load().orc_block_partition(time_blocks, samples_p1, overlap, decouple, _ptr(st), _ptr(of),
+                               _ptr(en))
+    return st, of, en
+
+
+def bm_run(secp, gamma, sc, units, inp, out_rows, fp64=False, threads=None, jacobi_mode=None):
+    """Runs the BM step over `units`; returns (velocity[out_rows,256], failed, stats)."""
+    osc = scalars_from(sc)
+    if jacobi_mode is not None:
+        osc.jacobi_mode = jacobi_mode
+    units = np.ascontiguousarray(units).view(UNIT_DTYPE)
+    secp = np.ascontiguousarray(secp, np.float32)
+    gamma = np.ascontiguousarray(gamma, np.float32)
+    inp = np.ascontiguousarray(inp, np.float32)
+    out = np.zeros((out_rows, 256), np.float64 if fp64 else np.float32)
+    failed = np.zeros(out_rows, np.int32)
+    stats = np.zeros(len(units), STATS_DTYPE)
+    fn = load().orc_bm_run_f64 if fp64 else load().orc_bm_run_f32
+    fn(_ptr(secp), _ptr(gamma), C.byref(osc), _ptr(units), len(units), _ptr(inp), _ptr(out),
+       _ptr(failed), _ptr(stats), threads or (os.cpu_count() or 1))
+    return out, failed, stats
+
+
+def ihc_lambda(v, seg, frdp, total, lam_rows, ac_taps, dc_taps, scale, eta_ac, eta_dc,
+               ihc_damage, aihc, spont, lambda_sat, fp64=False):
+    v = np.ascontiguousarray(v, np.float32)
+    rows = v.shape[0]
+    ihc = np.zeros((rows, 256), np.float32)
+    lam = np.zeros((3, lam_rows, 256), np.float32)
+    ac = np.ascontiguousarray(ac_taps, np.float64)
+    dc = np.ascontiguousarray(dc_taps, np.float64)
+    load().orc_ihc_lambda(_ptr(v), rows, seg, frdp, total, lam_rows, _ptr(ac), len(ac),
+                          _ptr(dc), len(dc), scale, eta_ac, eta_dc,
+                          _ptr(np.ascontiguousarray(ihc_damage, np.float64)),
+                          _ptr(np.ascontiguousarray(aihc, np.float32)),
+                          _ptr(np.ascontiguousarray(spont, np.float32)), lambda_sat,
+                          _ptr(ihc), _ptr(lam), lam_rows, 1 if fp64 else 0)
+    return ihc, lam
+
+
+def jnd(lam, n_int, interval_nodes, head, length, dA, ref_of, nIHC, W, Fs, factor, fp64=True):
+    lam = np.ascontiguousarray(lam, np.float32)
+    stride = lam.shape[1]
+    F_RA = np.zeros((3, n_int), np.float64)
+    F_AI = np.zeros((3, n_int), np.float64)
+    load().orc_jnd(_ptr(lam), stride, n_int, interval_nodes, head, length,
+                   _ptr(np.ascontiguousarray(dA, np.float64)),
+                   _ptr(np.ascontiguousarray(ref_of, np.int32)),
+                   _ptr(np.ascontiguousarray(nIHC, np.float64)),
+                   _ptr(np.ascontiguousarray(W, np.float32)), Fs, factor, _ptr(F_RA), _ptr(F_AI),
+                   1 if fp64 else 0)
+    return F_RA, F_AI
+
+
+def jnd_db(fisher_sum, spl_ref=2e-5, max_db=150.0):
+    return load().orc_jnd_db(float(fisher_sum), spl_ref, max_db)
+
+
+def input_gen(prof, wn, interval_len, head, Fs, wn_dc, wn_norm, sig_norm):
+    prof = np.ascontiguousarray(prof, np.float64)
+    wn = np.ascontiguousarray(wn, np.float32)
+    out = np.zeros((prof.shape[0], interval_len), np.float32)
+    load().orc_input_gen(_ptr(prof), prof.shape[0], _ptr(wn), interval_len, head, Fs, wn_dc,
+                         wn_norm, sig_norm, _ptr(out))
+    return out

@@ -1,0 +1,27 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def mv():
+    from cochlearmodel_gb300 import model
+    return model.ModelVectors.build()
+
+
+@pytest.fixture(scope="session")
+def bm_solver():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cochlearmodel_gb300.solver import BMSolver
+    return BMSolver("cuda:0")

@@ -1,0 +1,77 @@
+"""Host logic of the product against the oracle, no GPU needed:
+model vectors (row a4), the block partition (row a2), section packing."""
+import numpy as np
+import pytest
+
+from cochlearmodel_gb300 import model
+from oracle import oracle as orc
+
+
+def test_model_vectors_match_oracle(mv):
+    o = orc.model_setup()
+    for k in ("M", "R", "S", "Q", "S_ohc", "S_tm", "R_tm", "diag_m", "diag_l", "diag_u"):
+        assert np.array_equal(getattr(mv, k), o[k]), k
+    assert np.array_equal(mv.scal, o["scal"])
+
+
+def test_model_vectors_closed_form(mv):
+    """KAT: M0 e^{M1 x}, R0 e^{R1 x}, S0 e^{S1 x} at s = 0, 128, 255."""
+    dx = 3.5 / 256
+    for s in (0, 128, 255):
+        x = dx * s
+        assert mv.M[s] == pytest.approx(1.286e-6 * np.exp(1.5 * x), rel=1e-6)
+        assert mv.R[s] == pytest.approx(0.25 * np.exp(-0.06 * x), rel=1e-6)
+        assert mv.S[s] == pytest.approx(1.282e4 * np.exp(-1.5 * x), rel=1e-6)
+        assert mv.Q[s] == pytest.approx(2 * 1.0 * 0.003 / (0.5 * mv.M[s]), rel=1e-6)
+    assert mv.diag_m[255] == 1.0 and mv.diag_l[254] == 0.0 and mv.diag_l[255] == 0.0
+    assert mv.diag_m[0] == pytest.approx(-(1 + dx * 0.024), rel=1e-6)
+
+
+@pytest.mark.parametrize("tb,dec,blk,ov", [(1, 1, 0.05, 0.005), (8, 8, 0.01, 0.005),
+                                          (16, 8, 0.01, 0.005), (6, 2, 0.002, 0.001),
+                                          (5, 0, 0.004, 0.002), (4, 1, 0.003, 0.001)])
+def test_block_partition_matches_oracle(tb, dec, blk, ov):
+    cfg = model.RunConfig(Time_Blocks=tb, Decouple_Filter=dec, Time_Block_Length=blk,
+                          Overlap_Time=ov)
+    args = (tb, cfg.total_time_nodes_p1(), cfg.calc_overlap_nodes(), dec)
+    got = model.block_partition(*args)
+    want = orc.block_partition(*args)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_block_partition_decoupled_semantics():
+    """Decouple_Filter=8, 10 ms blocks at 100 kHz: a group opens with a block
+    that writes from its start, mid-group blocks warm up for the overlap, and
+    the group's last block stops at the group boundary."""
+    cfg = model.RunConfig(Time_Blocks=16, Decouple_Filter=8, Time_Block_Length=0.01)
+    st, of, en = model.block_partition(16, cfg.total_time_nodes_p1(), 500, 8)
+    N = 1000
+    assert list(st) == [b * N for b in range(16)]
+    assert of[0] == 0 and of[8] == 8 * N
+    assert of[1] == N + 500 and en[1] == 2 * N + 500
+    assert en[7] == 8 * N and en[15] == 16 * N + 500
+
+
+def test_derived_node_counts():
+    cfg = model.RunConfig(Time_Block_Length=0.01, Time_Blocks=8, Overlap_Time=0.005)
+    assert cfg.calc_time_block_nodes() == 1000
+    assert cfg.calc_overlap_nodes() == 500
+    assert cfg.total_time_nodes_p1() == 500 + 9000
+    assert cfg.cuda_iterations_per_kernel() == 10
+    assert cfg.time_step_out() == np.float32(1e-6) * np.float32(10)
+
+
+def test_expand_vector():
+    v = model.expand_vector([1.0, 2.0, 3.0])
+    assert v.shape == (256,)
+    assert (v[:86] == 1).all() and (v[86:171] == 2).all() and (v[171:] == 3).all()
+    assert (model.expand_vector(0.5) == 0.5).all()
+
+
+def test_section_packing(mv):
+    sp = mv.section_params()
+    assert sp.dtype == np.float32 and sp.shape == (8, 256)
+    assert sp[0, 10] == np.float32(1.0) / np.float32(mv.M[10])
+    assert sp[1, 0] == np.float32(1.0) / np.float32(mv.diag_m[0])
+    assert sp[1, 255] == 1.0

@@ -1,0 +1,75 @@
+"""Known-answer and property tests of the CPU oracle itself."""
+import numpy as np
+import pytest
+
+from cochlearmodel_gb300 import model
+from oracle import oracle as orc
+from tests import cases
+
+
+def test_own_tanh_accuracy():
+    """The project's float tanh stays within 2 ulp of the exact value."""
+    xs = np.concatenate([np.linspace(-12, 12, 20001), np.linspace(-0.6, 0.6, 20001),
+                         np.geomspace(1e-8, 1e-1, 2001), [0.55, 0.5499999, 20.0, 25.0]])
+    xs = xs.astype(np.float32)
+    got = np.array([orc.tanhf(float(x)) for x in xs], np.float32)
+    exact = np.tanh(xs.astype(np.float64))
+    ulp = np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)
+    err = np.abs(got.astype(np.float64) - exact) / ulp
+    assert err.max() <= 2.0, (xs[err.argmax()], err.max())
+    assert orc.tanhf(0.0) == 0.0 and orc.tanhf(30.0) == 1.0 and orc.tanhf(-30.0) == -1.0
+
+
+def test_thomas_matches_dense_solve():
+    o = orc.model_setup()
+    m, l, u = o["diag_m"], o["diag_l"], o["diag_u"]
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal(256)
+    A = np.diag(m) + np.diag(u[:-1], 1) + np.diag(l[:-1], -1)
+    assert np.allclose(orc.thomas(m, l, u, v), np.linalg.solve(A, v), rtol=1e-9, atol=1e-12)
+
+
+def test_fixed_sweeps_approach_exact_solution(mv):
+    """More Jacobi sweeps move the FP64 solution toward the exact tridiagonal
+    solve; the default 20/2 sweeps stay within 1e-3 of it."""
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=1.0)
+    secp = mv.section_params()
+    ex, _, _ = orc.bm_run(secp, gamma, sc, units, x, rows, fp64=True, jacobi_mode=1)
+    e = units["end"][0]
+    scale = np.abs(ex[:e]).max()
+    errs = []
+    for slow, fast in ((20, 2), (200, 50)):
+        sc.jacobi_slow, sc.jacobi_fast = slow, fast
+        v, _, _ = orc.bm_run(secp, gamma, sc, units, x, rows, fp64=True)
+        errs.append(np.abs(v[:e] - ex[:e]).max() / scale)
+    assert errs[1] < errs[0] < 1e-3
+
+
+def test_fp32_vs_fp64_small(mv):
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=2.0)
+    secp = mv.section_params()
+    v32, f32, st32 = orc.bm_run(secp, gamma, sc, units, x, rows)
+    v64, f64, st64 = orc.bm_run(secp, gamma, sc, units, x, rows, fp64=True)
+    e = units["end"][0]
+    rel = np.abs(v32[:e] - v64[:e]).max() / np.abs(v64[:e]).max()
+    assert rel < 1e-3
+    assert st32["written_samples"][0] == units["end"][0] - units["out_first"][0]
+
+
+def test_reduction_width_changes_only_rounding(mv):
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=1.0)
+    secp = mv.section_params()
+    a, _, _ = orc.bm_run(secp, gamma, sc, units, x, rows)
+    sc.red_lanes = 64
+    b, _, _ = orc.bm_run(secp, gamma, sc, units, x, rows)
+    e = units["end"][0]
+    assert np.abs(a[:e] - b[:e]).max() <= 1e-4 * np.abs(a[:e]).max()
+
+
+def test_threads_do_not_change_results(mv):
+    case = cases.decoupled_sweep(mv, n_signals=2, decouple=2, block_ms=1.0, overlap_ms=0.5)
+    cfg, sc, gamma, units, x, rows = case
+    secp = mv.section_params()
+    a = orc.bm_run(secp, gamma, sc, units, x, rows, threads=1)[0]
+    b = orc.bm_run(secp, gamma, sc, units, x, rows, threads=4)[0]
+    assert np.array_equal(a, b)
