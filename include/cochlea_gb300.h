@@ -131,6 +131,12 @@ int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
 int cgb_check_units(const cgb_unit* units, int n_units, int n_profiles, int64_t in_len,
                     int64_t out_rows);
 
+/* Launch shape of the BM kernel (register bound / CTAs per SM); 0 is the
+ * default, cgb_bm_launch_shape_count() shapes are built.  Results do not
+ * depend on the shape. */
+int cgb_bm_set_launch_shape(int shape);
+int cgb_bm_launch_shape_count(void);
+
 /* Number of BM kernel launches enqueued by this process (for accounting). */
 int64_t cgb_kernel_launch_count(void);
 

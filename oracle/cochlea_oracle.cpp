@@ -78,9 +78,22 @@ float own_expf_pos(float y) {
   return p * scale;
 }
 
+// 1/d for a positive normal d: bit-level seed 0x7EF311C3 - bits(d), then
+// three Newton steps r <- r + r(1 - d r).
+float own_rcpf(float d) {
+  uint32_t bits;
+  std::memcpy(&bits, &d, 4);
+  bits = 0x7EF311C3u - bits;
+  float r;
+  std::memcpy(&r, &bits, 4);
+  r = fmaf(r, fmaf(-d, r, 1.0f), r);
+  r = fmaf(r, fmaf(-d, r, 1.0f), r);
+  r = fmaf(r, fmaf(-d, r, 1.0f), r);
+  return r;
+}
+
 float own_tanhf(float x) {
   float ax = fabsf(x);
-  float r;
   if (ax < 0.55f) {
     float x2 = x * x;
     float p = (float)(18888466084.0 / 194896477400625.0);
@@ -95,17 +108,22 @@ float own_tanhf(float x) {
     p = fmaf(p, x2, (float)(-1.0 / 3.0));
     p = p * x2;
     return fmaf(p, x, x);
-  } else if (ax < 20.0f) {
+  }
+  float r = 1.0f;
+  if (ax < 20.0f) {
     float e = own_expf_pos(2.0f * ax);
-    r = 1.0f - 2.0f / (e + 1.0f);
-  } else {
-    r = 1.0f;
+    r = fmaf(-2.0f, own_rcpf(e + 1.0f), 1.0f);
   }
   return x < 0.0f ? -r : r;
 }
 
 template <typename T> struct Ar;
 template <> struct Ar<float> {
+  // n/d as n * (1/|d|) with the sign of d (the kernels' division-free form)
+  static float div(float n, float d) {
+    float q = n * own_rcpf(fabsf(d));
+    return d < 0.0f ? -q : q;
+  }
   static float fma(float a, float b, float c) { return fmaf(a, b, c); }
   static float tanh(float x) { return own_tanhf(x); }
   static float abs(float x) { return fabsf(x); }
@@ -113,6 +131,7 @@ template <> struct Ar<float> {
   static float min(float a, float b) { return fminf(a, b); }
 };
 template <> struct Ar<double> {
+  static double div(double n, double d) { return n / d; }
   static double fma(double a, double b, double c) { return std::fma(a, b, c); }
   static double tanh(double x) { return std::tanh(x); }
   static double abs(double x) { return std::fabs(x); }
@@ -268,14 +287,17 @@ struct BMModel {
 };
 
 template <typename T>
+T pair_sum(const T* t, int n) {
+  return n == 1 ? t[0] : pair_sum(t, n / 2) + pair_sum(t + n / 2, n / 2);
+}
+
+// Sum over the 256 sections in the kernels' order: a pairwise tree over the
+// sections of each lane, then an xor-butterfly across the lanes.
+template <typename T>
 T tree_sum(const T* term, int lanes) {
   int chunk = NS / lanes;
   T part[NS];
-  for (int l = 0; l < lanes; ++l) {
-    T acc = T(0);
-    for (int c = 0; c < chunk; ++c) acc = acc + term[l * chunk + c];
-    part[l] = acc;
-  }
+  for (int l = 0; l < lanes; ++l) part[l] = pair_sum(term + l * chunk, chunk);
   for (int o = lanes / 2; o >= 1; o /= 2) {
     T nxt[NS];
     for (int l = 0; l < lanes; ++l) nxt[l] = part[l] + part[l ^ o];
@@ -378,7 +400,7 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
           T Pp = A::fma(md.S_tm[s], y[s], Pohc);
           T num = A::fma(-gam[s], N, Pp);
           T den = md.R_tm[s] * A::fma(gam[s] * Aa, e2, (T)-1);
-          u[s] = num / den;
+          u[s] = A::div(num, den);
           Ptm[s] = A::fma(md.R_tm[s], u[s], md.S_tm[s] * y[s]);
         }
         T g = md.R[s] * A::fma(ar, v[s] * v[s], (T)1);
