@@ -59,23 +59,68 @@ __device__ __forceinline__ void load8(const float* p, float (&r)[kSPL]) {
   r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
 }
 
+__device__ __forceinline__ void store8(float* p, const float (&r)[kSPL]) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(r[0], r[1], r[2], r[3]);
+  reinterpret_cast<float4*>(p)[1] = make_float4(r[4], r[5], r[6], r[7]);
+}
+
+// The previous-step state (x, v, a, y, u, psi, psi') of a unit lives either
+// in registers or, with PREV_SMEM, in the warp's slice of shared memory
+// (7 x 256 floats), which frees 56 registers per thread at the cost of
+// reloading it on every outer iteration.
+template <bool PREV_SMEM>
+struct PrevState {
+  float r[7][kSPL];
+  float* sm;  // [7][256] slice of this warp (PREV_SMEM only)
+  __device__ __forceinline__ void init(float* slice, int base) {
+    sm = slice;
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+#pragma unroll
+      for (int k = 0; k < kSPL; ++k) r[j][k] = 0.0f;
+    if (PREV_SMEM)
+#pragma unroll
+      for (int j = 0; j < 7; ++j) store8(sm + j * 256 + base, r[j]);
+  }
+  __device__ __forceinline__ void load(int j, int base, float (&o)[kSPL]) const {
+    if (PREV_SMEM) {
+      load8(sm + j * 256 + base, o);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kSPL; ++k) o[k] = r[j][k];
+    }
+  }
+  __device__ __forceinline__ void store(int j, int base, const float (&o)[kSPL]) {
+    if (PREV_SMEM) {
+      store8(sm + j * 256 + base, o);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kSPL; ++k) r[j][k] = o[k];
+    }
+  }
+};
+
 // One unit, executed by one full warp.  sp: shared [8][256] section
 // parameters; sg / sgs: shared gamma and gamma*S_ohc of the unit's profile.
+template <bool PREV_SMEM>
 __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
                                          const float* __restrict__ sp,
                                          const float* __restrict__ sg,
-                                         const float* __restrict__ sgs, int lane,
-                                         cgb_unit_stats* st) {
+                                         const float* __restrict__ sgs, float* prev_slice,
+                                         int lane, cgb_unit_stats* st) {
   const int base = lane * kSPL;
   float rm[kSPL];
   load8(sp + 1 * 256 + base, rm);
+  // 1/m of the halo sections 8l-1 and 8l+8 (used by the paired sweeps)
+  const float rmL = __shfl_up_sync(kFull, rm[kSPL - 1], 1);
+  const float rmR = __shfl_down_sync(kFull, rm[0], 1);
 
-  float x0[kSPL], v0[kSPL], a0[kSPL], y0[kSPL], u0[kSPL], ps0[kSPL], dp0[kSPL];
+  PrevState<PREV_SMEM> prev;
+  prev.init(prev_slice, base);
   float x[kSPL], v[kSPL], a[kSPL], y[kSPL], u[kSPL], ps[kSPL], dp[kSPL];
   float Ptm[kSPL], p[kSPL], G[kSPL], Yrm[kSPL];
 #pragma unroll
   for (int k = 0; k < kSPL; ++k) {
-    x0[k] = v0[k] = a0[k] = y0[k] = u0[k] = ps0[k] = dp0[k] = 0.0f;
     x[k] = v[k] = a[k] = y[k] = u[k] = ps[k] = dp[k] = 0.0f;
     Ptm[k] = p[k] = G[k] = Yrm[k] = 0.0f;
   }
@@ -107,6 +152,14 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // Euler, which is the trapezoid rule with the new-derivative slots
       // holding the previous derivatives: (d0 + d0) * 0.5 == d0 exactly, so
       // one code path serves both.
+      float x0[kSPL], v0[kSPL], a0[kSPL], y0[kSPL], u0[kSPL], ps0[kSPL], dp0[kSPL];
+      prev.load(0, base, x0);
+      prev.load(1, base, v0);
+      prev.load(2, base, a0);
+      prev.load(3, base, y0);
+      prev.load(4, base, u0);
+      prev.load(5, base, ps0);
+      prev.load(6, base, dp0);
       if (out_loop == 0 || reset) {
         out_loop = 0;
 #pragma unroll
@@ -166,18 +219,54 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       }
 
       // Jacobi sweeps on the pressure; p persists across iterations and steps.
+      // Sweeps run in pairs: a lane fetches a halo of two sections on each
+      // side, computes the first sweep on sections 8l-1..8l+8 (the two halo
+      // sections duplicate exactly what the neighbours compute) and the
+      // second on its own sections, so one shuffle round serves two sweeps.
+      // Sections 254 and 255 carry no lower coefficient; p_{-1} = p_256 = 0.
       const int J = tm_update ? A.jslow : A.jfast;
-      for (int it = 0; it < J; ++it) {
+      const float YrmL = __shfl_up_sync(kFull, Yrm[kSPL - 1], 1);
+      const float YrmR = __shfl_down_sync(kFull, Yrm[0], 1);
+      const bool first = lane == 0, last = lane == 31;
+      int it = 0;
+      for (; it + 1 < J; it += 2) {
+        const float L1 = __shfl_up_sync(kFull, p[kSPL - 1], 1);
+        const float L2 = __shfl_up_sync(kFull, p[kSPL - 2], 1);
+        const float R1 = __shfl_down_sync(kFull, p[0], 1);
+        const float R2 = __shfl_down_sync(kFull, p[1], 1);
+        float q[kSPL];
+        float qL = __fmaf_rn(-__fadd_rn(L2, p[0]), rmL, YrmL);
+        float qR = __fmaf_rn(-__fadd_rn(p[kSPL - 1], R2), rmR, YrmR);
+        if (first) qL = 0.0f;
+        if (last) qR = 0.0f;
+        q[0] = __fmaf_rn(-__fadd_rn(first ? 0.0f : L1, p[1]), rm[0], Yrm[0]);
+#pragma unroll
+        for (int k = 1; k < kSPL - 2; ++k)
+          q[k] = __fmaf_rn(-__fadd_rn(p[k - 1], p[k + 1]), rm[k], Yrm[k]);
+        const float t6 = last ? p[kSPL - 1] : __fadd_rn(p[kSPL - 3], p[kSPL - 1]);
+        const float t7 = last ? 0.0f : __fadd_rn(p[kSPL - 2], R1);
+        q[kSPL - 2] = __fmaf_rn(-t6, rm[kSPL - 2], Yrm[kSPL - 2]);
+        q[kSPL - 1] = __fmaf_rn(-t7, rm[kSPL - 1], Yrm[kSPL - 1]);
+        p[0] = __fmaf_rn(-__fadd_rn(qL, q[1]), rm[0], Yrm[0]);
+#pragma unroll
+        for (int k = 1; k < kSPL - 2; ++k)
+          p[k] = __fmaf_rn(-__fadd_rn(q[k - 1], q[k + 1]), rm[k], Yrm[k]);
+        const float u6 = last ? q[kSPL - 1] : __fadd_rn(q[kSPL - 3], q[kSPL - 1]);
+        const float u7 = last ? 0.0f : __fadd_rn(q[kSPL - 2], qR);
+        p[kSPL - 2] = __fmaf_rn(-u6, rm[kSPL - 2], Yrm[kSPL - 2]);
+        p[kSPL - 1] = __fmaf_rn(-u7, rm[kSPL - 1], Yrm[kSPL - 1]);
+      }
+      if (it < J) {
         float left = __shfl_up_sync(kFull, p[kSPL - 1], 1);
         float right = __shfl_down_sync(kFull, p[0], 1);
-        if (lane == 0) left = 0.0f;
-        if (lane == 31) right = 0.0f;
+        if (first) left = 0.0f;
+        if (last) right = 0.0f;
         float t[kSPL];
         t[0] = __fadd_rn(left, p[1]);
 #pragma unroll
         for (int k = 1; k < kSPL - 1; ++k) t[k] = __fadd_rn(p[k - 1], p[k + 1]);
         t[kSPL - 1] = __fadd_rn(p[kSPL - 2], right);
-        if (lane == 31) {  // rows 254, 255 carry no lower coefficient
+        if (last) {
           t[kSPL - 2] = p[kSPL - 1];
           t[kSPL - 1] = right;
         }
@@ -253,16 +342,13 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       sub_in_sample = 0;
       ++n;
     }
-#pragma unroll
-    for (int k = 0; k < kSPL; ++k) {
-      x0[k] = x[k];
-      v0[k] = v[k];
-      a0[k] = a[k];
-      ps0[k] = ps[k];
-      dp0[k] = dp[k];
-      u0[k] = u[k];
-      y0[k] = y[k];
-    }
+    prev.store(0, base, x);
+    prev.store(1, base, v);
+    prev.store(2, base, a);
+    prev.store(3, base, y);
+    prev.store(4, base, u);
+    prev.store(5, base, ps);
+    prev.store(6, base, dp);
     w0 = w;
     wd0 = wd;
     wdd0 = wdd;
@@ -278,10 +364,11 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   }
 }
 
-template <int WARPS, int MINB>
+template <int WARPS, int MINB, bool PREV_SMEM>
 __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs A) {
   __shared__ __align__(16) float s_par[8 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
+  __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 7 * 256 : 4];
   for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) s_par[i] = A.secp[i];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -300,8 +387,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs 
       s_gam[warp][1][s] = __fmul_rn(gm, s_par[5 * 256 + s]);
     }
     __syncwarp();
-    run_unit(A, un, s_par, s_gam[warp][0], s_gam[warp][1], lane,
-             A.stats ? A.stats + uid : nullptr);
+    run_unit<PREV_SMEM>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
+                        PREV_SMEM ? s_prev[warp] : nullptr, lane,
+                        A.stats ? A.stats + uid : nullptr);
     __syncwarp();
   }
 }
@@ -309,21 +397,25 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs 
 constexpr int kWarpsPerCta = 4;
 
 // Launch shapes built: (warps per CTA, minimum resident CTAs per SM the
-// register allocation is bounded for).  Shape 0 lets ptxas use up to 255
-// registers (2 CTAs of 4 warps per SM); shape 1 bounds it for 3 CTAs.
+// register allocation is bounded for, previous-step state in shared
+// memory).  Shape 0: registers only, up to 255 per thread (2 CTAs of 4 warps
+// per SM); 1: bounded for 3 CTAs; 2, 3: the same with the previous-step
+// state in shared memory.
 struct LaunchShape {
   const void* fn;
   void (*launch)(unsigned, cudaStream_t, const BMArgs&);
 };
 
-template <int W, int M>
+template <int W, int M, bool PS>
 void launch_shape(unsigned grid, cudaStream_t st, const BMArgs& A) {
-  bm_warp_kernel<W, M><<<grid, W * 32, 0, st>>>(A);
+  bm_warp_kernel<W, M, PS><<<grid, W * 32, 0, st>>>(A);
 }
 
 const LaunchShape kShapes[] = {
-    {reinterpret_cast<const void*>(bm_warp_kernel<4, 1>), launch_shape<4, 1>},
-    {reinterpret_cast<const void*>(bm_warp_kernel<4, 3>), launch_shape<4, 3>},
+    {reinterpret_cast<const void*>(bm_warp_kernel<4, 1, false>), launch_shape<4, 1, false>},
+    {reinterpret_cast<const void*>(bm_warp_kernel<4, 3, false>), launch_shape<4, 3, false>},
+    {reinterpret_cast<const void*>(bm_warp_kernel<4, 1, true>), launch_shape<4, 1, true>},
+    {reinterpret_cast<const void*>(bm_warp_kernel<4, 3, true>), launch_shape<4, 3, true>},
 };
 int g_shape = 0;
 
