@@ -69,6 +69,32 @@ __device__ __forceinline__ float own_tanhf(float x) {
   return ax < 0.55f ? tp : te;
 }
 
+// log10(x) for a positive normal x: x = m 2^e with m in [sqrt(1/2), sqrt(2)),
+// ln m = 2 atanh(s), s = (m-1)/(m+1), by its odd series to s^11, then
+// log10 x = e log10(2) + ln(m) log10(e) (log10(2) split hi + lo).  <= 4 ulp.
+__device__ __forceinline__ float own_log10f(float x) {
+  const int ix = __float_as_int(x);
+  int e = ((ix >> 23) & 0xff) - 127;
+  float m = __int_as_float((ix & 0x7fffff) | 0x3f800000);
+  const bool hi = m > 1.41421356f;
+  m = hi ? __fmul_rn(m, 0.5f) : m;
+  e += hi ? 1 : 0;
+  const float f = __fsub_rn(m, 1.0f);
+  const float s = __fmul_rn(f, own_rcpf(__fadd_rn(2.0f, f)));
+  const float s2 = __fmul_rn(s, s);
+  float p = 1.0f / 11.0f;
+  p = __fmaf_rn(p, s2, 1.0f / 9.0f);
+  p = __fmaf_rn(p, s2, 1.0f / 7.0f);
+  p = __fmaf_rn(p, s2, 1.0f / 5.0f);
+  p = __fmaf_rn(p, s2, 1.0f / 3.0f);
+  const float two_s = __fmul_rn(2.0f, s);
+  const float lnm = __fmaf_rn(__fmul_rn(two_s, s2), p, two_s);
+  const float ef = (float)e;
+  const float l2hi = 0.30102999566398120f;
+  const float l2lo = (float)(0.30102999566398120 - (double)0.30102999566398120f);
+  return __fmaf_rn(ef, l2hi, __fmaf_rn(ef, l2lo, __fmul_rn(lnm, 0.43429448190325182f)));
+}
+
 __device__ __forceinline__ float warp_sum_xor(float v) {
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));

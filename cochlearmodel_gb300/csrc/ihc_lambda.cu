@@ -1,0 +1,369 @@
+// Fused IHC + auditory-nerve rate (lambda) kernel: reference RunIHCKernel
+// (src/cochlea.cu:3573-3644) = CudaUnifiedCalcIHC (:3431-3506) followed by
+// CudaCalcLambda (:3365-3408), with the decoupled FIR look-back rule of
+// DeviceCudaFIRFilter (:2712-2730).
+//
+// Per point (t, s) of a frame:
+//   AC  = sum_{i<tu(t)} b_i v[t-i]          (AC low-pass, taps pre-scaled)
+//   dS  = (scale v - AC)^2
+//   DC  = sum_{i<tu(t)} d_i dS[t-i]         (DC moving average)
+//   IHC = log10(max(10^ihc_s (eta_AC AC + eta_DC DC), 0) + 1e-20)
+//   lambda_j = s ? min(SAT, max(A_js IHC, spont_j)) : spont_j,  j = 0..2
+// in FP32 (FFMA accumulation over taps in order).
+//
+// GB300 layout: one CTA = 32 sections x TR output rows.  The velocity window
+// it needs (TR rows plus both filters' look-back) is staged into shared
+// memory by TMA (cp.async.bulk.tensor.2d, 128-row boxes, completion on an
+// mbarrier with a bounded wait); AC / dS / DC are computed from shared
+// memory with 8-row register blocking (one LDS feeds 8 FFMAs), and the three
+// lambda planes are written with coalesced 128-byte rows.
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "cgb_device.cuh"
+#include "cgb_internal.h"
+
+namespace cgb {
+namespace {
+
+constexpr int kSecTile = 32;   // sections per CTA (one per lane)
+constexpr int kBoxRows = 64;   // rows per TMA box
+constexpr int kIhcWarps = 8;
+constexpr int kRB = 8;         // output rows per register block
+constexpr long long kWaitPolls = 1ll << 26;
+
+struct IHCArgs {
+  const cgb_ihc_frame* frames;
+  const int32_t* tile_prefix;  // [n_frames + 1]
+  int n_frames;
+  const float* taps;           // [n_ac] AC taps (x scale) then [n_dc] DC taps
+  int n_ac, n_dc;
+  float scale, eta_ac, eta_dc, sat;
+  float spont0, spont1, spont2;
+  const float* dmg;            // [P][256] 10^ihc
+  const float* aihc;           // [3][256]
+  float* lam;                  // [3][lam_plane_rows][256]
+  int64_t lam_plane_rows;
+  float* ihc;                  // [lam rows][256] or null
+  int TR, xrows;               // output rows per tile, staged rows (multiple of 128)
+  int32_t* status;
+};
+
+__device__ __forceinline__ int taps_used(int k, const cgb_ihc_frame& f, int taps) {
+  const int sg = k < f.frdp - 1 ? f.seg : f.total;
+  const int lim = (k + 1) % sg;
+  return lim < taps ? lim : taps;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// FIR of one 8-row block, rows kb..kb+7 all using `taps` taps.  src points at
+// the staged row of output kb (lane's column); rows above it are older.
+__device__ __forceinline__ void fir_block8(const float* __restrict__ src,
+                                           const float* __restrict__ b, int taps,
+                                           float (&acc)[kRB]) {
+  float w[kRB];
+#pragma unroll
+  for (int r = 0; r < kRB; ++r) {
+    acc[r] = 0.0f;
+    w[r] = src[r * kSecTile];
+  }
+#pragma unroll 8
+  for (int i = 0; i < taps; ++i) {
+    const float bi = b[i];
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) acc[r] = __fmaf_rn(bi, w[r], acc[r]);
+#pragma unroll
+    for (int r = kRB - 1; r > 0; --r) w[r] = w[r - 1];
+    w[0] = src[-(i + 1) * kSecTile];
+  }
+}
+
+__device__ __forceinline__ float fir_row(const float* __restrict__ src,
+                                         const float* __restrict__ b, int tu) {
+  float acc = 0.0f;
+  for (int i = 0; i < tu; ++i) acc = __fmaf_rn(b[i], src[-i * kSecTile], acc);
+  return acc;
+}
+
+__global__ void __launch_bounds__(kIhcWarps * 32)
+    ihc_lambda_kernel(const __grid_constant__ CUtensorMap vmap, const IHCArgs A) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // layout: X [xrows][32] | dS [TR + n_dc][32] | AC [TR][32] | taps | mbarrier
+  float* X = reinterpret_cast<float*>(smem_raw);
+  float* DS = X + (size_t)A.xrows * kSecTile;
+  float* ACb = DS + (size_t)(A.TR + A.n_dc) * kSecTile;
+  float* TP = ACb + (size_t)A.TR * kSecTile;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(
+      (reinterpret_cast<uintptr_t>(TP + A.n_ac + A.n_dc) + 15) & ~uintptr_t(15));
+
+  // locate the frame and the tile
+  const int bx = blockIdx.x;
+  int lo = 0, hi = A.n_frames;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (A.tile_prefix[mid] <= bx) lo = mid; else hi = mid;
+  }
+  const cgb_ihc_frame f = A.frames[lo];
+  const int row0 = (bx - A.tile_prefix[lo]) * A.TR;
+  const int TRt = min(A.TR, f.lam_rows - row0);
+  const int s0 = blockIdx.y * kSecTile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // staged rows start one row below the oldest row any filter reads
+  const int xbase = row0 - A.n_ac - A.n_dc + 1;
+  const int dsbase = row0 - A.n_dc;
+
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  for (int i = threadIdx.x; i < A.n_ac + A.n_dc; i += blockDim.x) TP[i] = A.taps[i];
+  __syncthreads();
+  const int boxes = A.xrows / kBoxRows;
+  if (threadIdx.x == 0) {
+    const uint32_t bytes = (uint32_t)boxes * kBoxRows * kSecTile * 4;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
+                 "r"(bytes)
+                 : "memory");
+    for (int bxi = 0; bxi < boxes; ++bxi) {
+      const int y = (int)f.v_row0 + xbase + bxi * kBoxRows;  // may be negative: zero fill
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+          " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(X + (size_t)bxi * kBoxRows * kSecTile)),
+          "l"(&vmap), "r"(s0), "r"(y), "r"(smem_u32(mbar))
+          : "memory");
+    }
+  }
+  // bounded wait on the TMA transaction
+  {
+    uint32_t done = 0;
+    long long polls = 0;
+    while (!done && polls < kWaitPolls) {
+      asm volatile(
+          "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+          : "=r"(done)
+          : "r"(smem_u32(mbar))
+          : "memory");
+      ++polls;
+    }
+    if (!done) {
+      if (threadIdx.x == 0) atomicOr(A.status, 1);
+      return;
+    }
+  }
+
+  const float* bac = TP;
+  const float* bdc = TP + A.n_ac;
+  const float scale = A.scale;
+
+  // phase 1: AC and dS on rows [max(0, row0 - n_dc + 1), row0 + TRt)
+  const int k_lo = max(0, row0 - A.n_dc + 1), k_hi = row0 + TRt;
+  for (int kb = k_lo + warp * kRB; kb < k_hi; kb += kIhcWarps * kRB) {
+    const int nr = min(kRB, k_hi - kb);
+    bool fast = nr == kRB;
+#pragma unroll
+    for (int r = 0; r < kRB; ++r)
+      fast = fast && taps_used(kb + r, f, A.n_ac) == A.n_ac;
+    float acc[kRB];
+    const float* src = X + (size_t)(kb - xbase) * kSecTile + lane;
+    if (fast) {
+      fir_block8(src, bac, A.n_ac, acc);
+    } else {
+#pragma unroll
+      for (int r = 0; r < kRB; ++r)
+        acc[r] = r < nr ? fir_row(src + r * kSecTile, bac, taps_used(kb + r, f, A.n_ac)) : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) {
+      if (r < nr) {
+        const int k = kb + r;
+        const float ms = __fmaf_rn(src[r * kSecTile], scale, -acc[r]);
+        DS[(size_t)(k - dsbase) * kSecTile + lane] = __fmul_rn(ms, ms);
+        if (k >= row0) ACb[(size_t)(k - row0) * kSecTile + lane] = acc[r];
+      }
+    }
+  }
+  __syncthreads();
+
+  // phase 2: DC, IHC and lambda on rows [row0, row0 + TRt)
+  const int s = s0 + lane;
+  const float dmg = A.dmg[(size_t)f.ihc_profile * 256 + s];
+  const float a0 = A.aihc[0 * 256 + s], a1 = A.aihc[1 * 256 + s], a2 = A.aihc[2 * 256 + s];
+  const bool sec0 = s == 0;
+  for (int kb = row0 + warp * kRB; kb < k_hi; kb += kIhcWarps * kRB) {
+    const int nr = min(kRB, k_hi - kb);
+    bool fast = nr == kRB;
+#pragma unroll
+    for (int r = 0; r < kRB; ++r)
+      fast = fast && taps_used(kb + r, f, A.n_dc) == A.n_dc;
+    float acc[kRB];
+    const float* src = DS + (size_t)(kb - dsbase) * kSecTile + lane;
+    if (fast) {
+      fir_block8(src, bdc, A.n_dc, acc);
+    } else {
+#pragma unroll
+      for (int r = 0; r < kRB; ++r)
+        acc[r] = r < nr ? fir_row(src + r * kSecTile, bdc, taps_used(kb + r, f, A.n_dc)) : 0.0f;
+    }
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) {
+      if (r < nr) {
+        const int k = kb + r;
+        const float ac = ACb[(size_t)(k - row0) * kSecTile + lane];
+        const float pre = __fmaf_rn(ac, A.eta_ac, __fmul_rn(acc[r], A.eta_dc));
+        const float y = __fmul_rn(dmg, pre);
+        const float lg = own_log10f(__fadd_rn(fmaxf(y, 0.0f), 1e-20f));
+        const int64_t row = f.lam_row0 + k;
+        if (A.ihc) A.ihc[row * 256 + s] = lg;
+        const float l0 = sec0 ? A.spont0 : fminf(A.sat, fmaxf(__fmul_rn(a0, lg), A.spont0));
+        const float l1 = sec0 ? A.spont1 : fminf(A.sat, fmaxf(__fmul_rn(a1, lg), A.spont1));
+        const float l2 = sec0 ? A.spont2 : fminf(A.sat, fmaxf(__fmul_rn(a2, lg), A.spont2));
+        A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
+        A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
+        A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
+      }
+    }
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+size_t smem_bytes(int TR, int xrows, int n_ac, int n_dc) {
+  return ((size_t)xrows + TR + n_dc + TR) * kSecTile * 4 + (size_t)(n_ac + n_dc) * 4 + 32;
+}
+
+}  // namespace
+}  // namespace cgb
+
+extern "C" int64_t cgb_ihc_lambda_scratch_bytes(int n_frames, int n_ac, int n_dc) {
+  return ((int64_t)n_frames * (int64_t)sizeof(cgb_ihc_frame) + 255) / 256 * 256 +
+         ((int64_t)(n_frames + 1) * 4 + 255) / 256 * 256 +
+         ((int64_t)(n_ac + n_dc) * 4 + 255) / 256 * 256;
+}
+
+extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                                  int n_frames, const float* ac_taps, int n_ac,
+                                  const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+                                  const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
+                                  float* d_lam, int64_t lam_plane_rows, float* d_ihc,
+                                  void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
+                                  void* stream) {
+  using namespace cgb;
+  if (n_frames == 0) return CGB_OK;
+  if (!d_v || !frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_dmg || !d_aihc ||
+      !d_lam || !d_scratch || !d_status)
+    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_dev: null pointer argument");
+  if (n_ac < 1 || n_dc < 1 || n_ac > 1024 || n_dc > 1024)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filter lengths must be in [1, 1024]");
+  if (scratch_bytes < cgb_ihc_lambda_scratch_bytes(n_frames, n_ac, n_dc))
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: scratch buffer too small");
+  if (reinterpret_cast<uintptr_t>(d_v) & 15)
+    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_dev: d_v must be 16-byte aligned");
+  if (v_rows > INT32_MAX)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: more than 2^31-1 velocity rows");
+  std::vector<int32_t> prefix(n_frames + 1, 0);
+  int max_tr = 384;
+  // shrink the tile until the staged window fits 227 KB of shared memory
+  int TR = max_tr, xrows = 0;
+  for (; TR >= 8; TR -= 8) {
+    xrows = (TR + n_ac + n_dc - 1 + kBoxRows - 1) / kBoxRows * kBoxRows;
+    if (smem_bytes(TR, xrows, n_ac, n_dc) <= 227 * 1024) break;
+  }
+  if (TR < 8) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
+  for (int i = 0; i < n_frames; ++i) {
+    const cgb_ihc_frame& fr = frames[i];
+    const bool ok = fr.v_row0 >= 0 && fr.lam_rows >= 0 && fr.lam_rows <= fr.rows &&
+                    fr.v_row0 + fr.rows <= v_rows && fr.lam_row0 >= 0 &&
+                    fr.lam_row0 + fr.lam_rows <= lam_plane_rows && fr.seg > 0 && fr.frdp > 0 &&
+                    fr.total > 0 && fr.ihc_profile >= 0 && fr.ihc_profile < n_dmg_profiles;
+    if (!ok)
+      return fail(CGB_ERR_RANGE,
+                  "cgb_ihc_lambda_dev: frame " + std::to_string(i) + " out of range");
+    prefix[i + 1] = prefix[i] + (fr.lam_rows + TR - 1) / TR;
+  }
+  const int n_tiles = prefix[n_frames];
+  if (n_tiles == 0) return CGB_OK;
+
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  unsigned char* sc = static_cast<unsigned char*>(d_scratch);
+  const size_t fbytes = ((size_t)n_frames * sizeof(cgb_ihc_frame) + 255) / 256 * 256;
+  const size_t pbytes = ((size_t)(n_frames + 1) * 4 + 255) / 256 * 256;
+  std::vector<float> taps(n_ac + n_dc);
+  for (int i = 0; i < n_ac; ++i) taps[i] = ac_taps[i] * prm->scale;
+  for (int i = 0; i < n_dc; ++i) taps[n_ac + i] = dc_taps[i];
+  CGB_TRY_CUDA(cudaMemcpyAsync(sc, frames, (size_t)n_frames * sizeof(cgb_ihc_frame),
+                               cudaMemcpyHostToDevice, st),
+               "upload frames");
+  CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes, prefix.data(), (size_t)(n_frames + 1) * 4,
+                               cudaMemcpyHostToDevice, st),
+               "upload tile prefix");
+  CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes + pbytes, taps.data(), taps.size() * 4,
+                               cudaMemcpyHostToDevice, st),
+               "upload taps");
+
+  auto encode = get_encode();
+  if (!encode) return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  CUtensorMap map;
+  cuuint64_t dims[2] = {256, (cuuint64_t)v_rows};
+  cuuint64_t strides[1] = {256 * 4};
+  cuuint32_t box[2] = {(cuuint32_t)kSecTile, (cuuint32_t)kBoxRows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(d_v), dims,
+                       strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS)
+    return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
+
+  IHCArgs A;
+  A.frames = reinterpret_cast<const cgb_ihc_frame*>(sc);
+  A.tile_prefix = reinterpret_cast<const int32_t*>(sc + fbytes);
+  A.n_frames = n_frames;
+  A.taps = reinterpret_cast<const float*>(sc + fbytes + pbytes);
+  A.n_ac = n_ac;
+  A.n_dc = n_dc;
+  A.scale = prm->scale;
+  A.eta_ac = prm->eta_ac;
+  A.eta_dc = prm->eta_dc;
+  A.sat = prm->lambda_sat;
+  A.spont0 = prm->spont[0];
+  A.spont1 = prm->spont[1];
+  A.spont2 = prm->spont[2];
+  A.dmg = d_dmg;
+  A.aihc = d_aihc;
+  A.lam = d_lam;
+  A.lam_plane_rows = lam_plane_rows;
+  A.ihc = d_ihc;
+  A.TR = TR;
+  A.xrows = xrows;
+  A.status = d_status;
+  const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
+  CGB_TRY_CUDA(cudaFuncSetAttribute(ihc_lambda_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "cudaFuncSetAttribute(ihc smem)");
+  dim3 grid((unsigned)n_tiles, 256 / kSecTile);
+  ihc_lambda_kernel<<<grid, kIhcWarps * 32, smem, st>>>(map, A);
+  CGB_TRY_CUDA(cudaGetLastError(), "ihc_lambda_kernel launch");
+  note_launch();
+  return CGB_OK;
+}

@@ -57,6 +57,9 @@ _SIGS = {
     "cgb_block_partition": (_i, [_i, _i64, _i, _i, _p, _p, _p]),
     "cgb_check_units": (_i, [_p, _i, _i, _i64, _i64]),
     "cgb_bm_set_launch_shape": (_i, [_i]),
+    "cgb_ihc_lambda_scratch_bytes": (_i64, [_i, _i, _i]),
+    "cgb_ihc_lambda_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64, _p,
+                                _p, _i64, _p, _p]),
     "cgb_bm_launch_shape_count": (_i, []),
     "cgb_bm_run_dev": (_i, [_p, _p, _i, C.POINTER(BMScalars), _p, _i, _p, _i64, _p, _i64,
                             _p, _p, _p, _p]),

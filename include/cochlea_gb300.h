@@ -85,6 +85,31 @@ typedef struct cgb_bm_scalars {
   int32_t max_substeps_per_sample; /* guard against a collapsed dt (>= 1)       */
 } cgb_bm_scalars;
 
+/* One frame of the IHC/lambda stage: a run of consecutive velocity rows that
+ * the reference filters as one buffer (one Run_Cuda chunk, or one signal of a
+ * batch).  FIR look-back at row k of the frame uses
+ *   min((k+1) % (k < frdp-1 ? seg : total), taps) taps
+ * (DeviceCudaFIRFilter, src/cochlea.cu:2712-2730). */
+typedef struct cgb_ihc_frame {
+  int64_t v_row0;      /* first velocity row of the frame                     */
+  int64_t lam_row0;    /* first row of the frame in each lambda plane         */
+  int32_t rows;        /* velocity rows available to the frame                */
+  int32_t lam_rows;    /* rows for which IHC and lambda are produced (<= rows) */
+  int32_t seg;         /* decoupled interval length: block nodes x Decouple_Filter */
+  int32_t frdp;        /* block nodes x Time_Blocks                           */
+  int32_t total;       /* calcTime: rows rounded up to 64                      */
+  int32_t ihc_profile; /* row of the 10^IHC damage table                      */
+} cgb_ihc_frame;
+
+typedef struct cgb_ihc_params {
+  float scale;       /* scaleBMVelocityForLambdaCalculation (AC taps are scaled) */
+  float eta_ac;      /* IHC AC coupling                                          */
+  float eta_dc;      /* IHC DC coupling                                          */
+  float lambda_sat;  /* Lambda_SAT                                               */
+  float spont[3];    /* spontaneous rates of the high/medium/low fibres          */
+  int32_t pad_;
+} cgb_ihc_params;
+
 const char* cgb_last_error(void);
 int cgb_abi_version(void);
 
@@ -125,6 +150,24 @@ int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
                    const float* d_in, int64_t in_len, float* d_out, int64_t out_rows,
                    int32_t* d_failed, cgb_unit_stats* d_stats, int32_t* d_work,
                    void* stream);
+
+/* IHC + lambda over n_frames frames (host frame table, device buffers).
+ *   d_v      float[v_rows][256]  BM velocity (16-byte aligned)
+ *   ac_taps / dc_taps  host float taps (AC taps are multiplied by scale)
+ *   d_dmg    float[P][256]       10^IHC damage factors
+ *   d_aihc   float[3][256]       A of the three fibre groups
+ *   d_lam    float[3][lam_plane_rows][256] output
+ *   d_ihc    float[lam_plane_rows][256] IHC output (may be null)
+ *   d_scratch  device scratch of cgb_ihc_lambda_scratch_bytes() bytes
+ *   d_status int32: bit 0 set if a staged copy did not complete in time
+ * Filters of 1..1024 taps. */
+int64_t cgb_ihc_lambda_scratch_bytes(int n_frames, int n_ac, int n_dc);
+int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                       int n_frames, const float* ac_taps, int n_ac, const float* dc_taps,
+                       int n_dc, const cgb_ihc_params* prm, const float* d_dmg,
+                       int n_dmg_profiles, const float* d_aihc, float* d_lam,
+                       int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
+                       int64_t scratch_bytes, int32_t* d_status, void* stream);
 
 /* Host-side validation of a unit table against buffer sizes (the checks
  * cgb_bm_run_dev relies on); returns CGB_ERR_RANGE on the first bad unit. */

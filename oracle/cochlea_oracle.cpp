@@ -117,6 +117,36 @@ float own_tanhf(float x) {
   return x < 0.0f ? -r : r;
 }
 
+// log10 of a positive normal float: x = m 2^e, m in [sqrt(1/2), sqrt(2)),
+// ln m = 2 atanh((m-1)/(m+1)) by its odd series to s^11.
+float own_log10f(float x) {
+  uint32_t ix;
+  std::memcpy(&ix, &x, 4);
+  int e = (int)((ix >> 23) & 0xff) - 127;
+  uint32_t mb = (ix & 0x7fffffu) | 0x3f800000u;
+  float m;
+  std::memcpy(&m, &mb, 4);
+  bool hi = m > 1.41421356f;
+  if (hi) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  float f = m - 1.0f;
+  float s = f * own_rcpf(2.0f + f);
+  float s2 = s * s;
+  float p = 1.0f / 11.0f;
+  p = fmaf(p, s2, 1.0f / 9.0f);
+  p = fmaf(p, s2, 1.0f / 7.0f);
+  p = fmaf(p, s2, 1.0f / 5.0f);
+  p = fmaf(p, s2, 1.0f / 3.0f);
+  float two_s = 2.0f * s;
+  float lnm = fmaf(two_s * s2, p, two_s);
+  float ef = (float)e;
+  const float l2hi = 0.30102999566398120f;
+  const float l2lo = (float)(0.30102999566398120 - (double)0.30102999566398120f);
+  return fmaf(ef, l2hi, fmaf(ef, l2lo, lnm * 0.43429448190325182f));
+}
+
 template <typename T> struct Ar;
 template <> struct Ar<float> {
   // n/d as n * (1/|d|) with the sign of d (the kernels' division-free form)
@@ -179,6 +209,7 @@ typedef struct {
 } orc_bm_scalars;
 
 float orc_tanhf(float x) { return own_tanhf(x); }
+float orc_log10f(float x) { return own_log10f(x); }
 
 // ---------------------------------------------------------------------------
 // Model vectors in FP64 from the reference's float-valued constants
@@ -589,13 +620,51 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
                     double scale, double eta_ac, double eta_dc, const double* ihc_damage,
                     const float* aihc /*[3][256]*/, const float* spont /*[3]*/,
                     double lambda_sat, float* ihc, float* lam, int64_t lam_stride,
-                    int fp64 /*0: reference mixed precision, 1: all double*/) {
+                    int mode /*0: reference mixed precision, 1: all double, 2: kernel FP32*/) {
+  if (mode == 2) {
+    // The GB300 kernel's arithmetic: float taps (AC taps pre-scaled),
+    // fmaf accumulation over taps in order, own log10, float lambda.
+    std::vector<float> acf((size_t)rows * NS), dsf((size_t)rows * NS);
+    std::vector<float> bt(n_ac), dt(n_dc);
+    for (int i = 0; i < n_ac; ++i) bt[i] = (float)(ac_taps[i] * scale);
+    for (int i = 0; i < n_dc; ++i) dt[i] = (float)dc_taps[i];
+    const float sc = (float)scale, ea = (float)eta_ac, ed = (float)eta_dc;
+    for (int k = 0; k < lam_rows; ++k) {
+      int tu = fir_taps_used(k, seg, frdp, total, n_ac);
+      for (int s = 0; s < NS; ++s) {
+        float acc = 0.0f;
+        for (int i = 0; i < tu; ++i) acc = fmaf(bt[i], v[(size_t)(k - i) * NS + s], acc);
+        acf[(size_t)k * NS + s] = acc;
+        float ms = fmaf(v[(size_t)k * NS + s], sc, -acc);
+        dsf[(size_t)k * NS + s] = ms * ms;
+      }
+    }
+    for (int k = 0; k < lam_rows; ++k) {
+      int tu = fir_taps_used(k, seg, frdp, total, n_dc);
+      for (int s = 0; s < NS; ++s) {
+        float acc = 0.0f;
+        for (int i = 0; i < tu; ++i) acc = fmaf(dt[i], dsf[(size_t)(k - i) * NS + s], acc);
+        float pre = fmaf(acf[(size_t)k * NS + s], ea, acc * ed);
+        float y = (float)ihc_damage[s] * pre;
+        float lg = own_log10f(fmaxf(y, 0.0f) + 1e-20f);
+        if (ihc) ihc[(size_t)k * NS + s] = lg;
+        for (int j = 0; j < 3; ++j) {
+          float val = s != 0 ? fminf((float)lambda_sat, fmaxf(aihc[j * NS + s] * lg, spont[j]))
+                             : spont[j];
+          lam[(size_t)j * lam_stride * NS + (size_t)k * NS + s] = val;
+        }
+      }
+    }
+    return;
+  }
+  int fp64 = mode == 1;
   std::vector<double> ac((size_t)rows * NS), ds((size_t)rows * NS);
   for (int k = 0; k < rows; ++k) {
     int tu = fir_taps_used(k, seg, frdp, total, n_ac);
     for (int s = 0; s < NS; ++s) {
       double acc = 0.0;
-      for (int i = 0; i < tu; ++i) acc = acc + ac_taps[i] * (double)v[(size_t)(k - i) * NS + s];
+      for (int i = 0; i < tu; ++i)
+        acc = acc + ac_taps[i] * scale * (double)v[(size_t)(k - i) * NS + s];
       if (fp64) {
         ac[(size_t)k * NS + s] = acc;
         double ms = (double)v[(size_t)k * NS + s] * scale - acc;
@@ -621,17 +690,16 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
         pre = (double)fmaf((float)ac[(size_t)k * NS + s], (float)eta_ac,
                            (float)((double)dcf * eta_dc));
       }
-      ihc[(size_t)k * NS + s] = (float)std::log10(std::fmax(ihc_damage[s] * pre, 0.0) + 1e-20);
-    }
-  }
-  for (int j = 0; j < 3; ++j) {
-    double sp = (double)spont[j];
-    for (int k = 0; k < lam_rows; ++k) {
-      for (int s = 0; s < NS; ++s) {
-        double A = (double)aihc[j * NS + s];
-        double base = std::fmin(lambda_sat, std::fmax(A * (double)ihc[(size_t)k * NS + s], sp));
-        double val = s != 0 ? base : sp;
-        lam[(size_t)j * lam_stride * NS + (size_t)k * NS + s] = (float)val;
+      double lg = std::log10(std::fmax(ihc_damage[s] * pre, 0.0) + 1e-20);
+      if (ihc && k < lam_rows) ihc[(size_t)k * NS + s] = (float)lg;
+      if (k < lam_rows) {
+        for (int j = 0; j < 3; ++j) {
+          double sp = (double)spont[j];
+          double A = (double)aihc[j * NS + s];
+          double base = std::fmin(lambda_sat, std::fmax(A * (fp64 ? lg : (double)(float)lg), sp));
+          double val = s != 0 ? base : sp;
+          lam[(size_t)j * lam_stride * NS + (size_t)k * NS + s] = (float)val;
+        }
       }
     }
   }

@@ -52,6 +52,8 @@ def load():
         lib = C.CDLL(str(LIB))
         lib.orc_tanhf.restype = C.c_float
         lib.orc_tanhf.argtypes = [C.c_float]
+        lib.orc_log10f.restype = C.c_float
+        lib.orc_log10f.argtypes = [C.c_float]
         lib.orc_model_setup.argtypes = [_p] * 11
         lib.orc_thomas.argtypes = [_p, _p, _p, _p, _p, C.c_int]
         lib.orc_block_partition.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, _p, _p, _p]
@@ -134,7 +136,8 @@ def bm_run(secp, gamma, sc, units, inp, out_rows, fp64=False, threads=None, jaco
 
 
 def ihc_lambda(v, seg, frdp, total, lam_rows, ac_taps, dc_taps, scale, eta_ac, eta_dc,
-               ihc_damage, aihc, spont, lambda_sat, fp64=False):
+               ihc_damage, aihc, spont, lambda_sat, mode=0):
+    """mode 0: the reference's mixed precision; 1: FP64; 2: the GPU kernel's FP32."""
     v = np.ascontiguousarray(v, np.float32)
     rows = v.shape[0]
     ihc = np.zeros((rows, 256), np.float32)
@@ -146,7 +149,7 @@ def ihc_lambda(v, seg, frdp, total, lam_rows, ac_taps, dc_taps, scale, eta_ac, e
                           _ptr(np.ascontiguousarray(ihc_damage, np.float64)),
                           _ptr(np.ascontiguousarray(aihc, np.float32)),
                           _ptr(np.ascontiguousarray(spont, np.float32)), lambda_sat,
-                          _ptr(ihc), _ptr(lam), lam_rows, 1 if fp64 else 0)
+                          _ptr(ihc), _ptr(lam), lam_rows, mode)
     return ihc, lam
 
 

@@ -1,0 +1,77 @@
+"""GPU parity of the fused IHC/lambda kernel: bit-exact against the oracle's
+kernel-FP32 mode; within 1e-4 max-rel of the reference's mixed-precision
+arithmetic (double taps and accumulators), the lambda bar."""
+import numpy as np
+import pytest
+
+from cochlearmodel_gb300 import ihc
+from oracle import oracle as orc
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-4  # max |a-b| / max |b| per lambda plane
+
+
+@pytest.fixture(scope="module")
+def stage():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return ihc.IHCStage("cuda:0", ihc_profiles=np.stack([np.full(256, 8.0, np.float32),
+                                                         np.linspace(8, 5, 256, dtype=np.float32)]))
+
+
+def _oracle(stage, v, fr, mode):
+    return orc.ihc_lambda(v[fr["v_row0"]:fr["v_row0"] + fr["rows"]], int(fr["seg"]),
+                          int(fr["frdp"]), int(fr["total"]), int(fr["lam_rows"]),
+                          stage.ac.astype(np.float64), stage.dc.astype(np.float64),
+                          stage.nerve.scale, stage.nerve.eta_AC, stage.nerve.eta_DC,
+                          stage.dmg_host[fr["ihc_profile"]].astype(np.float64),
+                          stage.nerve.aihc(), np.asarray(stage.nerve.spontRate, np.float32),
+                          stage.nerve.Lambda_SAT, mode=mode)
+
+
+def _check(stage, v, frames, lam_rows):
+    lam, ih = stage.run(v, frames, lam_rows, want_ihc=True)
+    for fr in frames:
+        r0, n = int(fr["lam_row0"]), int(fr["lam_rows"])
+        o_ihc, o_lam = _oracle(stage, v, fr, 2)
+        assert np.array_equal(ih[r0:r0 + n].view(np.uint32), o_ihc[:n].view(np.uint32))
+        assert np.array_equal(lam[:, r0:r0 + n].view(np.uint32), o_lam.view(np.uint32))
+        _, ref_lam = _oracle(stage, v, fr, 0)
+        for j in range(3):
+            d = np.abs(lam[j, r0:r0 + n] - ref_lam[j]).max() / np.abs(ref_lam[j]).max()
+            assert d <= REL, (j, d)
+    return lam
+
+
+def test_reference_run_frame(mv, stage):
+    case = cases.decoupled_sweep(mv, n_signals=2, decouple=2, block_ms=1.5, overlap_ms=0.5)
+    cfg, sc, gamma, units, x, rows = case
+    v, _, _ = orc.bm_run(mv.section_params(), gamma, sc, units, x, rows)
+    fr = ihc.reference_frame(cfg)
+    v = v[:int(fr["rows"][0])]
+    lam = _check(stage, v, fr, int(fr["lam_rows"][0]))
+    assert (lam[:, :, 0] == np.asarray(stage.nerve.spontRate, np.float32)[:, None]).all()
+
+
+def test_many_tiles_and_frames(stage):
+    rng = np.random.default_rng(3)
+    t = np.arange(3600)[:, None] / 1e5
+    f = 300 + 40 * np.arange(256)[None, :]
+    v = (1e-3 * np.sin(2 * np.pi * f * t) * (1 + rng.random((1, 256)))).astype(np.float32)
+    frames = np.zeros(3, ihc.FRAME_DTYPE)
+    # three frames back to back: 1000 + 1500 + 1100 rows, different rules
+    starts, lens = [0, 1000, 2500], [1000, 1500, 1100]
+    lam0 = 0
+    for i, (s, n) in enumerate(zip(starts, lens)):
+        frames[i] = (s, lam0, n, n - 100 if i == 2 else n, [500, 1500, 400][i], n if i < 2 else n - 100,
+                     ihc.round64(n), i % 2)
+        lam0 += frames[i]["lam_rows"]
+    _check(stage, v, frames, lam0)
+
+
+def test_empty_frame_table(stage):
+    lam, _ = stage.run(np.zeros((10, 256), np.float32), np.zeros(0, ihc.FRAME_DTYPE), 4)
+    assert not lam.any()
