@@ -9,13 +9,13 @@
 //   DC  = sum_{i<tu(t)} d_i dS[t-i]         (DC moving average)
 //   IHC = log10(max(10^ihc_s (eta_AC AC + eta_DC DC), 0) + 1e-20)
 //   lambda_j = s ? min(SAT, max(A_js IHC, spont_j)) : spont_j,  j = 0..2
-// in FP32 (FFMA accumulation over taps in order).
+// in FP32, each FIR accumulated with a compensated dot product (Dot2).
 //
 // GB300 layout: one CTA = 32 sections x TR output rows.  The velocity window
 // it needs (TR rows plus both filters' look-back) is staged into shared
 // memory by TMA (cp.async.bulk.tensor.2d, 128-row boxes, completion on an
 // mbarrier with a bounded wait); AC / dS / DC are computed from shared
-// memory with 8-row register blocking (one LDS feeds 8 FFMAs), and the three
+// memory with 8-row register blocking (one LDS feeds 8 rows), and the three
 // lambda planes are written with coalesced 128-byte rows.
 
 #include <cuda.h>
@@ -51,7 +51,7 @@ struct IHCArgs {
   float* lam;                  // [3][lam_plane_rows][256]
   int64_t lam_plane_rows;
   float* ihc;                  // [lam rows][256] or null
-  int TR, xrows;               // output rows per tile, staged rows (multiple of 128)
+  int TR, xrows;               // output rows per tile, staged rows (multiple of 64)
   int32_t* status;
 };
 
@@ -65,33 +65,58 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// Compensated tap accumulation (Ogita-Rump-Oishi Dot2): the product error
+// comes from one FMA, the sum error from TwoSum, and both are carried in c.
+// The result equals the dot product evaluated in about twice the working
+// precision and rounded once -- what the reference's double accumulators
+// give after their float store -- at FP32 instruction rates.
+struct Dot2 {
+  float s, c;
+  __device__ __forceinline__ void init() { s = c = 0.0f; }
+  __device__ __forceinline__ void add(float b, float x) {
+    const float p = __fmul_rn(b, x);
+    const float q = __fmaf_rn(b, x, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(e, q));
+  }
+  __device__ __forceinline__ float result() const { return __fadd_rn(s, c); }
+};
+
 // FIR of one 8-row block, rows kb..kb+7 all using `taps` taps.  src points at
-// the staged row of output kb (lane's column); rows above it are older.
+// the staged row of output kb (lane's column); rows above it are older.  One
+// shared-memory load feeds the eight rows' accumulators.
 __device__ __forceinline__ void fir_block8(const float* __restrict__ src,
                                            const float* __restrict__ b, int taps,
-                                           float (&acc)[kRB]) {
+                                           float (&out)[kRB]) {
   float w[kRB];
+  Dot2 acc[kRB];
 #pragma unroll
   for (int r = 0; r < kRB; ++r) {
-    acc[r] = 0.0f;
+    acc[r].init();
     w[r] = src[r * kSecTile];
   }
-#pragma unroll 8
+#pragma unroll 4
   for (int i = 0; i < taps; ++i) {
     const float bi = b[i];
 #pragma unroll
-    for (int r = 0; r < kRB; ++r) acc[r] = __fmaf_rn(bi, w[r], acc[r]);
+    for (int r = 0; r < kRB; ++r) acc[r].add(bi, w[r]);
 #pragma unroll
     for (int r = kRB - 1; r > 0; --r) w[r] = w[r - 1];
     w[0] = src[-(i + 1) * kSecTile];
   }
+#pragma unroll
+  for (int r = 0; r < kRB; ++r) out[r] = acc[r].result();
 }
 
 __device__ __forceinline__ float fir_row(const float* __restrict__ src,
                                          const float* __restrict__ b, int tu) {
-  float acc = 0.0f;
-  for (int i = 0; i < tu; ++i) acc = __fmaf_rn(b[i], src[-i * kSecTile], acc);
-  return acc;
+  Dot2 acc;
+  acc.init();
+  for (int i = 0; i < tu; ++i) acc.add(b[i], src[-i * kSecTile]);
+  return acc.result();
 }
 
 __global__ void __launch_bounds__(kIhcWarps * 32)

@@ -1,0 +1,222 @@
+// Input generation (reference CudaGenerateInputFromProfile,
+// src/cochlea.cu:4070-4103, normalisation :4165-4254) and the JND stage
+// (CudaCalculateJND = GlobalCalculateMeanRate + GlobalCalculateJND,
+// src/cochlea.cu:3741-3944, 3946-4065; final dB src/AudioGramCreator.cpp:454-508).
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "cgb_device.cuh"
+#include "cgb_internal.h"
+
+namespace cgb {
+namespace {
+
+// x[p][n] = dA cos(2 pi f (n - head) / Fs) / norm_s + Wn (WN[n] - dc_w) / norm_w
+// (signal_mode 0), or dA (S[n] - dc_s) / norm_s + ... (signal_mode 1), in
+// double, stored as float.  2 pi is formed from the float constant PI of the
+// reference (2 * 3.14159265f), as the reference does.
+__global__ void input_gen_kernel(const cgb_profile* __restrict__ prof, int n_prof,
+                                 const float* __restrict__ wn, const float* __restrict__ sig,
+                                 int signal_mode, int interval_len, int head, float Fs,
+                                 double wn_dc, double wn_norm, double sig_dc, double sig_norm,
+                                 float* __restrict__ out) {
+  const int p = blockIdx.y;
+  const double two_pi = (double)(2.0f * 3.141592653589793f);
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < interval_len;
+       n += gridDim.x * blockDim.x) {
+    const cgb_profile pr = prof[p];
+    double sum;
+    if (signal_mode) {
+      sum = pr.dA * ((double)sig[n] - sig_dc) / sig_norm;
+    } else {
+      const double t = (double)(n - head) / (double)Fs;
+      sum = pr.dA * cos(two_pi * pr.frequency * t) / sig_norm;
+    }
+    if (wn) sum = sum + pr.Wn * ((double)wn[n] - wn_dc) / wn_norm;
+    out[(int64_t)p * interval_len + n] = (float)sum;
+  }
+}
+
+constexpr int kJndThreads = 256;
+constexpr int kJndRows = 8;  // rows folded in FP32 before an FP64 add
+
+// One CTA per (interval i, lambda plane j), one thread per section.  Each
+// thread walks the interval's window and its reference interval's window
+// once: FP64 sums of lambda and lambda_ref (the two mean rates) and of
+// (lambda - lambda_ref)^2 / lambda_ref (the AI term); each term is formed in
+// FP32 and 8 rows are folded in FP32 before the FP64 add.  The 256 section
+// terms are then reduced in FP64.
+__global__ void __launch_bounds__(kJndThreads)
+    jnd_kernel(const float* __restrict__ lam, int64_t plane_rows, int interval_nodes, int head,
+               int len, const double* __restrict__ dA, const int32_t* __restrict__ ref_of,
+               const double* __restrict__ nihc, double w0, double w1, double w2, double Fs,
+               double T, double* __restrict__ F_RA, double* __restrict__ F_AI, int n_int) {
+  const int i = blockIdx.x, j = blockIdx.y, s = threadIdx.x;
+  const int r = ref_of[i];
+  const float* c = lam + ((int64_t)j * plane_rows + (int64_t)i * interval_nodes + head) * 256 + s;
+  const float* rf = lam + ((int64_t)j * plane_rows + (int64_t)r * interval_nodes + head) * 256 + s;
+  double sum_c = 0.0, sum_r = 0.0, sum_ai = 0.0;
+  int t = 0;
+  for (; t + kJndRows <= len; t += kJndRows) {
+    float pc = 0.0f, pr = 0.0f, pa = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kJndRows; ++k) {
+      const float lc = c[(int64_t)(t + k) * 256];
+      const float lr = rf[(int64_t)(t + k) * 256];
+      const float d = __fsub_rn(lc, lr);
+      pc = __fadd_rn(pc, lc);
+      pr = __fadd_rn(pr, lr);
+      pa = __fmaf_rn(__fmul_rn(d, d), own_rcpf(lr), pa);
+    }
+    sum_c += (double)pc;
+    sum_r += (double)pr;
+    sum_ai += (double)pa;
+  }
+  for (; t < len; ++t) {
+    const float lc = c[(int64_t)t * 256];
+    const float lr = rf[(int64_t)t * 256];
+    const float d = __fsub_rn(lc, lr);
+    sum_c += (double)lc;
+    sum_r += (double)lr;
+    sum_ai += (double)__fmul_rn(__fmul_rn(d, d), own_rcpf(lr));
+  }
+  const double da = dA[i];
+  const double mr = sum_c / len, mrr = sum_r / len;
+  const double tl = (double)len / Fs;
+  double rate = 0.0, ai = 0.0;
+  if (da > 0.0) {
+    const double dmr = (mr - mrr) / da;
+    rate = nihc[s] * T * dmr * dmr / mrr;
+    ai = nihc[s] * (T / tl) * sum_ai / (Fs * da * da);
+  }
+  // FP64 block reduction over the 256 sections
+  __shared__ double sh_r[kJndThreads / 32], sh_a[kJndThreads / 32];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    rate += __shfl_xor_sync(kFull, rate, o);
+    ai += __shfl_xor_sync(kFull, ai, o);
+  }
+  if ((s & 31) == 0) {
+    sh_r[s >> 5] = rate;
+    sh_a[s >> 5] = ai;
+  }
+  __syncthreads();
+  if (s == 0) {
+    double tr = 0.0, ta = 0.0;
+    for (int k = 0; k < kJndThreads / 32; ++k) {
+      tr += sh_r[k];
+      ta += sh_a[k];
+    }
+    const double w = j == 0 ? w0 : (j == 1 ? w1 : w2);
+    F_RA[(int64_t)j * n_int + i] = tr * w;
+    F_AI[(int64_t)j * n_int + i] = ta * w;
+  }
+}
+
+}  // namespace
+}  // namespace cgb
+
+extern "C" int cgb_input_gen_dev(const cgb_profile* d_prof, int n_prof, const float* d_wn,
+                                 const float* d_signal, int signal_mode, int interval_len,
+                                 int head, float Fs, double wn_dc, double wn_norm, double sig_dc,
+                                 double sig_norm, float* d_out, void* stream) {
+  using namespace cgb;
+  if (n_prof == 0 || interval_len == 0) return CGB_OK;
+  if (!d_prof || !d_out || n_prof < 0 || interval_len < 0 || (signal_mode && !d_signal))
+    return fail(CGB_ERR_ARG, "cgb_input_gen_dev: bad arguments");
+  if (n_prof > 65535) return fail(CGB_ERR_RANGE, "cgb_input_gen_dev: more than 65535 profiles");
+  if (!(wn_norm != 0.0) || !(sig_norm != 0.0))
+    return fail(CGB_ERR_ARG, "cgb_input_gen_dev: zero normalisation factor");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int threads = 256;
+  int bx = (interval_len + threads - 1) / threads;
+  if (bx > 1024) bx = 1024;
+  dim3 grid((unsigned)bx, (unsigned)n_prof);
+  input_gen_kernel<<<grid, threads, 0, st>>>(d_prof, n_prof, d_wn, d_signal, signal_mode,
+                                              interval_len, head, Fs, wn_dc, wn_norm, sig_dc,
+                                              sig_norm, d_out);
+  CGB_TRY_CUDA(cudaGetLastError(), "input_gen_kernel launch");
+  note_launch();
+  return CGB_OK;
+}
+
+extern "C" int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, int interval_nodes,
+                           int head, int len, const double* d_dA, const int32_t* d_ref_of,
+                           const double* d_nihc, const float* W, double Fs,
+                           double delta_alpha_len_factor, double* d_F_RA, double* d_F_AI,
+                           void* stream) {
+  using namespace cgb;
+  if (n_int == 0) return CGB_OK;
+  if (!d_lam || !d_dA || !d_ref_of || !d_nihc || !W || !d_F_RA || !d_F_AI || n_int < 0 ||
+      len <= 0 || interval_nodes <= 0 || head < 0)
+    return fail(CGB_ERR_ARG, "cgb_jnd_dev: bad arguments");
+  if ((int64_t)n_int * interval_nodes > plane_rows || head + len > interval_nodes)
+    return fail(CGB_ERR_RANGE, "cgb_jnd_dev: intervals reach outside the lambda planes");
+  if (n_int > 65535 * 32) return fail(CGB_ERR_RANGE, "cgb_jnd_dev: too many intervals");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const double T = delta_alpha_len_factor / Fs;
+  dim3 grid((unsigned)n_int, 3);
+  jnd_kernel<<<grid, kJndThreads, 0, st>>>(d_lam, plane_rows, interval_nodes, head, len, d_dA,
+                                           d_ref_of, d_nihc, (double)W[0], (double)W[1],
+                                           (double)W[2], Fs, T, d_F_RA, d_F_AI, n_int);
+  CGB_TRY_CUDA(cudaGetLastError(), "jnd_kernel launch");
+  note_launch();
+  return CGB_OK;
+}
+
+extern "C" int cgb_jnd_final(const double* F_RA, const double* F_AI, int n_int,
+                             const int32_t* ref_of, double spl_ref, double max_db,
+                             double* jnd_rate_db, double* jnd_ai_db) {
+  if (!F_RA || !F_AI || !ref_of || !jnd_rate_db || !jnd_ai_db || n_int < 0)
+    return cgb::fail(CGB_ERR_ARG, "cgb_jnd_final: bad arguments");
+  const double max_pa = std::pow(10.0, max_db / 20.0) * spl_ref;
+  auto to_db = [&](double sum) {
+    const double pa = 1.0 / std::sqrt(sum);
+    return (std::isinf(pa) || pa > max_pa) ? max_db : 20.0 * std::log10(pa / spl_ref);
+  };
+  for (int i = 0; i < n_int; ++i) {
+    double ra = 0.0, ai = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      ra += F_RA[(int64_t)j * n_int + i];
+      ai += F_AI[(int64_t)j * n_int + i];
+    }
+    const bool is_ref = ref_of[i] == i;
+    jnd_rate_db[i] = is_ref ? NAN : to_db(ra);
+    jnd_ai_db[i] = is_ref ? NAN : to_db(ai);
+  }
+  return CGB_OK;
+}
+
+extern "C" int cgb_noise_normalization(const float* src, int normalize_type,
+                                       double normalize_to_interval, double remove_dc,
+                                       int start_dc, int end_dc, int start_norm, int end_norm,
+                                       float Fs, double* dc, double* factor) {
+  if (!dc || !factor) return cgb::fail(CGB_ERR_ARG, "cgb_noise_normalization: null output");
+  // src == null: a pure tone (calculateDCANDNornalizationFactorPureTone)
+  double d = 0.0, e;
+  if (src) {
+    if (end_dc <= start_dc || end_norm <= start_norm)
+      return cgb::fail(CGB_ERR_ARG, "cgb_noise_normalization: empty window");
+    d = src[start_dc];
+    for (int i = start_dc + 1; i < end_dc; ++i) d = d + src[i];
+    d = remove_dc * d / (double)(end_dc - start_dc);
+    // the first term enters without the dc removed, as in the reference
+    e = (double)src[start_norm] * (double)src[start_norm];
+    for (int i = start_norm + 1; i < end_norm; ++i) e = e + ((src[i] - d) * (src[i] - d));
+    e = std::sqrt(e);
+  } else {
+    e = std::sqrt(0.5 * (double)(end_norm - start_norm));
+  }
+  if (normalize_type == 1)
+    e = e / std::sqrt((double)(end_norm - start_norm));
+  else if (normalize_type == 2 && normalize_to_interval > 0)
+    e = e / std::sqrt(Fs * normalize_to_interval);
+  else if (normalize_type == 3)
+    e = 1.0;
+  *dc = d;
+  *factor = e;
+  return CGB_OK;
+}

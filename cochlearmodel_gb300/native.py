@@ -24,6 +24,7 @@ STATS_DTYPE = np.dtype([
     ("substeps", "<i8"), ("iterations", "<i8"), ("sweeps", "<i8"),
     ("failed_samples", "<i4"), ("written_samples", "<i4"), ("status", "<i4"), ("pad_", "<i4"),
 ])
+PROFILE_DTYPE = np.dtype([("dA", "<f8"), ("Wn", "<f8"), ("frequency", "<f8")])
 assert UNIT_DTYPE.itemsize == 40 and STATS_DTYPE.itemsize == 40
 
 
@@ -58,6 +59,10 @@ _SIGS = {
     "cgb_check_units": (_i, [_p, _i, _i, _i64, _i64]),
     "cgb_bm_set_launch_shape": (_i, [_i]),
     "cgb_ihc_lambda_scratch_bytes": (_i64, [_i, _i, _i]),
+    "cgb_input_gen_dev": (_i, [_p, _i, _p, _p, _i, _i, _i, C.c_float, _d, _d, _d, _d, _p, _p]),
+    "cgb_noise_normalization": (_i, [_p, _i, _d, _d, _i, _i, _i, _i, C.c_float, _p, _p]),
+    "cgb_jnd_dev": (_i, [_p, _i64, _i, _i, _i, _i, _p, _p, _p, _p, _d, _d, _p, _p, _p]),
+    "cgb_jnd_final": (_i, [_p, _p, _i, _p, _d, _d, _p, _p]),
     "cgb_ihc_lambda_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64, _p,
                                 _p, _i64, _p, _p]),
     "cgb_bm_launch_shape_count": (_i, []),

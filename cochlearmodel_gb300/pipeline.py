@@ -1,0 +1,169 @@
+"""The solver path as Run_Cuda drives it in profile mode (src/solver.cpp:234-962):
+input generation -> BM/OHC solver -> IHC/lambda -> JND, on device buffers.
+
+ProfileSweep mirrors CParams::updateInputProfile (src/params.cpp:661-782):
+per noise level, per power level, per frequency one tested interval, plus one
+noise-only reference interval per noise level when JND is computed.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native
+from .ihc import FRAME_DTYPE, IHCStage, NerveConfig, reference_frame
+from .model import ModelVectors, RunConfig, bm_scalars, reference_units, spl_to_amplitude
+
+F32 = np.float32
+
+
+@dataclass
+class ProfileSweep:
+    frequencies: list
+    powers: list                       # dB SPL
+    noises: list = field(default_factory=lambda: [1111.0])  # 1111 = no noise
+    calculate_jnd: bool = False
+    spl_ref: float = 2e-5
+
+    def build(self):
+        """Returns (profiles PROFILE_DTYPE[n], is_reference bool[n], ref_of int32[n])."""
+        prof, is_ref, ref_of = [], [], []
+        for nl in self.noises:
+            wn = spl_to_amplitude(float(nl), self.spl_ref)
+            first = len(prof)
+            for pl in self.powers:
+                for f in self.frequencies:
+                    prof.append((spl_to_amplitude(float(pl), self.spl_ref), wn, float(f)))
+                    is_ref.append(False)
+            if self.calculate_jnd:
+                prof.append((0.0, wn, 0.0))
+                is_ref.append(True)
+                r = len(prof) - 1
+                ref_of += [r] * (r - first) + [r]
+            else:
+                ref_of += list(range(first, len(prof)))
+        p = np.array(prof, dtype=native.PROFILE_DTYPE)
+        return p, np.array(is_ref), np.array(ref_of, np.int32)
+
+
+@dataclass
+class JNDWindow:
+    """JND_Interval_Head / JND_Interval_Tail / JND_Delta_Alpha_Time_Factor."""
+    head: float = 0.014
+    tail: float = 0.002
+    delta_alpha_time_factor: float = 0.2
+    max_db: float = 150.0
+
+    def nodes(self, Fs: int, interval_len: int):
+        head = int(round(F32(Fs) * F32(self.head)))
+        length = interval_len - head - int(round(F32(Fs) * F32(self.tail)))
+        return head, length
+
+
+class ProfileRun:
+    """One Run_Cuda chunk in profile mode: a sweep of intervals of equal length
+    laid end to end, partitioned into Decouple_Filter blocks per interval."""
+
+    def __init__(self, device, cfg: RunConfig, sweep: ProfileSweep, noise: np.ndarray | None = None,
+                 nerve: NerveConfig | None = None, jnd: JNDWindow | None = None,
+                 mv: ModelVectors | None = None, ac_taps=None, want_lambda=True):
+        import torch
+        from .solver import BMSolver, units_to_device
+        self.torch = torch
+        self.device = torch.device(device)
+        self.cfg = cfg
+        self.lib = native.load()
+        self.mv = mv or ModelVectors.build()
+        self.prof, self.is_ref, self.ref_of = sweep.build()
+        self.n_int = len(self.prof)
+        if cfg.Decouple_Filter < 1:
+            raise ValueError("profile runs need Decouple_Filter >= 1")
+        cfg.Time_Blocks = self.n_int * cfg.Decouple_Filter
+        self.N = cfg.calc_time_block_nodes()
+        self.L = self.N * cfg.Decouple_Filter
+        self.sc = bm_scalars(cfg, self.mv)
+        self.units = reference_units(cfg)
+        self.rows = cfg.total_time_nodes_p1() + 4
+        self.bm = BMSolver(self.device, self.mv)
+        self.bm.check_units(self.units, 1, self.rows, self.rows)
+        self.d_units = units_to_device(self.units, self.device)
+        self.d_gamma = torch.from_numpy(cfg.gamma()[None].copy()).to(self.device)
+        self.d_prof = torch.from_numpy(self.prof.view(np.uint8).copy()).to(self.device)
+        self.d_in = torch.zeros(self.rows, dtype=torch.float32, device=self.device)
+        self.d_v = torch.zeros((self.rows, 256), dtype=torch.float32, device=self.device)
+        self.d_failed = torch.zeros(self.rows, dtype=torch.int32, device=self.device)
+        self.d_stats = torch.zeros((len(self.units), native.STATS_DTYPE.itemsize),
+                                   dtype=torch.uint8, device=self.device)
+        # noise (Input_Noise) and its normalisation (type 3: no energy scaling)
+        self.noise = None if noise is None else np.ascontiguousarray(noise[:self.L], np.float32)
+        self.d_wn = None if self.noise is None else torch.from_numpy(self.noise).to(self.device)
+        self.wn_dc, self.wn_norm, self.sig_norm = 0.0, 1.0, 1.0
+        self.want_lambda = want_lambda
+        self.nerve = nerve or NerveConfig()
+        self.jnd_win = jnd or JNDWindow()
+        if want_lambda:
+            self.ihc = IHCStage(self.device, self.nerve, cfg.IHC_Vector[None], ac_taps, cfg.Fs)
+            self.frames = reference_frame(cfg)
+            self.lam_rows = int(self.frames["lam_rows"][0])
+            self.d_lam = torch.zeros((3, self.lam_rows, 256), dtype=torch.float32,
+                                     device=self.device)
+        if sweep.calculate_jnd:
+            self.head, self.len = self.jnd_win.nodes(cfg.Fs, self.L)
+            self.d_dA = torch.from_numpy(np.ascontiguousarray(self.prof["dA"])).to(self.device)
+            self.d_ref = torch.from_numpy(self.ref_of).to(self.device)
+            self.d_nihc = torch.from_numpy(self.nerve.nihc()).to(self.device)
+            self.d_FRA = torch.zeros((3, self.n_int), dtype=torch.float64, device=self.device)
+            self.d_FAI = torch.zeros((3, self.n_int), dtype=torch.float64, device=self.device)
+        self.calc_jnd = sweep.calculate_jnd
+
+    @property
+    def audio_seconds(self) -> float:
+        return self.n_int * self.L / self.cfg.Fs
+
+    def _stream(self, stream):
+        s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
+        return C.c_void_p(s.cuda_stream)
+
+    def generate_input(self, stream=None):
+        native.check(self.lib.cgb_input_gen_dev(
+            native.ptr(self.d_prof), self.n_int, native.ptr(self.d_wn), None, 0, self.L, 0,
+            float(self.cfg.Fs), self.wn_dc, self.wn_norm, 0.0, self.sig_norm,
+            native.ptr(self.d_in), self._stream(stream)), "cgb_input_gen_dev")
+
+    def solve_bm(self, stream=None):
+        self.bm.run_dev(self.sc, self.d_gamma, self.d_units, len(self.units), self.d_in,
+                        self.d_v, self.d_failed, self.d_stats, stream)
+
+    def ihc_lambda(self, stream=None):
+        self.ihc.run_dev(self.d_v, self.frames, self.d_lam, None, stream)
+
+    def jnd_sums(self, stream=None):
+        W = np.asarray(self.nerve.W, np.float32)
+        native.check(self.lib.cgb_jnd_dev(
+            native.ptr(self.d_lam), self.lam_rows, self.n_int, self.L, self.head, self.len,
+            native.ptr(self.d_dA), native.ptr(self.d_ref), native.ptr(self.d_nihc),
+            native.ptr(W), float(self.cfg.Fs),
+            self.jnd_win.delta_alpha_time_factor * self.cfg.Fs,
+            native.ptr(self.d_FRA), native.ptr(self.d_FAI), self._stream(stream)), "cgb_jnd_dev")
+
+    def step(self, stream=None):
+        """One pass of the path over the whole sweep (device buffers only)."""
+        self.generate_input(stream)
+        self.solve_bm(stream)
+        if self.want_lambda:
+            self.ihc_lambda(stream)
+        if self.calc_jnd:
+            self.jnd_sums(stream)
+
+    def jnd_db(self):
+        F_RA = self.d_FRA.cpu().numpy()
+        F_AI = self.d_FAI.cpu().numpy()
+        rate = np.zeros(self.n_int)
+        ai = np.zeros(self.n_int)
+        native.check(self.lib.cgb_jnd_final(native.ptr(F_RA), native.ptr(F_AI), self.n_int,
+                                            native.ptr(self.ref_of), self.cfg.SPLRef,
+                                            self.jnd_win.max_db, native.ptr(rate),
+                                            native.ptr(ai)), "cgb_jnd_final")
+        return rate, ai, F_RA, F_AI

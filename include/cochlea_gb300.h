@@ -110,6 +110,14 @@ typedef struct cgb_ihc_params {
   int32_t pad_;
 } cgb_ihc_params;
 
+/* One generated input interval (the fields of device_jnd_params the input
+ * kernel reads, include/cochlea_common.h:56-66). */
+typedef struct cgb_profile {
+  double dA;         /* tone amplitude (dyn/cm^2), 0 for a noise-only interval */
+  double Wn;         /* noise amplitude                                          */
+  double frequency;  /* tone frequency (Hz)                                      */
+} cgb_profile;
+
 const char* cgb_last_error(void);
 int cgb_abi_version(void);
 
@@ -168,6 +176,42 @@ int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* fr
                        int n_dmg_profiles, const float* d_aihc, float* d_lam,
                        int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
                        int64_t scratch_bytes, int32_t* d_status, void* stream);
+
+/* Input generation: d_out[p*interval_len + n] for n < interval_len,
+ *   signal_mode 0: dA cos(2 pi f (n-head)/Fs)/sig_norm + Wn (wn[n]-wn_dc)/wn_norm
+ *   signal_mode 1: dA (signal[n]-sig_dc)/sig_norm    + Wn (wn[n]-wn_dc)/wn_norm
+ * in double, stored as float; d_wn may be null (no noise term). */
+int cgb_input_gen_dev(const cgb_profile* d_prof, int n_prof, const float* d_wn,
+                      const float* d_signal, int signal_mode, int interval_len, int head,
+                      float Fs, double wn_dc, double wn_norm, double sig_dc, double sig_norm,
+                      float* d_out, void* stream);
+
+/* DC and energy normalisation of a noise (or signal) array over the given
+ * windows; src == null gives the pure-tone factor sqrt(0.5 * window). */
+int cgb_noise_normalization(const float* src, int normalize_type, double normalize_to_interval,
+                            double remove_dc, int start_dc, int end_dc, int start_norm,
+                            int end_norm, float Fs, double* dc, double* factor);
+
+/* JND Fisher sums per interval and lambda plane (Eq. 17-24).
+ *   d_lam   float[3][plane_rows][256]; interval i occupies rows
+ *           [i*interval_nodes, (i+1)*interval_nodes), its window starts at +head
+ *           and is len rows long
+ *   d_dA    double[n_int] tone amplitude of each interval
+ *   d_ref_of int32[n_int] the noise-only reference interval of each interval
+ *           (ref_of[i] == i marks a reference)
+ *   d_nihc  double[256] nerve fibres per section; W: host float[3]
+ *   d_F_RA, d_F_AI  double[3][n_int] rate and all-information Fisher sums
+ * Time and section sums are FP64. */
+int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, int interval_nodes, int head,
+                int len, const double* d_dA, const int32_t* d_ref_of, const double* d_nihc,
+                const float* W, double Fs, double delta_alpha_len_factor, double* d_F_RA,
+                double* d_F_AI, void* stream);
+
+/* Final JND in dB SPL per interval from the Fisher sums (host arrays):
+ * 20 log10((1/sqrt(sum_j F_j)) / spl_ref), bounded at max_db; NaN for
+ * reference intervals. */
+int cgb_jnd_final(const double* F_RA, const double* F_AI, int n_int, const int32_t* ref_of,
+                  double spl_ref, double max_db, double* jnd_rate_db, double* jnd_ai_db);
 
 /* Host-side validation of a unit table against buffer sizes (the checks
  * cgb_bm_run_dev relies on); returns CGB_ERR_RANGE on the first bad unit. */

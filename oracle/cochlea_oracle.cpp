@@ -622,8 +622,22 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
                     double lambda_sat, float* ihc, float* lam, int64_t lam_stride,
                     int mode /*0: reference mixed precision, 1: all double, 2: kernel FP32*/) {
   if (mode == 2) {
-    // The GB300 kernel's arithmetic: float taps (AC taps pre-scaled),
-    // fmaf accumulation over taps in order, own log10, float lambda.
+    // The GB300 kernel's arithmetic: float taps (AC taps pre-scaled), each
+    // FIR summed over taps in order with the compensated dot product Dot2
+    // (Ogita, Rump, Oishi 2005), own log10, float lambda.
+    auto dot2 = [](const float* b, const float* x, int tu) {
+      float s = 0.0f, c = 0.0f;
+      for (int i = 0; i < tu; ++i) {
+        float p = b[i] * x[-(int64_t)i * NS];
+        float q = fmaf(b[i], x[-(int64_t)i * NS], -p);
+        float t = s + p;
+        float z = t - s;
+        float e = (s - (t - z)) + (p - z);
+        s = t;
+        c = c + (e + q);
+      }
+      return s + c;
+    };
     std::vector<float> acf((size_t)rows * NS), dsf((size_t)rows * NS);
     std::vector<float> bt(n_ac), dt(n_dc);
     for (int i = 0; i < n_ac; ++i) bt[i] = (float)(ac_taps[i] * scale);
@@ -632,8 +646,7 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
     for (int k = 0; k < lam_rows; ++k) {
       int tu = fir_taps_used(k, seg, frdp, total, n_ac);
       for (int s = 0; s < NS; ++s) {
-        float acc = 0.0f;
-        for (int i = 0; i < tu; ++i) acc = fmaf(bt[i], v[(size_t)(k - i) * NS + s], acc);
+        float acc = dot2(bt.data(), v + (size_t)k * NS + s, tu);
         acf[(size_t)k * NS + s] = acc;
         float ms = fmaf(v[(size_t)k * NS + s], sc, -acc);
         dsf[(size_t)k * NS + s] = ms * ms;
@@ -642,8 +655,7 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
     for (int k = 0; k < lam_rows; ++k) {
       int tu = fir_taps_used(k, seg, frdp, total, n_dc);
       for (int s = 0; s < NS; ++s) {
-        float acc = 0.0f;
-        for (int i = 0; i < tu; ++i) acc = fmaf(dt[i], dsf[(size_t)(k - i) * NS + s], acc);
+        float acc = dot2(dt.data(), dsf.data() + (size_t)k * NS + s, tu);
         float pre = fmaf(acf[(size_t)k * NS + s], ea, acc * ed);
         float y = (float)ihc_damage[s] * pre;
         float lg = own_log10f(fmaxf(y, 0.0f) + 1e-20f);

@@ -75,3 +75,38 @@ def test_section_packing(mv):
     assert sp[0, 10] == np.float32(1.0) / np.float32(mv.M[10])
     assert sp[1, 0] == np.float32(1.0) / np.float32(mv.diag_m[0])
     assert sp[1, 255] == 1.0
+
+
+def test_noise_normalization_matches_formula():
+    """calculateDCANDNornalizationFactor (src/cochlea.cu:4219-4254): the energy
+    starts from the first sample's raw square, later samples have the dc removed."""
+    from cochlearmodel_gb300 import native
+    lib = native.load()
+    rng = np.random.default_rng(1)
+    x = (rng.standard_normal(1000) + 0.3).astype(np.float32)
+    dc, fac = np.zeros(1), np.zeros(1)
+    for ntype, remove in ((0, 1.0), (1, 1.0), (2, 0.0), (3, 1.0)):
+        native.check(lib.cgb_noise_normalization(native.ptr(x), ntype, 0.16, remove, 100, 900,
+                                                 50, 950, 100000.0, native.ptr(dc),
+                                                 native.ptr(fac)))
+        d = remove * x[100:900].astype(np.float64).sum() / 800
+        e = float(x[50]) ** 2 + ((x[51:950].astype(np.float64) - d) ** 2).sum()
+        e = np.sqrt(e)
+        e = {0: e, 1: e / np.sqrt(900), 2: e / np.sqrt(100000.0 * 0.16), 3: 1.0}[ntype]
+        assert dc[0] == pytest.approx(d, rel=1e-12, abs=1e-15)
+        assert fac[0] == pytest.approx(e, rel=1e-12)
+    native.check(lib.cgb_noise_normalization(None, 0, 0.0, 0.0, 0, 10, 0, 800, 100000.0,
+                                             native.ptr(dc), native.ptr(fac)))
+    assert fac[0] == pytest.approx(np.sqrt(400.0)) and dc[0] == 0.0
+
+
+def test_profile_sweep_grid():
+    from cochlearmodel_gb300.pipeline import ProfileSweep
+    sw = ProfileSweep(frequencies=[1000.0], powers=[10.0 * k for k in range(1, 11)],
+                      noises=[1111.0, 0.0, 10.0, 20.0, 30.0, 40.0], calculate_jnd=True)
+    p, is_ref, ref_of = sw.build()
+    assert len(p) == 66 and is_ref.sum() == 6
+    assert list(np.flatnonzero(is_ref)) == [10, 21, 32, 43, 54, 65]
+    assert ref_of[0] == 10 and ref_of[11] == 21 and ref_of[65] == 65
+    assert p["Wn"][0] == 0.0 and p["dA"][10] == 0.0
+    assert p["dA"][5] == pytest.approx(10 * 10 ** (60 / 20) * 2e-5)
