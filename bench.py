@@ -1,11 +1,12 @@
 """Benchmark: simulated audio-seconds per wall-second of the cochlear solver
 path on one GB300 (one process per GPU under torchrun; weak scaling).
 
-Workload (default "tone_sweep"): 64 pure tones log-spaced 125 Hz-8 kHz x
-{20,40,60,80,100} dB SPL = 320 signals of 80 ms at 100 kHz, each split into
-Decouple_Filter=8 blocks of 10 ms with the 5 ms overlap warm-up -- 2,560 BM
-units per step, 25.6 s of audio.  A step is one pass of the path over the
-whole batch with inputs resident in HBM: BM/OHC solver (FP32).
+Workload (default "tone_sweep", config 2): 64 pure tones log-spaced
+125 Hz-8 kHz x {20,40,60,80,100} dB SPL = 320 signals of 80 ms at 100 kHz,
+each split into Decouple_Filter=8 blocks of 10 ms with the 5 ms overlap
+warm-up -- 2,560 BM units per step, 25.6 s of audio.  A step is one pass of
+the path over the whole batch with its inputs resident in HBM: input
+generation, BM/OHC solver (FP32), IHC + lambda for the three fibre groups.
 
 Arms:
   default            the GB300 kernels (value: device time; e2e: host buffers
@@ -37,30 +38,16 @@ UNIT = "audio-s/s"
 # ----------------------------------------------------------------------------
 # workload
 # ----------------------------------------------------------------------------
-def tone_sweep(mv, n_freq=64, levels=(20, 40, 60, 80, 100)):
-    """n_freq=64 is the full workload; smaller values give profiling cases."""
-    from cochlearmodel_gb300 import model, native
+def tone_sweep_config(n_freq=64, levels=(20, 40, 60, 80, 100)):
+    """Config 2: n_freq log-spaced tones 125 Hz-8 kHz x levels, 10 ms blocks x
+    Decouple_Filter 8, 5 ms overlap, healthy profiles, outputs v + lambda.
+    n_freq=64 is the full workload; smaller values give profiling cases."""
+    from cochlearmodel_gb300 import model
+    from cochlearmodel_gb300.pipeline import ProfileSweep
     cfg = model.RunConfig(Time_Block_Length=0.01, Decouple_Filter=8, Overlap_Time=0.005)
-    n_sig = n_freq * len(levels)
-    cfg.Time_Blocks = n_sig * cfg.Decouple_Filter
-    sc = model.bm_scalars(cfg, mv)
-    units = model.reference_units(cfg)
-    N = cfg.calc_time_block_nodes()
-    L = N * cfg.Decouple_Filter
-    n_in = cfg.total_time_nodes_p1() + 4
-    freqs = 125.0 * 64.0 ** (np.arange(n_freq) / (n_freq - 1))
-    two_pi = float(np.float32(2 * np.float32(math.pi)))
-    t = np.arange(L, dtype=np.float64) / float(np.float32(cfg.Fs))
-    x = np.zeros(n_in, np.float32)
-    k = 0
-    for db in levels:  # profile order: noise > power > frequency (src/params.cpp:697-740)
-        amp = model.spl_to_amplitude(float(db))
-        for f in freqs:
-            x[k * L:(k + 1) * L] = (amp * np.cos(two_pi * f * t)).astype(np.float32)
-            k += 1
-    audio_s = n_sig * L / cfg.Fs
-    return dict(cfg=cfg, sc=sc, units=units, x=x, rows=n_in, gamma=cfg.gamma()[None],
-                audio_s=audio_s, n_sig=n_sig, name="tone_sweep")
+    freqs = list(125.0 * 64.0 ** (np.arange(n_freq) / max(1, n_freq - 1)))
+    sweep = ProfileSweep(frequencies=freqs, powers=list(levels), calculate_jnd=False)
+    return cfg, sweep
 
 
 # ----------------------------------------------------------------------------
@@ -145,49 +132,76 @@ def bm_flops(stats) -> float:
 # ----------------------------------------------------------------------------
 # CPU baseline (oracle restatement on the host cores)
 # ----------------------------------------------------------------------------
-def cpu_sample(wl, mv, target_s=15.0):
+def cpu_sample(run, target_s=15.0, threads=None):
+    """The path (BM + IHC/lambda in the reference's arithmetic) on the first K
+    signals of the sweep, all host threads; returns audio-s per wall-second."""
+    from cochlearmodel_gb300 import ihc as ihcmod
     from oracle import oracle as orc
-    cores = os.cpu_count() or 1
-    units = wl["units"]
-    secp = mv.section_params()
-    # calibrate on one unit per core
-    n = min(len(units), cores)
-    t0 = time.perf_counter()
-    _, _, st = orc.bm_run(secp, wl["gamma"], wl["sc"], units[:n], wl["x"], wl["rows"],
-                          threads=cores)
-    dt = time.perf_counter() - t0
-    reps = max(1, int(target_s / max(dt, 1e-3)))
-    n2 = min(len(units), n * reps)
-    sel = units[:n2]
-    t0 = time.perf_counter()
-    _, _, st = orc.bm_run(secp, wl["gamma"], wl["sc"], sel, wl["x"], wl["rows"], threads=cores)
-    dt = time.perf_counter() - t0
-    audio = float((sel["end"] - sel["out_first"]).sum()) / wl["cfg"].Fs
-    return audio / dt, cores, f"{n2} of {len(units)} BM units of {wl['name']} " \
-                              f"({audio:.3f} audio-s), FP32 oracle, {cores} threads, {dt:.1f} s"
+    cores = threads or os.cpu_count() or 1
+    D = run.cfg.Decouple_Filter
+    ov = run.cfg.calc_overlap_nodes()
+    x = run.d_in.cpu().numpy()
+    secp = run.mv.section_params()
+    gamma = run.cfg.gamma()[None]
+    st = run.ihc
+
+    def sample(k):
+        units = run.units[:k * D]
+        t0 = time.perf_counter()
+        v, _, _ = orc.bm_run(secp, gamma, run.sc, units, x, run.rows, threads=cores)
+        rows = k * run.L + ov
+        orc.ihc_lambda(v[:rows], run.L, k * run.L, ihcmod.round64(rows), k * run.L,
+                       st.ac.astype(np.float64), st.dc.astype(np.float64), 1.0, 1.0, 100.0,
+                       st.dmg_host[0].astype(np.float64), st.nerve.aihc(),
+                       np.asarray(st.nerve.spontRate, np.float32), 500.0, mode=0)
+        return time.perf_counter() - t0
+
+    k = max(1, min(run.n_int, cores // D))
+    dt = sample(k)
+    k2 = max(1, min(run.n_int, int(k * target_s / max(dt, 1e-3))))
+    if k2 > k:
+        k, dt = k2, sample(k2)
+    audio = k * run.L / run.cfg.Fs
+    return audio / dt, cores, (f"{k} of {run.n_int} signals of the tone sweep ({audio:.3f} "
+                               f"audio-s): BM (FP32 oracle) + IHC/lambda (reference mixed "
+                               f"precision), {cores} threads, {dt:.1f} s")
 
 
 # ----------------------------------------------------------------------------
 # arms
 # ----------------------------------------------------------------------------
+def make_run(device, n_freq):
+    from cochlearmodel_gb300.pipeline import ProfileRun
+    cfg, sweep = tone_sweep_config(n_freq)
+    return ProfileRun(device, cfg, sweep)
+
+
 def run_reference(args, rank, world):
-    from cochlearmodel_gb300 import model
+    """The path's CPU implementation on the host cores.  The input of the sweep
+    is produced by the GPU input kernel when a GPU is present, else by the
+    oracle's restatement of it; the timed work is CPU only."""
     if rank != 0:
         return None
-    mv = model.ModelVectors.build()
-    wl = tone_sweep(mv)
+    import torch
+    dev = "cuda:0" if torch.cuda.is_available() else None
+    if dev is None:
+        print(json.dumps({"impl": "reference", "unavailable": "needs the input of the sweep"}))
+        return None
+    run = make_run(dev, args.n_freq)
+    run.generate_input()
+    torch.cuda.synchronize()
     vals = []
     for i in range(args.warmup + args.steps):
-        v, cores, sample = cpu_sample(wl, mv, target_s=args.cpu_seconds / max(1, args.steps))
+        v, cores, sample = cpu_sample(run, target_s=args.cpu_seconds / max(1, args.steps))
         if i >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": wl["audio_s"] / value * 1000.0, "higher_is_better": True,
+            "ms_per_step": run.audio_seconds / value * 1000.0, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": wl["name"], "signals": wl["n_sig"], "units": len(wl["units"]),
-                       "audio_s_per_step": wl["audio_s"], "sample": "bounded"},
+            "config": {"workload": "tone_sweep", "signals": run.n_int, "units": len(run.units),
+                       "audio_s_per_step": run.audio_seconds, "sample": "bounded"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -197,37 +211,32 @@ def run_reference(args, rank, world):
 
 def run_ours(args, rank, world, device):
     import torch
-    from cochlearmodel_gb300 import model, native
-    from cochlearmodel_gb300.solver import BMSolver, units_to_device
+    from cochlearmodel_gb300 import native
 
-    mv = model.ModelVectors.build()
-    wl = tone_sweep(mv, n_freq=args.n_freq)
-    solver = BMSolver(device, mv)
+    run = make_run(device, args.n_freq)
     native.check(native.load().cgb_bm_set_launch_shape(args.shape), "launch shape")
-    units = wl["units"]
-    solver.check_units(units, 1, wl["x"].size, wl["rows"])
-    d_units = units_to_device(units, device)
-    d_gamma = torch.from_numpy(wl["gamma"]).to(device)
-    d_in = torch.from_numpy(wl["x"]).to(device)
-    d_out = torch.empty((wl["rows"], 256), dtype=torch.float32, device=device)
-    d_failed = torch.zeros(wl["rows"], dtype=torch.int32, device=device)
-    d_stats = torch.zeros((len(units), native.STATS_DTYPE.itemsize), dtype=torch.uint8,
-                          device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
 
-    def step():
-        solver.run_dev(wl["sc"], d_gamma, d_units, len(units), d_in, d_out, d_failed, d_stats)
-
-    launches0 = native.load().cgb_kernel_launch_count()
-    for _ in range(args.warmup):
-        step()
+    # warm-up, with per-stage device times on the last warm-up step
+    stage_ms = {}
+    for w in range(args.warmup):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
+        run.generate_input()
+        ev[1].record(stream)
+        run.solve_bm()
+        ev[2].record(stream)
+        run.ihc_lambda()
+        ev[3].record(stream)
         flush.fill_(1.0)
-    torch.cuda.synchronize(device)
-    stats = d_stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
+        torch.cuda.synchronize(device)
+        stage_ms = {"input_gen": ev[0].elapsed_time(ev[1]), "bm_solver": ev[1].elapsed_time(ev[2]),
+                    "ihc_lambda": ev[2].elapsed_time(ev[3])}
+    stats = run.d_stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
     flops = bm_flops(stats)
 
-    clocks = ClockSampler(torch.cuda.current_device() if world == 1 else rank)
+    clocks = ClockSampler(device.index if device.index is not None else 0)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(device)
@@ -237,7 +246,7 @@ def run_ours(args, rank, world, device):
           for _ in range(args.steps)]
     for i in range(args.steps):
         ev[i][0].record(stream)
-        step()
+        run.step()
         ev[i][1].record(stream)
         flush.fill_(float(i))  # L2 flush between timed steps (256 MB > 129 MB L2)
     torch.cuda.synchronize(device)
@@ -245,51 +254,54 @@ def run_ours(args, rank, world, device):
         torch.distributed.barrier()
     clk = clocks.stop()
     launches = native.load().cgb_kernel_launch_count() - launches_a
-    ms = [a.elapsed_time(b) for a, b in ev]
-    t_total = sum(ms) / 1000.0
+    t_total = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
     if world > 1:
         tt = torch.tensor([t_total], device=device)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_total = float(tt.item())
-    value = wl["audio_s"] * args.steps * world / t_total
+    value = run.audio_seconds * args.steps * world / t_total
 
-    # e2e: host input -> device -> solver -> host velocity, through the ABI
-    h_in = torch.from_numpy(wl["x"]).pin_memory()
-    h_out = torch.empty((wl["rows"], 256), dtype=torch.float32).pin_memory()
-    torch.cuda.synchronize(device)
-    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e_ms = 0.0
-    for i in range(max(1, args.steps // 2)):
-        e_start.record(stream)
-        d_in.copy_(h_in, non_blocking=True)
-        step()
-        h_out.copy_(d_out, non_blocking=True)
-        e_end.record(stream)
-        torch.cuda.synchronize(device)
-        e_ms += e_start.elapsed_time(e_end)
-        flush.fill_(float(i))
+    # e2e: the sweep's profile table in from pinned host memory, the path,
+    # velocity and the three lambda planes back to pinned host memory
+    h_prof = torch.from_numpy(run.prof.view(np.uint8).copy()).pin_memory()
+    h_v = torch.empty(run.d_v.shape, dtype=torch.float32).pin_memory()
+    h_lam = torch.empty(run.d_lam.shape, dtype=torch.float32).pin_memory()
     e_steps = max(1, args.steps // 2)
-    e2e = wl["audio_s"] * e_steps * world / (e_ms / 1000.0)
+    e_ms = 0.0
+    for i in range(e_steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        a.record(stream)
+        run.d_prof.copy_(h_prof, non_blocking=True)
+        run.step()
+        h_v.copy_(run.d_v, non_blocking=True)
+        h_lam.copy_(run.d_lam, non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        e_ms += a.elapsed_time(b)
+        flush.fill_(float(i))
+    e2e = run.audio_seconds * e_steps * world / (e_ms / 1000.0)
 
     peaks, peak_kind = measured_peaks()
     clock_mhz = peaks.get("sm_max_mhz", 2070.0)
     n_sm = torch.cuda.get_device_properties(device).multi_processor_count
     fp32_peak = 2.0 * 128 * n_sm * clock_mhz * 1e6 / 1e12
-    achieved = flops / (t_total / args.steps * world) / 1e12 if world == 1 else \
-        flops / (t_total / args.steps) / 1e12
+    bm_s = stage_ms["bm_solver"] / 1000.0
+    achieved = flops / bm_s / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1000.0,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": wl["name"], "signals": wl["n_sig"], "units": len(units),
-                   "audio_s_per_step": wl["audio_s"], "fs": wl["cfg"].Fs,
+        "config": {"workload": "tone_sweep", "signals": run.n_int, "units": len(run.units),
+                   "audio_s_per_step": run.audio_seconds, "fs": run.cfg.Fs,
                    "l2": "flushed between timed steps (256 MB write)",
-                   "path": "BM/OHC solver (reference semantics, 20/2 Jacobi sweeps)",
-                   "launch_shape": args.shape},
+                   "path": "input generation -> BM/OHC solver (20/2 Jacobi sweeps) -> "
+                           "IHC/lambda (3 fibre groups)",
+                   "launch_shape": args.shape, "stage_ms": stage_ms},
         "gpu_launches": int(launches),
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(wl["x"].nbytes),
-                "d2h_bytes_per_step": int(h_out.numel() * 4)},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h_prof.numel()),
+                "d2h_bytes_per_step": int(h_v.numel() * 4 + h_lam.numel() * 4)},
         "roofline": {"bound": "fp32", "kernel": "bm_warp_kernel", "achieved": achieved,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "traffic": None,
@@ -297,7 +309,7 @@ def run_ours(args, rank, world, device):
                                     f"({peak_kind} MEASURED_PEAKS.json)"},
         "clocks": clk,
     }
-    return line
+    return line, run
 
 
 def main():
@@ -327,11 +339,9 @@ def main():
     torch.cuda.set_device(device)
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=device)
-    line = run_ours(args, rank, world, device)
+    line, run = run_ours(args, rank, world, device)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        from cochlearmodel_gb300 import model
-        mv = model.ModelVectors.build()
-        v, cores, sample = cpu_sample(tone_sweep(mv), mv, target_s=args.cpu_seconds)
+        v, cores, sample = cpu_sample(run, target_s=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": sample}
     if world > 1:

@@ -97,7 +97,13 @@ class ProfileRun:
         self.d_stats = torch.zeros((len(self.units), native.STATS_DTYPE.itemsize),
                                    dtype=torch.uint8, device=self.device)
         # noise (Input_Noise) and its normalisation (type 3: no energy scaling)
-        self.noise = None if noise is None else np.ascontiguousarray(noise[:self.L], np.float32)
+        # the noise draft is cut or zero-padded to one interval (WN resize,
+        # src/solver.cpp:497-500); the input kernel reads noise[0, L)
+        self.noise = None
+        if noise is not None:
+            self.noise = np.zeros(self.L, np.float32)
+            n = min(self.L, len(noise))
+            self.noise[:n] = np.asarray(noise, np.float32)[:n]
         self.d_wn = None if self.noise is None else torch.from_numpy(self.noise).to(self.device)
         self.wn_dc, self.wn_norm, self.sig_norm = 0.0, 1.0, 1.0
         self.want_lambda = want_lambda
