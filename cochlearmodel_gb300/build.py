@@ -58,14 +58,33 @@ def lib_path() -> Path:
     return LIBDIR / LIBNAME
 
 
+HARNESS = PKG / "harness" / "run_cuda_harness.cpp"
+
+
+def harness_path() -> Path:
+    return LIBDIR / "run_cuda_harness"
+
+
+def build_harness() -> Path:
+    """The Run_Cuda-order host harness over the reference-named API."""
+    out = harness_path()
+    cmd = [nvcc(), "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(HARNESS), "-o",
+           str(out), "-L", str(LIBDIR), "-lcochlea_gb300", "-lcudart",
+           "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"harness build failed:\n{res.stdout}\n{res.stderr}")
+    return out
+
+
 def up_to_date() -> bool:
     lib = lib_path()
     if not lib.exists():
         return False
     t = lib.stat().st_mtime
     deps = sources() + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + \
-        list((ROOT / "include").glob("*.h")) + [Path(__file__)]
-    return all(d.stat().st_mtime <= t for d in deps)
+        list((ROOT / "include").glob("*.h")) + [Path(__file__), HARNESS]
+    return harness_path().exists() and all(d.stat().st_mtime <= t for d in deps)
 
 
 def build(force: bool = False, jobs: int | None = None) -> Path:
@@ -82,6 +101,7 @@ def build(force: bool = False, jobs: int | None = None) -> Path:
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, lib_path())
+    build_harness()
     return lib_path()
 
 

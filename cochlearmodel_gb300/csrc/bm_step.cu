@@ -39,6 +39,7 @@ struct BMArgs {
   const float* in;
   float* out;
   int32_t* failed;
+  float* conv;  // [rows][3] mean dt, substeps, mean outer iterations per sample
   cgb_unit_stats* stats;
   int32_t* work;
   float ratio, nas, al, e1, e2, nw, ar, dx2, dxa0, na1, na2, gme, sow;
@@ -130,6 +131,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   const float* inb = A.in + un.in_base;
   float* outb = A.out + un.out_base * 256;
   int32_t* fb = A.failed ? A.failed + un.out_base : nullptr;
+  float* cb = A.conv ? A.conv + un.out_base * 3 : nullptr;
 
   float dt = A.dt0;
   double tau = 0.0;
@@ -138,6 +140,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   int fail_flag = 0;
   long long n_sub = 0, n_it = 0, n_sw = 0;
   int n_failed = 0, n_written = 0, status = 0, sub_in_sample = 0;
+  float smp_dt = 0.0f, smp_sub = 0.0f, smp_it = 0.0f;  // per-sample sums
 
   while (n < un.end) {
     if (++sub_in_sample > A.max_sub) {  // dt collapsed: stop this unit, flag it
@@ -325,6 +328,9 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
     } while (another);
     ++n_sub;
     n_it += out_loop;
+    smp_sub = __fadd_rn(smp_sub, 1.0f);
+    smp_dt = __fadd_rn(smp_dt, dt);
+    smp_it = __fadd_rn(smp_it, (float)out_loop);
 
     if (tau > A.tout) {
       tau -= A.tout;
@@ -335,11 +341,17 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         o[0] = make_float4(v[0], v[1], v[2], v[3]);
         o[1] = make_float4(v[4], v[5], v[6], v[7]);
         if (fb && lane == 0) fb[n] = fail_flag;
+        if (cb && lane == 0) {
+          cb[(int64_t)n * 3 + 0] = __fdiv_rn(smp_dt, smp_sub);
+          cb[(int64_t)n * 3 + 1] = smp_sub;
+          cb[(int64_t)n * 3 + 2] = __fdiv_rn(smp_it, smp_sub);
+        }
         ++n_written;
         n_failed += fail_flag;
       }
       fail_flag = 0;
       sub_in_sample = 0;
+      smp_dt = smp_sub = smp_it = 0.0f;
       ++n;
     }
     prev.store(0, base, x);
@@ -435,7 +447,8 @@ extern "C" int cgb_bm_launch_shape_count(void) {
 extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
                               const cgb_bm_scalars* sc, const cgb_unit* d_units, int n_units,
                               const float* d_in, int64_t in_len, float* d_out,
-                              int64_t out_rows, int32_t* d_failed, cgb_unit_stats* d_stats,
+                              int64_t out_rows, int32_t* d_failed, float* d_conv,
+                              cgb_unit_stats* d_stats,
                               int32_t* d_work, void* stream) {
   using namespace cgb;
   if (n_units == 0) return CGB_OK;  // an empty table enqueues nothing
@@ -459,6 +472,7 @@ extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_p
   A.in = d_in;
   A.out = d_out;
   A.failed = d_failed;
+  A.conv = d_conv;
   A.stats = d_stats;
   A.work = d_work;
   A.ratio = sc->alpha_l / sc->alpha_s;

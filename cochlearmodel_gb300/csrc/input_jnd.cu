@@ -53,7 +53,8 @@ __global__ void __launch_bounds__(kJndThreads)
     jnd_kernel(const float* __restrict__ lam, int64_t plane_rows, int interval_nodes, int head,
                int len, const double* __restrict__ dA, const int32_t* __restrict__ ref_of,
                const double* __restrict__ nihc, double w0, double w1, double w2, double Fs,
-               double T, double* __restrict__ F_RA, double* __restrict__ F_AI, int n_int) {
+               double T, double* __restrict__ F_RA, double* __restrict__ F_AI,
+               double* __restrict__ MR, int n_int) {
   const int i = blockIdx.x, j = blockIdx.y, s = threadIdx.x;
   const int r = ref_of[i];
   const float* c = lam + ((int64_t)j * plane_rows + (int64_t)i * interval_nodes + head) * 256 + s;
@@ -85,6 +86,7 @@ __global__ void __launch_bounds__(kJndThreads)
   }
   const double da = dA[i];
   const double mr = sum_c / len, mrr = sum_r / len;
+  if (MR) MR[((int64_t)j * n_int + i) * 256 + s] = mr;
   const double tl = (double)len / Fs;
   double rate = 0.0, ai = 0.0;
   if (da > 0.0) {
@@ -147,7 +149,7 @@ extern "C" int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, in
                            int head, int len, const double* d_dA, const int32_t* d_ref_of,
                            const double* d_nihc, const float* W, double Fs,
                            double delta_alpha_len_factor, double* d_F_RA, double* d_F_AI,
-                           void* stream) {
+                           double* d_MR, void* stream) {
   using namespace cgb;
   if (n_int == 0) return CGB_OK;
   if (!d_lam || !d_dA || !d_ref_of || !d_nihc || !W || !d_F_RA || !d_F_AI || n_int < 0 ||
@@ -161,7 +163,7 @@ extern "C" int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, in
   dim3 grid((unsigned)n_int, 3);
   jnd_kernel<<<grid, kJndThreads, 0, st>>>(d_lam, plane_rows, interval_nodes, head, len, d_dA,
                                            d_ref_of, d_nihc, (double)W[0], (double)W[1],
-                                           (double)W[2], Fs, T, d_F_RA, d_F_AI, n_int);
+                                           (double)W[2], Fs, T, d_F_RA, d_F_AI, d_MR, n_int);
   CGB_TRY_CUDA(cudaGetLastError(), "jnd_kernel launch");
   note_launch();
   return CGB_OK;

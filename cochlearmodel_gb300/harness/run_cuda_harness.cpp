@@ -1,0 +1,310 @@
+// Linux host harness for the reference-named API (include/cochlea_common.h).
+//
+// Replays the call order the reference's CSolver::Run_Cuda uses in profile
+// mode (src/solver.cpp:234-962; AudioGramCreator::runInCuda/calcJND,
+// src/AudioGramCreator.cpp:261-313, 829-974): model setup, profile grid,
+// BMOHCKernel_Init, input generation on the GPU, BMOHCNewKernel, velocity
+// copy-back, IHCNewKernel + RunIHCKernel, lambda copy-back, CudaCalculateJND
+// and the final JND in dB.  Parameters come from a key = value file in the
+// grammar of the reference's .par files (src/ConfigFileHandler.cpp:31-59).
+//
+// Output (little-endian): int64 header {rows, lam_rows, n_intervals, n_ac},
+// float velocity[rows][256], float lambda[3][lam_rows][256],
+// float F_RA[3][n], float FisherAI[3][n], double jnd_rate_db[n],
+// double jnd_ai_db[n].
+//
+// usage: run_cuda_harness <params.par>
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <regex>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cochlea_common.h"
+#include "cochlea_gb300.h"
+
+class Log {};  // the caller's logger; the library never dereferences it
+
+namespace {
+
+std::map<std::string, std::string> parse_par(const std::string& path) {
+  std::ifstream f(path);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  std::map<std::string, std::string> m;
+  const std::regex kv("^\\s*([_[:alnum:]]+)\\s*=\\s*(\"(.*)\"|([^\"\\r\\n]+))$");
+  std::string line;
+  while (std::getline(f, line)) {
+    std::smatch s;
+    if (std::regex_match(line, s, kv)) m[s[1]] = s[3].matched ? s[3].str() : s[4].str();
+  }
+  return m;
+}
+
+std::vector<double> numbers(const std::string& v) {
+  std::string t = v;
+  for (char& c : t)
+    if (c == ',' || c == '[' || c == ']' || c == ';') c = ' ';
+  std::istringstream is(t);
+  std::vector<double> out;
+  double x;
+  while (is >> x) out.push_back(x);
+  return out;
+}
+
+struct Par {
+  std::map<std::string, std::string> m;
+  double num(const std::string& k, double def) const {
+    auto it = m.find(k);
+    return it == m.end() ? def : std::stod(it->second);
+  }
+  std::vector<double> vec(const std::string& k, std::vector<double> def) const {
+    auto it = m.find(k);
+    return it == m.end() ? def : numbers(it->second);
+  }
+  std::string str(const std::string& k, const std::string& def) const {
+    auto it = m.find(k);
+    return it == m.end() ? def : it->second;
+  }
+};
+
+// expandVectorToSize (include/cvector.cpp:609-623)
+std::vector<float> expand(const std::vector<double>& v, size_t n) {
+  std::vector<float> out;
+  const size_t times = n / v.size(), rem = n % v.size();
+  for (size_t i = 0; i < v.size(); ++i) {
+    for (size_t k = 0; k < times; ++k) out.push_back((float)v[i]);
+    if (i < rem) out.push_back((float)v[i]);
+  }
+  return out;
+}
+
+std::vector<float> read_f32(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("cannot open " + path);
+  std::vector<char> b((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  std::vector<float> v(b.size() / 4);
+  std::memcpy(v.data(), b.data(), v.size() * 4);
+  return v;
+}
+
+double spl2pa(double db, double ref) { return db == 1111.0 ? 0.0 : 10.0 * std::pow(10.0, db / 20.0) * ref; }
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 2) {
+    std::fprintf(stderr, "usage: %s <params.par>\n", argv[0]);
+    return 2;
+  }
+  try {
+    Par P{parse_par(argv[1])};
+    Log log;
+    const long Fs = (long)P.num("Fs", 100000);
+    const float tbl = (float)P.num("Time_Block_Length", 0.01);
+    const int D = (int)P.num("Decouple_Filter", 1);
+    const double ov_time = P.num("Overlap_Time", 0.005);
+    const double spl_ref = P.num("SPLRef", 2e-5);
+    const bool calc_jnd = P.num("Calculate_JND", 0) != 0;
+    const auto freqs = P.vec("testedFrequencies", {1000.0});
+    const auto powers = P.vec("testedPowerLevels", {60.0});
+    const auto noises = P.vec("testedNoises", {1111.0});
+    const auto ohc = expand(P.vec("OHC_Vector", {0.5}), 256);
+    const auto ihcv = expand(P.vec("IHC_Vector", {8.0}), 256);
+
+    // node counts (include/params.h:288-395)
+    const long ov_us = (long)(std::round(ov_time * 1000) * 1000);
+    const int overlap = (int)(ov_us * Fs / 1000000);
+    const int N = (int)std::ceil((float)Fs * tbl);
+    const int L = N * D;
+
+    // profile grid (src/params.cpp:661-782), one reference per noise level
+    std::vector<device_jnd_params> prof;
+    std::vector<int> ref_pos;
+    for (double nl : noises) {
+      const double wn = spl2pa(nl, spl_ref);
+      for (double pl : powers)
+        for (double f : freqs) {
+          device_jnd_params p{};
+          p.dBSPLSignal = pl;
+          p.dBSPLNoise = nl != 1111.0 ? nl : 0.0;
+          p.dA = spl2pa(pl, spl_ref);
+          p.recipdA = p.dA > 0 ? 1.0 / p.dA : 0.0;
+          p.Wn = wn;
+          p.frequency = f;
+          p.calculateIndexPosition = (int)prof.size();
+          prof.push_back(p);
+        }
+      if (calc_jnd) {
+        device_jnd_params p{};
+        p.dBSPLNoise = nl != 1111.0 ? nl : 0.0;
+        p.Wn = wn;
+        p.isReference = true;
+        p.referenceIndex = (int)prof.size();
+        p.calculateIndexPosition = -1;
+        ref_pos.push_back((int)prof.size());
+        prof.push_back(p);
+      }
+    }
+    const int n_int = (int)prof.size();
+    const int TB = n_int * D;
+    const int64_t samples_p1 = (int64_t)overlap + (int64_t)N * (TB + 1);
+    const int64_t total_nodes = (int64_t)overlap + (int64_t)N * TB;
+
+    // model (src/solver.cpp:357-376)
+    double M[256], R[256], S[256], Q[256], So[256], St[256], Rt[256], dm[256], dl[256], du[256],
+        sc[16];
+    if (cgb_model_setup(M, R, S, Q, So, St, Rt, dm, dl, du, sc) != CGB_OK)
+      throw std::runtime_error(cgb_last_error());
+    std::vector<float> gamma(ohc), mass(256), rsm(256), uu(256), ll(256), Rf(256), Sf(256),
+        Qf(256), Sof(256), Stf(256), Rtf(256);
+    for (int i = 0; i < 256; ++i) {
+      mass[i] = (float)M[i];
+      rsm[i] = 1.0f / (float)dm[i];
+      uu[i] = (float)du[i];
+      ll[i] = (float)dl[i];
+      Rf[i] = (float)R[i];
+      Sf[i] = (float)S[i];
+      Qf[i] = (float)Q[i];
+      Sof[i] = (float)So[i];
+      Stf[i] = (float)St[i];
+      Rtf[i] = (float)Rt[i];
+    }
+    BMOHCKernel_Init(gamma.data(), mass.data(), rsm.data(), uu.data(), ll.data(), Rf.data(),
+                     Sf.data(), Qf.data(), Sof.data(), Stf.data(), Rtf.data(), 1.0f, 0.0f,
+                     (size_t)samples_p1 + 4, (size_t)(samples_p1 + 4) * 256, 0, true, 0, 0, log);
+
+    // input generation on the GPU
+    std::vector<float> noise(L, 0.0f);
+    const std::string nf = P.str("Input_Noise_File", "");
+    if (!nf.empty()) {
+      auto v = read_f32(nf);
+      for (int i = 0; i < L && i < (int)v.size(); ++i) noise[i] = v[i];
+    }
+    std::vector<float> signal(L, 0.0f);
+    InputProfilesArrayInitialization(n_int, L, L, 0, 0);
+    generateInputFromProfile(prof.data(), noise.data(), L, signal.data(), L, 0,
+                             (int)P.num("Normalize_Sigma_Type", 3),
+                             (int)P.num("Normalize_Sigma_Type_Signal", 3), 0.16, 0.0, 0, 0, 0, 0,
+                             n_int, false, 0, n_int, overlap, L, 0, L, (float)Fs, 0, nullptr,
+                             false, true, (float)P.num("MAX_M1_SP_ERROR", 1e-15),
+                             (float)P.num("MAX_TOLERANCE", 1e-10), 0, 0.0f, 0.0f, D, 0, nullptr,
+                             0, nullptr, 0, log);
+
+    // BM solver
+    cudaEvent_t e0{}, e1{};
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, 0);
+    const float time_step = 1e-6f;
+    const int iters = (int)(1.0f / ((float)Fs * 1e-6f));
+    const float time_step_out = time_step * (float)iters;
+    float tres = 0.0f;
+    BMOHCNewKernel(nullptr, true, (float)sc[0], time_step, time_step_out, (float)sc[1],
+                   (float)sc[2], 1, 1, 0, (float)(1.0 / (double)Fs), (float)sc[3], (float)sc[4],
+                   (float)sc[5], (float)sc[6], (float)sc[7], (float)sc[8], (float)sc[9],
+                   (float)sc[10], (float)sc[11], &tres, TB, (int)samples_p1, overlap, ov_us, 1,
+                   1e-6f, 1e-18f, D, (float)P.num("MAX_M1_SP_ERROR", 1e-15),
+                   (float)P.num("MAX_TOLERANCE", 1e-10), 0, 0, 0.0f, 0.0f, (float)spl_ref, 0, 0,
+                   0, (int)P.num("JACOBBY_Loops_Fast", 2), (int)P.num("JACOBBY_Loops_Slow", 20),
+                   (int)P.num("Cuda_Outern_Loops", 10), 17, 0, e0, e1, prop, log);
+    std::vector<float> v((size_t)total_nodes * 256);
+    BMOHCKernel_Copy_Results(v.data(), v.size(), 0);
+
+    // IHC + lambda (AudioGramCreator::runInCuda)
+    const auto ac = read_f32(P.str("AC_Filter_File", ""));
+    std::vector<double> acd(ac.begin(), ac.end());
+    const int dc_n = (int)std::round((float)Fs * 2e-3f);
+    std::vector<double> dcd(dc_n, (double)(1.0f / ((float)Fs * 2e-3f)));
+    std::vector<double> dmg(256);
+    for (int i = 0; i < 256; ++i) dmg[i] = std::pow(10.0, (double)ihcv[i]);
+    std::vector<float> aihc = expand({70.0, 50.0, 30.0}, 768);
+    float clusters[9] = {60.0f, 3.0f, 0.1f, 70.0f, 50.0f, 30.0f, 0.61f, 0.23f, 0.16f};
+    const int write_time = (int)total_nodes;
+    const int calc_time = (write_time + 63) / 64 * 64;
+    enableloadAihc();
+    loadAihc(aihc.data());
+    IHCNewKernel(dmg.data(), clusters, dcd.data(), dc_n, acd.data(), acd.data(), false,
+                 (int)acd.size(), 256, TB, spl_ref, nullptr, 0, calc_time, write_time,
+                 (int)(samples_p1 + 4), N, 0, 0, 500.0f, 1.0f, 100.0f, true, true, false, true,
+                 false, false, 1.0f, calc_jnd, n_int, overlap, D, 0, log);
+    allocateBuffer(LAMBDA_COUNT * calc_time * 256, 0, e0, e1, prop);
+    RunIHCKernel(nullptr, 0, 1, -1, 0, log);
+    std::vector<float> lam((size_t)LAMBDA_COUNT * calc_time * 256);
+    BMOHCKernel_Copy_Lambda(lam.data(), lam.size(), 0);
+    const int lam_rows = N * TB;
+
+    // JND (AudioGramCreator::calcJND / calcJNDFinal)
+    std::vector<float> FRA(3 * n_int, 0.0f), FAI(3 * n_int, 0.0f);
+    std::vector<double> jr(n_int, NAN), ja(n_int, NAN);
+    if (calc_jnd) {
+      const int head = (int)std::round((float)Fs * (float)P.num("JND_Interval_Head", 0.014));
+      const int tail = (int)std::round((float)Fs * (float)P.num("JND_Interval_Tail", 0.002));
+      const int len = L - head - tail;
+      std::vector<int> serial(n_int), calc_pos, to_ref;
+      int ci = 0;
+      for (int i = 0; i < n_int; ++i) {
+        const int rr = i * (int)ref_pos.size() / n_int;
+        bool isref = false;
+        for (int r : ref_pos) isref |= r == i;
+        if (!isref) {
+          serial[i] = ci++;
+          calc_pos.push_back(i);
+          to_ref.push_back(ref_pos[rr]);
+        } else {
+          serial[i] = rr;
+        }
+      }
+      std::vector<double> nihc(256, (double)(30000.0f / 256.0f));
+      CudaCalculateJND(true, true, n_int * 3 * 256, 3 * n_int, spl_ref, (double)Fs, 1.0,
+                       nihc.data(), calc_pos.data(), (int)calc_pos.size(), ref_pos.data(),
+                       (int)ref_pos.size(), 0, n_int, n_int, head, overlap, L, len,
+                       serial.data(), to_ref.data(), FRA.data(), FAI.data(), write_time * 256,
+                       calc_time * 256, 0.2 * (double)Fs, 1, 0, false, false, -1, log);
+      for (int i = 0; i < n_int; ++i) {
+        bool isref = false;
+        for (int r : ref_pos) isref |= r == i;
+        if (isref) continue;
+        double ra = 0, ai = 0;
+        for (int j = 0; j < 3; ++j) {
+          ra += FRA[j * n_int + i];
+          ai += FAI[j * n_int + i];
+        }
+        const double max_pa = std::pow(10.0, 150.0 / 20.0) * spl_ref;
+        auto db = [&](double s) {
+          const double pa = 1.0 / std::sqrt(s);
+          return (std::isinf(pa) || pa > max_pa) ? 150.0 : 20.0 * std::log10(pa / spl_ref);
+        };
+        jr[i] = db(ra);
+        ja[i] = db(ai);
+      }
+    }
+
+    std::ofstream out(P.str("Output_File", "harness_out.bin"), std::ios::binary);
+    const int64_t hdr[4] = {total_nodes, lam_rows, n_int, (int64_t)acd.size()};
+    out.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
+    out.write(reinterpret_cast<const char*>(v.data()), v.size() * 4);
+    for (int j = 0; j < 3; ++j)
+      out.write(reinterpret_cast<const char*>(lam.data() + (size_t)j * calc_time * 256),
+                (size_t)lam_rows * 256 * 4);
+    out.write(reinterpret_cast<const char*>(FRA.data()), FRA.size() * 4);
+    out.write(reinterpret_cast<const char*>(FAI.data()), FAI.size() * 4);
+    out.write(reinterpret_cast<const char*>(jr.data()), jr.size() * 8);
+    out.write(reinterpret_cast<const char*>(ja.data()), ja.size() * 8);
+    IHCKernel_Free();
+    BMOHCKernel_Free();
+    InputProfilesArrayTermination();
+    std::printf("harness ok: %lld rows, %d intervals\n", (long long)total_nodes, n_int);
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "harness failed: %s\n", e.what());
+    return 1;
+  }
+  return 0;
+}

@@ -61,13 +61,13 @@ _SIGS = {
     "cgb_ihc_lambda_scratch_bytes": (_i64, [_i, _i, _i]),
     "cgb_input_gen_dev": (_i, [_p, _i, _p, _p, _i, _i, _i, C.c_float, _d, _d, _d, _d, _p, _p]),
     "cgb_noise_normalization": (_i, [_p, _i, _d, _d, _i, _i, _i, _i, C.c_float, _p, _p]),
-    "cgb_jnd_dev": (_i, [_p, _i64, _i, _i, _i, _i, _p, _p, _p, _p, _d, _d, _p, _p, _p]),
+    "cgb_jnd_dev": (_i, [_p, _i64, _i, _i, _i, _i, _p, _p, _p, _p, _d, _d, _p, _p, _p, _p]),
     "cgb_jnd_final": (_i, [_p, _p, _i, _p, _d, _d, _p, _p]),
     "cgb_ihc_lambda_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64, _p,
                                 _p, _i64, _p, _p]),
     "cgb_bm_launch_shape_count": (_i, []),
     "cgb_bm_run_dev": (_i, [_p, _p, _i, C.POINTER(BMScalars), _p, _i, _p, _i64, _p, _i64,
-                            _p, _p, _p, _p]),
+                            _p, _p, _p, _p, _p]),
 }
 
 

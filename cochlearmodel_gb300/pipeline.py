@@ -152,7 +152,8 @@ class ProfileRun:
             native.ptr(self.d_dA), native.ptr(self.d_ref), native.ptr(self.d_nihc),
             native.ptr(W), float(self.cfg.Fs),
             self.jnd_win.delta_alpha_time_factor * self.cfg.Fs,
-            native.ptr(self.d_FRA), native.ptr(self.d_FAI), self._stream(stream)), "cgb_jnd_dev")
+            native.ptr(self.d_FRA), native.ptr(self.d_FAI), None, self._stream(stream)),
+            "cgb_jnd_dev")
 
     def step(self, stream=None):
         """One pass of the path over the whole sweep (device buffers only)."""

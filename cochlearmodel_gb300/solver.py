@@ -44,7 +44,7 @@ class BMSolver:
     def run_dev(self, sc: native.BMScalars, gamma: torch.Tensor, units: torch.Tensor,
                 n_units: int, inp: torch.Tensor, out: torch.Tensor,
                 failed: torch.Tensor | None = None, stats: torch.Tensor | None = None,
-                stream: torch.cuda.Stream | None = None) -> None:
+                stream: torch.cuda.Stream | None = None, conv: torch.Tensor | None = None) -> None:
         """Enqueues the solver on `stream` (default: torch's current stream).
         All tensors live on this solver's device; `units` holds cgb_unit
         records (see units_to_device) already validated by check_units."""
@@ -52,13 +52,15 @@ class BMSolver:
         native.check(self.lib.cgb_bm_run_dev(
             native.ptr(self.secp), native.ptr(gamma), int(gamma.shape[0]), C.byref(sc),
             native.ptr(units), int(n_units), native.ptr(inp), int(inp.numel()),
-            native.ptr(out), int(out.shape[0]), native.ptr(failed), native.ptr(stats),
+            native.ptr(out), int(out.shape[0]), native.ptr(failed), native.ptr(conv),
+            native.ptr(stats),
             native.ptr(self.work), C.c_void_p(st.cuda_stream)), "cgb_bm_run_dev")
 
     def run(self, sc: native.BMScalars, gamma: np.ndarray, units: np.ndarray,
-            inp: np.ndarray, out_rows: int):
+            inp: np.ndarray, out_rows: int, want_conv: bool = False):
         """Host-buffer call: validates, uploads, solves, downloads.
-        Returns (velocity float32[out_rows,256], failed int32[out_rows], stats)."""
+        Returns (velocity float32[out_rows,256], failed int32[out_rows], stats)
+        and, with want_conv, the per-sample statistics float32[out_rows,3]."""
         gamma = np.ascontiguousarray(np.atleast_2d(gamma), np.float32)
         inp = np.ascontiguousarray(inp, np.float32)
         self.check_units(units, gamma.shape[0], inp.size, out_rows)
@@ -70,7 +72,10 @@ class BMSolver:
         failed = torch.zeros(out_rows, dtype=torch.int32, device=d)
         stats = torch.zeros((len(units), native.STATS_DTYPE.itemsize), dtype=torch.uint8,
                             device=d)
-        self.run_dev(sc, g, u, len(units), x, out, failed, stats)
+        conv = torch.zeros((out_rows, 3), dtype=torch.float32, device=d) if want_conv else None
+        self.run_dev(sc, g, u, len(units), x, out, failed, stats, conv=conv)
         torch.cuda.synchronize(d)
         st = stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
+        if want_conv:
+            return out.cpu().numpy(), failed.cpu().numpy(), st, conv.cpu().numpy()
         return out.cpu().numpy(), failed.cpu().numpy(), st

@@ -150,13 +150,15 @@ int cgb_block_partition(int time_blocks, int64_t samples_p1, int overlap, int de
  *   d_out    float[out_rows][256] velocity rows
  *   d_failed int32[out_rows]   1 where a written sample had a step that hit
  *                              max_outer (may be null)
+ *   d_conv   float[out_rows][3] per written sample: mean dt, steps, mean outer
+ *                              iterations per step (may be null)
  *   d_stats  cgb_unit_stats[n_units] (may be null)
  *   d_work   int32[1] scratch: the work-queue counter (reset in-stream)
  * Units are taken from a device work queue by a persistent grid of warps. */
 int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
                    const cgb_bm_scalars* sc, const cgb_unit* d_units, int n_units,
                    const float* d_in, int64_t in_len, float* d_out, int64_t out_rows,
-                   int32_t* d_failed, cgb_unit_stats* d_stats, int32_t* d_work,
+                   int32_t* d_failed, float* d_conv, cgb_unit_stats* d_stats, int32_t* d_work,
                    void* stream);
 
 /* IHC + lambda over n_frames frames (host frame table, device buffers).
@@ -201,11 +203,12 @@ int cgb_noise_normalization(const float* src, int normalize_type, double normali
  *           (ref_of[i] == i marks a reference)
  *   d_nihc  double[256] nerve fibres per section; W: host float[3]
  *   d_F_RA, d_F_AI  double[3][n_int] rate and all-information Fisher sums
+ *   d_MR    double[3][n_int][256] mean rates over the window (may be null)
  * Time and section sums are FP64. */
 int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, int interval_nodes, int head,
                 int len, const double* d_dA, const int32_t* d_ref_of, const double* d_nihc,
                 const float* W, double Fs, double delta_alpha_len_factor, double* d_F_RA,
-                double* d_F_AI, void* stream);
+                double* d_F_AI, double* d_MR, void* stream);
 
 /* Final JND in dB SPL per interval from the Fisher sums (host arrays):
  * 20 log10((1/sqrt(sum_j F_j)) / spl_ref), bounded at max_db; NaN for

@@ -355,7 +355,7 @@ void exact_solve(const T* Y, const T* rm, T* p) {
 
 template <typename T, typename TO>
 void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scalars& sc,
-             const orc_unit& un, const float* in, TO* out, int32_t* failed,
+             const orc_unit& un, const float* in, TO* out, int32_t* failed, float* conv,
              orc_unit_stats* st) {
   using A = Ar<T>;
   T x0[NS] = {}, v0[NS] = {}, a0[NS] = {}, y0[NS] = {}, u0[NS] = {}, ps0[NS] = {}, dp0[NS] = {};
@@ -377,6 +377,8 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
   const float* inb = in + un.in_base;
   TO* outb = out ? out + un.out_base * (int64_t)NS : nullptr;
   int32_t* fb = failed ? failed + un.out_base : nullptr;
+  float* cb = conv ? conv + un.out_base * 3 : nullptr;
+  float smp_dt = 0.0f, smp_sub = 0.0f, smp_it = 0.0f;
 
   T dt = (T)sc.time_step;
   double tau = 0.0;
@@ -508,6 +510,9 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
     }
     S.substeps += 1;
     S.iterations += out_loop;
+    smp_sub = smp_sub + 1.0f;
+    smp_dt = smp_dt + (float)dt;
+    smp_it = smp_it + (float)out_loop;
     if (tau > Tout) {
       tau -= Tout;
       sx0 = sx1;
@@ -516,11 +521,17 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
         if (outb)
           for (int s = 0; s < NS; ++s) outb[n * NS + s] = (TO)v[s];
         if (fb) fb[n] = fail_flag;
+        if (cb) {
+          cb[n * 3 + 0] = smp_dt / smp_sub;
+          cb[n * 3 + 1] = smp_sub;
+          cb[n * 3 + 2] = smp_it / smp_sub;
+        }
         S.written_samples += 1;
         S.failed_samples += fail_flag;
       }
       fail_flag = 0;
       sub_in_sample = 0;
+      smp_dt = smp_sub = smp_it = 0.0f;
       ++n;
     }
     for (int s = 0; s < NS; ++s) {
@@ -543,7 +554,7 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
 template <typename T, typename TO>
 void bm_run(const float* secp, const float* gamma, const orc_bm_scalars* sc,
             const orc_unit* units, int n_units, const float* in, TO* out, int32_t* failed,
-            orc_unit_stats* stats, int n_threads) {
+            float* conv, orc_unit_stats* stats, int n_threads) {
   // secp: float[8][256] = invM, rm, R, S, Q, S_ohc, S_tm, R_tm
   BMModel<T> md;
   for (int s = 0; s < NS; ++s) {
@@ -567,7 +578,7 @@ void bm_run(const float* secp, const float* gamma, const orc_bm_scalars* sc,
         gam[s] = (T)gamma[(int64_t)un.profile * NS + s];
         gs[s] = gam[s] * md.S_ohc[s];
       }
-      bm_unit<T, TO>(md, gam, gs, *sc, un, in, out, failed, stats ? stats + i : nullptr);
+      bm_unit<T, TO>(md, gam, gs, *sc, un, in, out, failed, conv, stats ? stats + i : nullptr);
     }
   };
   n_threads = std::max(1, n_threads);
@@ -586,14 +597,14 @@ extern "C" {
 
 void orc_bm_run_f32(const float* secp, const float* gamma, const orc_bm_scalars* sc,
                     const orc_unit* units, int n_units, const float* in, float* out,
-                    int32_t* failed, orc_unit_stats* stats, int n_threads) {
-  bm_run<float, float>(secp, gamma, sc, units, n_units, in, out, failed, stats, n_threads);
+                    int32_t* failed, float* conv, orc_unit_stats* stats, int n_threads) {
+  bm_run<float, float>(secp, gamma, sc, units, n_units, in, out, failed, conv, stats, n_threads);
 }
 
 void orc_bm_run_f64(const float* secp, const float* gamma, const orc_bm_scalars* sc,
                     const orc_unit* units, int n_units, const float* in, double* out,
-                    int32_t* failed, orc_unit_stats* stats, int n_threads) {
-  bm_run<double, double>(secp, gamma, sc, units, n_units, in, out, failed, stats, n_threads);
+                    int32_t* failed, float* conv, orc_unit_stats* stats, int n_threads) {
+  bm_run<double, double>(secp, gamma, sc, units, n_units, in, out, failed, conv, stats, n_threads);
 }
 
 // ---------------------------------------------------------------------------

@@ -59,7 +59,7 @@ def load():
         lib.orc_block_partition.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, _p, _p, _p]
         for nm in ("orc_bm_run_f32", "orc_bm_run_f64"):
             getattr(lib, nm).argtypes = [_p, _p, C.POINTER(OrcScalars), _p, C.c_int, _p, _p,
-                                         _p, _p, C.c_int]
+                                         _p, _p, _p, C.c_int]
         lib.orc_ihc_lambda.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        _p, C.c_int, _p, C.c_int, C.c_double, C.c_double,
                                        C.c_double, _p, _p, _p, C.c_double, _p, _p, C.c_int64,
@@ -117,8 +117,10 @@ def block_partition(time_blocks, samples_p1, overlap, decouple):
     return st, of, en
 
 
-def bm_run(secp, gamma, sc, units, inp, out_rows, fp64=False, threads=None, jacobi_mode=None):
-    """Runs the BM step over `units`; returns (velocity[out_rows,256], failed, stats)."""
+def bm_run(secp, gamma, sc, units, inp, out_rows, fp64=False, threads=None, jacobi_mode=None,
+           conv=None):
+    """Runs the BM step over `units`; returns (velocity[out_rows,256], failed, stats).
+    conv: optional float32[out_rows, 3] filled with the per-sample statistics."""
     osc = scalars_from(sc)
     if jacobi_mode is not None:
         osc.jacobi_mode = jacobi_mode
@@ -131,7 +133,7 @@ def bm_run(secp, gamma, sc, units, inp, out_rows, fp64=False, threads=None, jaco
     stats = np.zeros(len(units), STATS_DTYPE)
     fn = load().orc_bm_run_f64 if fp64 else load().orc_bm_run_f32
     fn(_ptr(secp), _ptr(gamma), C.byref(osc), _ptr(units), len(units), _ptr(inp), _ptr(out),
-       _ptr(failed), _ptr(stats), threads or (os.cpu_count() or 1))
+       _ptr(failed), _ptr(conv), _ptr(stats), threads or (os.cpu_count() or 1))
     return out, failed, stats
 
 

@@ -82,3 +82,13 @@ def test_substep_guard_stops_unit(mv, bm_solver):
     sc.max_substeps_per_sample = 5
     v, st = _compare(mv, bm_solver, (cfg, sc, gamma, units, x, rows))
     assert st["status"][0] == 1 and st["written_samples"][0] == 0
+
+
+def test_per_sample_convergence_stats(mv, bm_solver):
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=1.0)
+    conv_o = np.zeros((rows, 3), np.float32)
+    orc.bm_run(mv.section_params(), gamma, sc, units, x, rows, conv=conv_o)
+    _, _, _, conv_g = bm_solver.run(sc, gamma, units, x, rows, want_conv=True)
+    assert np.array_equal(conv_g.view(np.uint32), conv_o.view(np.uint32))
+    e = int(units["end"][0])
+    assert (conv_g[:e, 1] >= 10).all() and (conv_g[:e, 2] >= 2).all()
