@@ -392,3 +392,161 @@ extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ih
   note_launch();
   return CGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// No-allocation variant of cgb_ihc_lambda_dev.
+//
+// The per-call tables (frames, tile prefix, filter taps) go to a file-scope
+// __device__ array instead of caller scratch, for callers that cannot
+// allocate device memory: a host that hands the library only the buffers it
+// already owns, or a real-time audio thread that must not enter the device
+// allocator.  The array is 192 KiB, holds at most kNoAllocMaxFrames frames and
+// kNoAllocMaxTaps taps, and stays resident on every GPU that loads this
+// library until the process exits.  All calls share it, so calls whose GPU
+// work overlaps (different streams, or a second call enqueued before the
+// first one ran) race on its contents; serialise them on one stream.  Each
+// call rewrites every table byte it reads, so nothing needs clearing.
+// ---------------------------------------------------------------------------
+namespace cgb {
+namespace {
+
+constexpr int kNoAllocMaxFrames = 4096;
+constexpr int kNoAllocMaxTaps = 2048;  // n_ac + n_dc
+constexpr size_t kNoAllocFrameBytes = (size_t)kNoAllocMaxFrames * sizeof(cgb_ihc_frame);
+constexpr size_t kNoAllocPrefixOff = (kNoAllocFrameBytes + 255) / 256 * 256;
+constexpr size_t kNoAllocTapsOff =
+    kNoAllocPrefixOff + ((size_t)(kNoAllocMaxFrames + 1) * 4 + 255) / 256 * 256;
+constexpr size_t kNoAllocBytes = 192 * 1024;
+static_assert(kNoAllocTapsOff + (size_t)kNoAllocMaxTaps * 4 <= kNoAllocBytes,
+              "no-allocation scratch too small");
+
+__device__ __align__(256) unsigned char g_ihc_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the array on the current device, looked up once per
+// device (the host-side symbol is only a stand-in, not a device address).
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  CGB_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: device index beyond 63");
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    CGB_TRY_CUDA(cudaGetSymbolAddress(&p, g_ihc_noalloc_scratch), "cudaGetSymbolAddress");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CGB_OK;
+}
+
+}  // namespace
+}  // namespace cgb
+
+extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
+                                          const cgb_ihc_frame* frames, int n_frames,
+                                          const float* ac_taps, int n_ac, const float* dc_taps,
+                                          int n_dc, const cgb_ihc_params* prm,
+                                          const float* d_dmg, int n_dmg_profiles,
+                                          const float* d_aihc, float* d_lam,
+                                          int64_t lam_plane_rows, float* d_ihc,
+                                          int32_t* d_status, void* stream) {
+  using namespace cgb;
+  if (n_frames == 0) return CGB_OK;
+  if (!d_v || !frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_dmg || !d_aihc ||
+      !d_lam || !d_status)
+    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_noalloc_dev: null pointer argument");
+  if (n_frames > kNoAllocMaxFrames)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: more than 4096 frames (the fixed "
+                               "scratch holds at most 4096)");
+  if (n_ac < 1 || n_dc < 1 || n_ac > 1024 || n_dc > 1024 || n_ac + n_dc > kNoAllocMaxTaps)
+    return fail(CGB_ERR_RANGE,
+                "cgb_ihc_lambda_noalloc_dev: filter lengths must be in [1, 1024]");
+  if (reinterpret_cast<uintptr_t>(d_v) & 15)
+    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_noalloc_dev: d_v must be 16-byte aligned");
+  if (v_rows > INT32_MAX)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: more than 2^31-1 velocity rows");
+  int TR = 384, xrows = 0;
+  for (; TR >= 8; TR -= 8) {
+    xrows = (TR + n_ac + n_dc - 1 + kBoxRows - 1) / kBoxRows * kBoxRows;
+    if (smem_bytes(TR, xrows, n_ac, n_dc) <= 227 * 1024) break;
+  }
+  if (TR < 8)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: filters too long for one tile");
+  int32_t prefix[kNoAllocMaxFrames + 1];
+  prefix[0] = 0;
+  for (int i = 0; i < n_frames; ++i) {
+    const cgb_ihc_frame& fr = frames[i];
+    const bool ok = fr.v_row0 >= 0 && fr.lam_rows >= 0 && fr.lam_rows <= fr.rows &&
+                    fr.v_row0 + fr.rows <= v_rows && fr.lam_row0 >= 0 &&
+                    fr.lam_row0 + fr.lam_rows <= lam_plane_rows && fr.seg > 0 && fr.frdp > 0 &&
+                    fr.total > 0 && fr.ihc_profile >= 0 && fr.ihc_profile < n_dmg_profiles;
+    if (!ok)
+      return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: frame " + std::to_string(i) +
+                                     " out of range");
+    prefix[i + 1] = prefix[i] + (fr.lam_rows + TR - 1) / TR;
+  }
+  const int n_tiles = prefix[n_frames];
+  if (n_tiles == 0) return CGB_OK;
+  void* scratch = nullptr;
+  if (int st = noalloc_scratch(&scratch)) return st;
+  unsigned char* sc = static_cast<unsigned char*>(scratch);
+  float taps[kNoAllocMaxTaps];
+  for (int i = 0; i < n_ac; ++i) taps[i] = ac_taps[i] * prm->scale;
+  for (int i = 0; i < n_dc; ++i) taps[n_ac + i] = dc_taps[i];
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  CGB_TRY_CUDA(cudaMemcpyAsync(sc, frames, (size_t)n_frames * sizeof(cgb_ihc_frame),
+                               cudaMemcpyHostToDevice, st),
+               "upload frames");
+  CGB_TRY_CUDA(cudaMemcpyAsync(sc + kNoAllocPrefixOff, prefix, (size_t)(n_frames + 1) * 4,
+                               cudaMemcpyHostToDevice, st),
+               "upload tile prefix");
+  CGB_TRY_CUDA(cudaMemcpyAsync(sc + kNoAllocTapsOff, taps, (size_t)(n_ac + n_dc) * 4,
+                               cudaMemcpyHostToDevice, st),
+               "upload taps");
+  auto encode = get_encode();
+  if (!encode) return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  CUtensorMap map;
+  cuuint64_t dims[2] = {256, (cuuint64_t)v_rows};
+  cuuint64_t strides[1] = {256 * 4};
+  cuuint32_t box[2] = {(cuuint32_t)kSecTile, (cuuint32_t)kBoxRows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(d_v), dims,
+                       strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (cr != CUDA_SUCCESS)
+    return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
+  IHCArgs A;
+  A.frames = reinterpret_cast<const cgb_ihc_frame*>(sc);
+  A.tile_prefix = reinterpret_cast<const int32_t*>(sc + kNoAllocPrefixOff);
+  A.n_frames = n_frames;
+  A.taps = reinterpret_cast<const float*>(sc + kNoAllocTapsOff);
+  A.n_ac = n_ac;
+  A.n_dc = n_dc;
+  A.scale = prm->scale;
+  A.eta_ac = prm->eta_ac;
+  A.eta_dc = prm->eta_dc;
+  A.sat = prm->lambda_sat;
+  A.spont0 = prm->spont[0];
+  A.spont1 = prm->spont[1];
+  A.spont2 = prm->spont[2];
+  A.dmg = d_dmg;
+  A.aihc = d_aihc;
+  A.lam = d_lam;
+  A.lam_plane_rows = lam_plane_rows;
+  A.ihc = d_ihc;
+  A.TR = TR;
+  A.xrows = xrows;
+  A.status = d_status;
+  const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
+  CGB_TRY_CUDA(cudaFuncSetAttribute(ihc_lambda_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+               "cudaFuncSetAttribute(ihc smem)");
+  dim3 grid((unsigned)n_tiles, 256 / kSecTile);
+  ihc_lambda_kernel<<<grid, kIhcWarps * 32, smem, st>>>(map, A);
+  CGB_TRY_CUDA(cudaGetLastError(), "ihc_lambda_kernel launch");
+  note_launch();
+  return CGB_OK;
+}

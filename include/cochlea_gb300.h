@@ -179,6 +179,25 @@ int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* fr
                        int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
                        int64_t scratch_bytes, int32_t* d_status, void* stream);
 
+/* IHC + lambda without any device allocation -- no counterpart in the
+ * reference.  For callers that cannot allocate device memory (a host that
+ * gives the library only buffers it already owns, a real-time audio thread
+ * that must not enter the device allocator): the same computation as
+ * cgb_ihc_lambda_dev, but the per-call tables live in a fixed 192 KiB
+ * __device__ array inside the library instead of caller scratch.  Limits:
+ * at most 4096 frames and n_ac + n_dc <= 2048 taps (CGB_ERR_RANGE beyond).
+ * The array stays resident on every GPU that loads the library until exit
+ * and is shared by all calls: calls whose GPU work overlaps race on it, so
+ * serialise them on one stream.  The first call on a device looks the array's
+ * device address up (cudaGetSymbolAddress); make that first call before any
+ * stream capture. */
+int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                               int n_frames, const float* ac_taps, int n_ac,
+                               const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+                               const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
+                               float* d_lam, int64_t lam_plane_rows, float* d_ihc,
+                               int32_t* d_status, void* stream);
+
 /* Input generation: d_out[p*interval_len + n] for n < interval_len,
  *   signal_mode 0: dA cos(2 pi f (n-head)/Fs)/sig_norm + Wn (wn[n]-wn_dc)/wn_norm
  *   signal_mode 1: dA (signal[n]-sig_dc)/sig_norm    + Wn (wn[n]-wn_dc)/wn_norm
