@@ -286,23 +286,29 @@ extern "C" int64_t cgb_ihc_lambda_scratch_bytes(int n_frames, int n_ac, int n_dc
          ((int64_t)(n_ac + n_dc) * 4 + 255) / 256 * 256;
 }
 
-extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
-                                  int n_frames, const float* ac_taps, int n_ac,
-                                  const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
-                                  const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
-                                  float* d_lam, int64_t lam_plane_rows, float* d_ihc,
-                                  void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
-                                  void* stream) {
-  using namespace cgb;
+namespace cgb {
+namespace {
+constexpr int kUpload = 1, kLaunch = 2;
+
+// Validates the frame table, then uploads the per-call tables (frames, tile
+// prefix, taps) to the scratch buffer (kUpload) and/or launches the kernel
+// on tables already there (kLaunch).  Upload and launch are separable so a
+// CUDA graph can capture the launch alone.
+int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames, int n_frames,
+                    const float* ac_taps, int n_ac, const float* dc_taps, int n_dc,
+                    const cgb_ihc_params* prm, const float* d_dmg, int n_dmg_profiles,
+                    const float* d_aihc, float* d_lam, int64_t lam_plane_rows, float* d_ihc,
+                    void* d_scratch, int64_t scratch_bytes, int32_t* d_status, void* stream,
+                    int mode) {
   if (n_frames == 0) return CGB_OK;
-  if (!d_v || !frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_dmg || !d_aihc ||
-      !d_lam || !d_scratch || !d_status)
+  if (!frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_scratch ||
+      ((mode & kLaunch) && (!d_v || !d_dmg || !d_aihc || !d_lam || !d_status)))
     return fail(CGB_ERR_ARG, "cgb_ihc_lambda_dev: null pointer argument");
   if (n_ac < 1 || n_dc < 1 || n_ac > 1024 || n_dc > 1024)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filter lengths must be in [1, 1024]");
   if (scratch_bytes < cgb_ihc_lambda_scratch_bytes(n_frames, n_ac, n_dc))
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: scratch buffer too small");
-  if (reinterpret_cast<uintptr_t>(d_v) & 15)
+  if ((mode & kLaunch) && (reinterpret_cast<uintptr_t>(d_v) & 15))
     return fail(CGB_ERR_ARG, "cgb_ihc_lambda_dev: d_v must be 16-byte aligned");
   if (v_rows > INT32_MAX)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: more than 2^31-1 velocity rows");
@@ -333,18 +339,21 @@ extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ih
   unsigned char* sc = static_cast<unsigned char*>(d_scratch);
   const size_t fbytes = ((size_t)n_frames * sizeof(cgb_ihc_frame) + 255) / 256 * 256;
   const size_t pbytes = ((size_t)(n_frames + 1) * 4 + 255) / 256 * 256;
-  std::vector<float> taps(n_ac + n_dc);
-  for (int i = 0; i < n_ac; ++i) taps[i] = ac_taps[i] * prm->scale;
-  for (int i = 0; i < n_dc; ++i) taps[n_ac + i] = dc_taps[i];
-  CGB_TRY_CUDA(cudaMemcpyAsync(sc, frames, (size_t)n_frames * sizeof(cgb_ihc_frame),
-                               cudaMemcpyHostToDevice, st),
-               "upload frames");
-  CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes, prefix.data(), (size_t)(n_frames + 1) * 4,
-                               cudaMemcpyHostToDevice, st),
-               "upload tile prefix");
-  CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes + pbytes, taps.data(), taps.size() * 4,
-                               cudaMemcpyHostToDevice, st),
-               "upload taps");
+  if (mode & kUpload) {
+    std::vector<float> taps(n_ac + n_dc);
+    for (int i = 0; i < n_ac; ++i) taps[i] = ac_taps[i] * prm->scale;
+    for (int i = 0; i < n_dc; ++i) taps[n_ac + i] = dc_taps[i];
+    CGB_TRY_CUDA(cudaMemcpyAsync(sc, frames, (size_t)n_frames * sizeof(cgb_ihc_frame),
+                                 cudaMemcpyHostToDevice, st),
+                 "upload frames");
+    CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes, prefix.data(), (size_t)(n_frames + 1) * 4,
+                                 cudaMemcpyHostToDevice, st),
+                 "upload tile prefix");
+    CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes + pbytes, taps.data(), taps.size() * 4,
+                                 cudaMemcpyHostToDevice, st),
+                 "upload taps");
+  }
+  if (!(mode & kLaunch)) return CGB_OK;
 
   auto encode = get_encode();
   if (!encode) return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -391,6 +400,45 @@ extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ih
   CGB_TRY_CUDA(cudaGetLastError(), "ihc_lambda_kernel launch");
   note_launch();
   return CGB_OK;
+}
+
+}  // namespace
+}  // namespace cgb
+
+extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                                  int n_frames, const float* ac_taps, int n_ac,
+                                  const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+                                  const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
+                                  float* d_lam, int64_t lam_plane_rows, float* d_ihc,
+                                  void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
+                                  void* stream) {
+  return cgb::ihc_lambda_impl(d_v, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc, prm,
+                              d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc,
+                              d_scratch, scratch_bytes, d_status, stream,
+                              cgb::kUpload | cgb::kLaunch);
+}
+
+extern "C" int cgb_ihc_lambda_upload_dev(const cgb_ihc_frame* frames, int n_frames,
+                                         const float* ac_taps, int n_ac, const float* dc_taps,
+                                         int n_dc, const cgb_ihc_params* prm, int64_t v_rows,
+                                         int64_t lam_plane_rows, int n_dmg_profiles,
+                                         void* d_scratch, int64_t scratch_bytes, void* stream) {
+  return cgb::ihc_lambda_impl(nullptr, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc,
+                              prm, nullptr, n_dmg_profiles, nullptr, nullptr, lam_plane_rows,
+                              nullptr, d_scratch, scratch_bytes, nullptr, stream, cgb::kUpload);
+}
+
+extern "C" int cgb_ihc_lambda_launch_dev(const float* d_v, int64_t v_rows,
+                                         const cgb_ihc_frame* frames, int n_frames,
+                                         const float* ac_taps, int n_ac, const float* dc_taps,
+                                         int n_dc, const cgb_ihc_params* prm,
+                                         const float* d_dmg, int n_dmg_profiles,
+                                         const float* d_aihc, float* d_lam,
+                                         int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
+                                         int64_t scratch_bytes, int32_t* d_status, void* stream) {
+  return cgb::ihc_lambda_impl(d_v, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc, prm,
+                              d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc,
+                              d_scratch, scratch_bytes, d_status, stream, cgb::kLaunch);
 }
 
 // ---------------------------------------------------------------------------

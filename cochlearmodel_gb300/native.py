@@ -59,6 +59,10 @@ _SIGS = {
     "cgb_check_units": (_i, [_p, _i, _i, _i64, _i64]),
     "cgb_bm_set_launch_shape": (_i, [_i]),
     "cgb_ihc_lambda_scratch_bytes": (_i64, [_i, _i, _i]),
+    "cgb_ihc_lambda_upload_dev": (_i, [_p, _i, _p, _i, _p, _i, _p, _i64, _i64, _i, _p, _i64,
+                                       _p]),
+    "cgb_ihc_lambda_launch_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64,
+                                       _p, _p, _i64, _p, _p]),
     "cgb_ihc_lambda_noalloc_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p,
                                         _i64, _p, _p, _p]),
     "cgb_input_gen_dev": (_i, [_p, _i, _p, _p, _i, _i, _i, C.c_float, _d, _d, _d, _d, _p, _p]),

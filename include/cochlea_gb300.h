@@ -179,6 +179,22 @@ int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* fr
                        int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
                        int64_t scratch_bytes, int32_t* d_status, void* stream);
 
+/* The two halves of cgb_ihc_lambda_dev, for CUDA-graph capture: the upload
+ * call copies the frame table, tile prefix and taps into d_scratch (host to
+ * device, not capturable); the launch call, given the same frames and taps,
+ * only launches the kernel on the tables already in d_scratch. */
+int cgb_ihc_lambda_upload_dev(const cgb_ihc_frame* frames, int n_frames, const float* ac_taps,
+                              int n_ac, const float* dc_taps, int n_dc,
+                              const cgb_ihc_params* prm, int64_t v_rows, int64_t lam_plane_rows,
+                              int n_dmg_profiles, void* d_scratch, int64_t scratch_bytes,
+                              void* stream);
+int cgb_ihc_lambda_launch_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                              int n_frames, const float* ac_taps, int n_ac, const float* dc_taps,
+                              int n_dc, const cgb_ihc_params* prm, const float* d_dmg,
+                              int n_dmg_profiles, const float* d_aihc, float* d_lam,
+                              int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
+                              int64_t scratch_bytes, int32_t* d_status, void* stream);
+
 /* IHC + lambda without any device allocation -- no counterpart in the
  * reference.  For callers that cannot allocate device memory (a host that
  * gives the library only buffers it already owns, a real-time audio thread

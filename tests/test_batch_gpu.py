@@ -1,0 +1,75 @@
+"""Batched sweeps: groups of different lengths solved in one BM launch and one
+IHC launch (and replayed from a CUDA graph) give exactly what each group gives
+when run on its own."""
+import numpy as np
+import pytest
+
+from cochlearmodel_gb300 import batch
+from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun, ProfileSweep
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sweep(mv):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    spec = batch.jnd_sweep_spec(n_seeds=2, seed=3, min_ms=3.0, max_ms=6.0,
+                                noises=(1111.0, 30.0), powers=(40.0, 80.0))
+    b = batch.BatchSweep("cuda:0", spec, mv=mv, overlap_time=0.001, block_target=150,
+                         jnd=JNDWindow(head=0.0005, tail=0.0002))
+    b.step()
+    torch.cuda.synchronize()
+    return b, spec
+
+
+def test_groups_match_single_runs(sweep, mv):
+    import torch
+    b, spec = sweep
+    res = b.jnd_db()
+    v_all = b.d_v.cpu().numpy()
+    lam_all = b.d_lam.cpu().numpy()
+    for gi, (g, s) in enumerate(zip(b.groups, spec)):
+        cfg = batch.RunConfig(Fs=g.cfg.Fs, Time_Block_Length=g.cfg.Time_Block_Length,
+                              Decouple_Filter=g.cfg.Decouple_Filter,
+                              Overlap_Time=g.cfg.Overlap_Time, OHC_Vector=g.cfg.OHC_Vector,
+                              IHC_Vector=g.cfg.IHC_Vector)
+        run = ProfileRun("cuda:0", cfg, s["sweep"], noise=g.noise, mv=mv, jnd=b.jnd_win)
+        run.step()
+        torch.cuda.synchronize()
+        rows = run.rows - 4
+        v1 = run.d_v.cpu().numpy()[:rows]
+        assert np.array_equal(v1.view(np.uint32), v_all[g.v_row0:g.v_row0 + rows].view(np.uint32))
+        lam1 = run.d_lam.cpu().numpy()
+        n = lam1.shape[1]
+        assert np.array_equal(lam1.view(np.uint32),
+                              lam_all[:, g.lam_row0:g.lam_row0 + n].view(np.uint32))
+        r1, a1, _, _ = run.jnd_db()
+        rb, ab, _, _ = res[gi]
+        tested = ~np.isnan(r1)
+        assert np.array_equal(r1[tested], rb[tested]) and np.array_equal(a1[tested], ab[tested])
+
+
+def test_graph_replay_matches_eager(sweep):
+    import torch
+    b, _ = sweep
+    v0 = b.d_v.clone()
+    lam0 = b.d_lam.clone()
+    F0 = [pg["d_FRA"].clone() for pg in b.per_group]
+    b.d_v.zero_()
+    b.d_lam.zero_()
+    b.capture()
+    b.d_v.zero_()
+    b.d_lam.zero_()
+    b.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(b.d_v, v0) and torch.equal(b.d_lam, lam0)
+    for f, pg in zip(F0, b.per_group):
+        assert torch.equal(f, pg["d_FRA"])
+
+
+def test_units_longest_first(sweep):
+    b, _ = sweep
+    span = b.units["end"] - b.units["start"]
+    assert (np.diff(span) <= 0).all()

@@ -110,3 +110,19 @@ def test_profile_sweep_grid():
     assert ref_of[0] == 10 and ref_of[11] == 21 and ref_of[65] == 65
     assert p["Wn"][0] == 0.0 and p["dA"][10] == 0.0
     assert p["dA"][5] == pytest.approx(10 * 10 ** (60 / 20) * 2e-5)
+
+
+def test_jnd_sweep_configuration():
+    from cochlearmodel_gb300 import batch
+    spec = batch.jnd_sweep_spec(n_seeds=4)
+    assert len(spec) == 24
+    n = sum(len(s["sweep"].build()[0]) for s in spec)
+    assert n == 264
+    lens = [s["length"] for s in spec]
+    assert min(lens) >= 2000 and max(lens) <= 20000
+    for s in spec:
+        N, D = batch.block_nodes_for(s["length"], 1000, 100000)
+        assert abs(N * D - s["length"]) <= 3 * D and N <= 1000 + 3
+    o, i = batch.hearing_loss_ohc(), batch.hearing_loss_ihc()
+    assert o[0] == 0.5 and o[127] == 0.5 and o[255] == np.float32(0.05)
+    assert i[0] == 8 and i[255] == 5 and (np.diff(i[127:]) < 0).all()
