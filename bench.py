@@ -1,19 +1,28 @@
 """Benchmark: simulated audio-seconds per wall-second of the cochlear solver
 path on one GB300 (one process per GPU under torchrun; weak scaling).
 
-Workload (default "tone_sweep", config 2): 64 pure tones log-spaced
-125 Hz-8 kHz x {20,40,60,80,100} dB SPL = 320 signals of 80 ms at 100 kHz,
-each split into Decouple_Filter=8 blocks of 10 ms with the 5 ms overlap
-warm-up -- 2,560 BM units per step, 25.6 s of audio.  A step is one pass of
-the path over the whole batch with its inputs resident in HBM: input
-generation, BM/OHC solver (FP32), IHC + lambda for the three fibre groups.
+Workloads (--workload):
+  jnd_sweep (default, configuration 3): a 1 kHz tone at 10..100 dB SPL x noise
+      levels {none, 0, 10, 20, 30, 40} dB SPL plus one noise-only reference per
+      noise level, 4 noise seeds -> 264 signals; interval lengths drawn per
+      (seed, noise) group uniformly in 20-200 ms; hearing-loss OHC/IHC
+      profiles; ~10 ms blocks with the 5 ms overlap warm-up.  A step is the
+      whole path -- input generation, BM/OHC solver, IHC + lambda, JND Fisher
+      sums -- for all 264 signals, replayed from one CUDA graph.
+  tone_sweep (configuration 2): 64 log-spaced tones 125 Hz-8 kHz x {20..100}
+      dB SPL = 320 signals of 80 ms, Decouple_Filter 8 blocks of 10 ms; input,
+      BM, IHC + lambda.
+
+Every step recomputes everything from the profile table in HBM.  Reported
+beside the batched value: the same kernels run one signal at a time ("plain
+single-signal"), and the CPU restatement on the host cores.
 
 Arms:
-  default            the GB300 kernels (value: device time; e2e: host buffers
-                     in, results back to host, through the C ABI)
+  default            the GB300 kernels (value: device time; e2e: host tables in,
+                     velocity + lambda back to host, through the C ABI)
   --impl reference   the reference algorithm on the host cores (the CPU
-                     restatement of kernel 17; the reference ships no
-                     runnable CPU path of its own), bounded sample per step
+                     restatement of the path; the reference ships no runnable
+                     CPU path of its own), bounded sample per step
 """
 from __future__ import annotations
 
@@ -36,18 +45,35 @@ UNIT = "audio-s/s"
 
 
 # ----------------------------------------------------------------------------
-# workload
+# workloads
 # ----------------------------------------------------------------------------
-def tone_sweep_config(n_freq=64, levels=(20, 40, 60, 80, 100)):
-    """Config 2: n_freq log-spaced tones 125 Hz-8 kHz x levels, 10 ms blocks x
-    Decouple_Filter 8, 5 ms overlap, healthy profiles, outputs v + lambda.
-    n_freq=64 is the full workload; smaller values give profiling cases."""
-    from cochlearmodel_gb300 import model
-    from cochlearmodel_gb300.pipeline import ProfileSweep
-    cfg = model.RunConfig(Time_Block_Length=0.01, Decouple_Filter=8, Overlap_Time=0.005)
-    freqs = list(125.0 * 64.0 ** (np.arange(n_freq) / max(1, n_freq - 1)))
-    sweep = ProfileSweep(frequencies=freqs, powers=list(levels), calculate_jnd=False)
-    return cfg, sweep
+def make_workload(name, device, n_freq=64, n_seeds=4):
+    from cochlearmodel_gb300 import batch, model
+    from cochlearmodel_gb300.pipeline import ProfileRun, ProfileSweep
+    if name == "tone_sweep":
+        cfg = model.RunConfig(Time_Block_Length=0.01, Decouple_Filter=8, Overlap_Time=0.005)
+        freqs = list(125.0 * 64.0 ** (np.arange(n_freq) / max(1, n_freq - 1)))
+        sweep = ProfileSweep(frequencies=freqs, powers=[20.0, 40.0, 60.0, 80.0, 100.0])
+        run = ProfileRun(device, cfg, sweep)
+        run.kind = "tone_sweep"
+        return run
+    if name == "jnd_sweep":
+        run = batch.BatchSweep(device, batch.jnd_sweep_spec(n_seeds=n_seeds))
+        run.kind = "jnd_sweep"
+        return run
+    raise ValueError(name)
+
+
+def stages(run):
+    s = [("input_gen", run.generate_input), ("bm_solver", run.solve_bm),
+         ("ihc_lambda", run.ihc_lambda)]
+    if run.kind == "jnd_sweep":
+        s.append(("jnd", run.jnd_sums))
+    return s
+
+
+def n_signals(run):
+    return run.n_signals if run.kind == "jnd_sweep" else run.n_int
 
 
 # ----------------------------------------------------------------------------
@@ -129,65 +155,129 @@ def bm_flops(stats) -> float:
                     FLOP_PER_SECTION_SWEEP * sw)
 
 
+# DRAM bytes per BM launch, from ncu (dram__bytes_read.sum + dram__bytes_write.sum)
+# on the 40-signal tone sweep (278.9 MB for 320 units), scaled by the units a
+# launch processes: the traffic is the velocity rows written, in proportion.
+BM_TRAFFIC_PER_UNIT = 278.9e6 / 320
+
+
 # ----------------------------------------------------------------------------
-# CPU baseline (oracle restatement on the host cores)
+# CPU restatement on the host cores (bounded sample)
 # ----------------------------------------------------------------------------
 def cpu_sample(run, target_s=15.0, threads=None):
-    """The path (BM + IHC/lambda in the reference's arithmetic) on the first K
-    signals of the sweep, all host threads; returns audio-s per wall-second."""
+    """The path (BM in FP32 + IHC/lambda in the reference's mixed precision)
+    on the first K signals (tone sweep) or groups (JND sweep), all host
+    threads; returns (audio-s per wall-second, cores, description)."""
     from cochlearmodel_gb300 import ihc as ihcmod
     from oracle import oracle as orc
     cores = threads or os.cpu_count() or 1
-    D = run.cfg.Decouple_Filter
-    ov = run.cfg.calc_overlap_nodes()
     x = run.d_in.cpu().numpy()
     secp = run.mv.section_params()
-    gamma = run.cfg.gamma()[None]
     st = run.ihc
 
-    def sample(k):
-        units = run.units[:k * D]
-        t0 = time.perf_counter()
-        v, _, _ = orc.bm_run(secp, gamma, run.sc, units, x, run.rows, threads=cores)
-        rows = k * run.L + ov
-        orc.ihc_lambda(v[:rows], run.L, k * run.L, ihcmod.round64(rows), k * run.L,
-                       st.ac.astype(np.float64), st.dc.astype(np.float64), 1.0, 1.0, 100.0,
+    def ihc_frame(v, fr):
+        r0 = int(fr["v_row0"])
+        orc.ihc_lambda(v[r0:r0 + int(fr["rows"])], int(fr["seg"]), int(fr["frdp"]),
+                       int(fr["total"]), int(fr["lam_rows"]), st.ac.astype(np.float64),
+                       st.dc.astype(np.float64), 1.0, 1.0, 100.0,
                        st.dmg_host[0].astype(np.float64), st.nerve.aihc(),
                        np.asarray(st.nerve.spontRate, np.float32), 500.0, mode=0)
-        return time.perf_counter() - t0
 
-    k = max(1, min(run.n_int, cores // D))
-    dt = sample(k)
-    k2 = max(1, min(run.n_int, int(k * target_s / max(dt, 1e-3))))
+    if run.kind == "tone_sweep":
+        D = run.cfg.Decouple_Filter
+        ov = run.cfg.calc_overlap_nodes()
+        gamma = run.cfg.gamma()[None]
+
+        def sample(k):
+            units = run.units[:k * D]
+            t0 = time.perf_counter()
+            v, _, _ = orc.bm_run(secp, gamma, run.sc, units, x, run.rows, threads=cores)
+            rows = k * run.L + ov
+            fr = np.zeros(1, ihcmod.FRAME_DTYPE)[0]
+            fr["v_row0"], fr["rows"], fr["lam_rows"] = 0, rows, k * run.L
+            fr["seg"], fr["frdp"], fr["total"] = run.L, k * run.L, ihcmod.round64(rows)
+            ihc_frame(v, fr)
+            return time.perf_counter() - t0, k * run.L / run.cfg.Fs
+
+        k, limit, what = max(1, min(run.n_int, cores // D)), run.n_int, "signals of the tone sweep"
+    else:
+        gamma = run.d_gamma.cpu().numpy()
+
+        def sample(k):
+            groups = run.groups[:k]
+            units = np.concatenate([run.units[run.units["out_base"] == g.v_row0] for g in groups])
+            t0 = time.perf_counter()
+            v, _, _ = orc.bm_run(secp, gamma, run.sc, units, x, run.v_rows, threads=cores)
+            for gi in range(k):
+                ihc_frame(v, run.frames[gi])
+            return time.perf_counter() - t0, sum(len(g.prof) * g.L for g in groups) / run.Fs
+
+        k, limit, what = 1, len(run.groups), "groups of the JND sweep"
+    dt, audio = sample(k)
+    k2 = max(1, min(limit, int(k * target_s / max(dt, 1e-3))))
     if k2 > k:
-        k, dt = k2, sample(k2)
-    audio = k * run.L / run.cfg.Fs
-    return audio / dt, cores, (f"{k} of {run.n_int} signals of the tone sweep ({audio:.3f} "
-                               f"audio-s): BM (FP32 oracle) + IHC/lambda (reference mixed "
-                               f"precision), {cores} threads, {dt:.1f} s")
+        k = k2
+        dt, audio = sample(k)
+    return audio / dt, cores, (f"{k} {what} ({audio:.3f} audio-s): BM (FP32 restatement) + "
+                               f"IHC/lambda (reference mixed precision), {cores} threads, "
+                               f"{dt:.1f} s")
+
+
+# ----------------------------------------------------------------------------
+# plain single-signal arm (the same kernels, one signal per launch)
+# ----------------------------------------------------------------------------
+def plain_single_signal(run, device, n_sample=12):
+    """Each sampled signal is solved alone -- its blocks as one BM launch, then
+    its IHC/lambda -- as a single-signal solver does; audio-s/s over the sample."""
+    import torch
+    from cochlearmodel_gb300 import batch
+    from cochlearmodel_gb300.pipeline import ProfileSweep
+    if run.kind != "jnd_sweep":
+        return None
+    rng = np.random.default_rng(1)
+    picks = rng.choice(len(run.groups), size=min(n_sample, len(run.groups)), replace=False)
+    tot_ms = tot_audio = 0.0
+    stream = torch.cuda.current_stream(device)
+    for gi in picks:
+        g = run.groups[gi]
+        p = g.prof[0]
+        noise_db = 1111.0 if p["Wn"] == 0 else 20 * math.log10(p["Wn"] / (10 * 2e-5))
+        spec = [dict(length=g.L, noise=g.noise,
+                     sweep=ProfileSweep(frequencies=[float(p["frequency"])],
+                                        powers=[20 * math.log10(p["dA"] / (10 * 2e-5))],
+                                        noises=[noise_db]))]
+        one = batch.BatchSweep(device, spec, mv=run.mv)
+        for _ in range(2):
+            one.generate_input()
+            one.solve_bm()
+            one.ihc_lambda()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        a.record(stream)
+        one.generate_input()
+        one.solve_bm()
+        one.ihc_lambda()
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        tot_ms += a.elapsed_time(b)
+        tot_audio += one.audio_seconds
+        del one
+    return {"value": tot_audio / (tot_ms / 1000.0), "unit": UNIT,
+            "sample": f"{len(picks)} signals, each solved alone (its blocks in one launch)"}
 
 
 # ----------------------------------------------------------------------------
 # arms
 # ----------------------------------------------------------------------------
-def make_run(device, n_freq):
-    from cochlearmodel_gb300.pipeline import ProfileRun
-    cfg, sweep = tone_sweep_config(n_freq)
-    return ProfileRun(device, cfg, sweep)
-
-
 def run_reference(args, rank, world):
-    """The path's CPU implementation on the host cores.  The input of the sweep
-    is produced by the GPU input kernel when a GPU is present, else by the
-    oracle's restatement of it; the timed work is CPU only."""
+    """The path's CPU restatement on the host cores.  The sweep's input comes
+    from the GPU input kernel when a GPU is present; the timed work is CPU only."""
     if rank != 0:
         return None
     import torch
-    dev = "cuda:0" if torch.cuda.is_available() else None
-    if dev is None:
-        print(json.dumps({"impl": "reference", "unavailable": "needs the input of the sweep"}))
-        return None
-    run = make_run(dev, args.n_freq)
+    if not torch.cuda.is_available():
+        return {"impl": "reference", "unavailable": "needs the generated input of the sweep"}
+    run = make_workload(args.workload, "cuda:0", args.n_freq, args.n_seeds)
     run.generate_input()
     torch.cuda.synchronize()
     vals = []
@@ -196,64 +286,68 @@ def run_reference(args, rank, world):
         if i >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals))
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": run.audio_seconds / value * 1000.0, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "tone_sweep", "signals": run.n_int, "units": len(run.units),
-                       "audio_s_per_step": run.audio_seconds, "sample": "bounded"},
+            "config": {"workload": run.kind, "signals": n_signals(run),
+                       "units": len(run.units), "audio_s_per_step": run.audio_seconds,
+                       "sample": "bounded"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    return line
 
 
 def run_ours(args, rank, world, device):
     import torch
     from cochlearmodel_gb300 import native
 
-    run = make_run(device, args.n_freq)
+    run = make_workload(args.workload, device, args.n_freq, args.n_seeds)
     native.check(native.load().cgb_bm_set_launch_shape(args.shape), "launch shape")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
 
-    # warm-up, with per-stage device times on the last warm-up step
+    # warm-up with per-stage device times (eager), then capture the step
     stage_ms = {}
-    for w in range(args.warmup):
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for _ in range(args.warmup):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(stages(run)) + 1)]
         ev[0].record(stream)
-        run.generate_input()
-        ev[1].record(stream)
-        run.solve_bm()
-        ev[2].record(stream)
-        run.ihc_lambda()
-        ev[3].record(stream)
+        for i, (_, fn) in enumerate(stages(run)):
+            fn()
+            ev[i + 1].record(stream)
         flush.fill_(1.0)
         torch.cuda.synchronize(device)
-        stage_ms = {"input_gen": ev[0].elapsed_time(ev[1]), "bm_solver": ev[1].elapsed_time(ev[2]),
-                    "ihc_lambda": ev[2].elapsed_time(ev[3])}
+        stage_ms = {nm: ev[i].elapsed_time(ev[i + 1]) for i, (nm, _) in enumerate(stages(run))}
     stats = run.d_stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
     flops = bm_flops(stats)
+    lib = native.load()
+    a0 = lib.cgb_kernel_launch_count()
+    run.step()
+    torch.cuda.synchronize(device)
+    per_step_launches = lib.cgb_kernel_launch_count() - a0
+    use_graph = not args.no_graph and hasattr(run, "capture")
+    if use_graph:
+        run.capture()
+        torch.cuda.synchronize(device)
+    step = run.replay if use_graph else run.step
 
     clocks = ClockSampler(device.index if device.index is not None else 0)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(device)
     clocks.start()
-    launches_a = native.load().cgb_kernel_launch_count()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     for i in range(args.steps):
         ev[i][0].record(stream)
-        run.step()
+        step()
         ev[i][1].record(stream)
         flush.fill_(float(i))  # L2 flush between timed steps (256 MB > 129 MB L2)
     torch.cuda.synchronize(device)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    launches = native.load().cgb_kernel_launch_count() - launches_a
     t_total = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
     if world > 1:
         tt = torch.tensor([t_total], device=device)
@@ -261,9 +355,10 @@ def run_ours(args, rank, world, device):
         t_total = float(tt.item())
     value = run.audio_seconds * args.steps * world / t_total
 
-    # e2e: the sweep's profile table in from pinned host memory, the path,
-    # velocity and the three lambda planes back to pinned host memory
-    h_prof = torch.from_numpy(run.prof.view(np.uint8).copy()).pin_memory()
+    # e2e: profile tables in from pinned host memory, the path, velocity and the
+    # three lambda planes back to pinned host memory, through the C ABI
+    tables = [pg["d_prof"] for pg in run.per_group] if run.kind == "jnd_sweep" else [run.d_prof]
+    h_tables = [t.cpu().pin_memory() for t in tables]
     h_v = torch.empty(run.d_v.shape, dtype=torch.float32).pin_memory()
     h_lam = torch.empty(run.d_lam.shape, dtype=torch.float32).pin_memory()
     e_steps = max(1, args.steps // 2)
@@ -272,7 +367,8 @@ def run_ours(args, rank, world, device):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(device)
         a.record(stream)
-        run.d_prof.copy_(h_prof, non_blocking=True)
+        for d_t, h_t in zip(tables, h_tables):
+            d_t.copy_(h_t, non_blocking=True)
         run.step()
         h_v.copy_(run.d_v, non_blocking=True)
         h_lam.copy_(run.d_lam, non_blocking=True)
@@ -282,33 +378,39 @@ def run_ours(args, rank, world, device):
         flush.fill_(float(i))
     e2e = run.audio_seconds * e_steps * world / (e_ms / 1000.0)
 
+    plain = plain_single_signal(run, device) if rank == 0 and not args.no_plain else None
+
     peaks, peak_kind = measured_peaks()
     clock_mhz = peaks.get("sm_max_mhz", 2070.0)
     n_sm = torch.cuda.get_device_properties(device).multi_processor_count
     fp32_peak = 2.0 * 128 * n_sm * clock_mhz * 1e6 / 1e12
-    bm_s = stage_ms["bm_solver"] / 1000.0
-    achieved = flops / bm_s / 1e12
+    achieved = flops / (stage_ms["bm_solver"] / 1000.0) / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1000.0,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "tone_sweep", "signals": run.n_int, "units": len(run.units),
-                   "audio_s_per_step": run.audio_seconds, "fs": run.cfg.Fs,
+        "config": {"workload": run.kind, "signals": n_signals(run), "units": len(run.units),
+                   "audio_s_per_step": run.audio_seconds, "fs": 100000,
                    "l2": "flushed between timed steps (256 MB write)",
-                   "path": "input generation -> BM/OHC solver (20/2 Jacobi sweeps) -> "
-                           "IHC/lambda (3 fibre groups)",
-                   "launch_shape": args.shape, "stage_ms": stage_ms},
-        "gpu_launches": int(launches),
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h_prof.numel()),
+                   "path": " -> ".join(nm for nm, _ in stages(run)),
+                   "bm_semantics": "reference (20/2 Jacobi sweeps)",
+                   "cuda_graph": use_graph, "launch_shape": args.shape,
+                   "stage_ms": stage_ms},
+        "gpu_launches": int(per_step_launches * args.steps),
+        "e2e": {"value": e2e, "unit": UNIT,
+                "h2d_bytes_per_step": int(sum(t.numel() for t in h_tables)),
                 "d2h_bytes_per_step": int(h_v.numel() * 4 + h_lam.numel() * 4)},
         "roofline": {"bound": "fp32", "kernel": "bm_warp_kernel", "achieved": achieved,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                     "traffic": None,
+                     "traffic": BM_TRAFFIC_PER_UNIT * len(run.units),
                      "peak_source": f"2 x 128 FP32 lanes x {n_sm} SMs x sm_max_mhz "
                                     f"({peak_kind} MEASURED_PEAKS.json)"},
         "clocks": clk,
     }
+    if plain is not None:
+        line["plain_single_signal"] = plain
+        line["speedup_vs_plain"] = value / plain["value"]
     return line, run
 
 
@@ -318,11 +420,16 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="jnd_sweep", choices=["jnd_sweep", "tone_sweep"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--shape", type=int, default=0, help="BM kernel launch shape")
     ap.add_argument("--n-freq", type=int, default=64,
-                    help="tones per level (64 = the full tone sweep; less for profiling)")
+                    help="tone_sweep: tones per level (64 = configuration 2)")
+    ap.add_argument("--n-seeds", type=int, default=4,
+                    help="jnd_sweep: noise seeds (4 = 264 signals)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
