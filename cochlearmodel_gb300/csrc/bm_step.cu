@@ -26,6 +26,7 @@
 
 #include "cgb_device.cuh"
 #include "cgb_internal.h"
+#include "warmstart.cuh"
 
 namespace cgb {
 
@@ -46,6 +47,14 @@ struct BMArgs {
   float dt0, dtmin, dtmax;
   int jfast, jslow, max_outer, max_sub;
   double tout, invts;
+  // tolerance mode (jacobi_mode 2)
+  float jtol;
+  int jcap, guess, learn_every;
+  const unsigned char* ws_blob;  // packed network weights (guess 2)
+  float* log;                    // training records [6][256] (optional)
+  long long log_cap;
+  int log_every;
+  int* log_count;
 };
 
 __device__ __forceinline__ float pair_sum8(const float (&t)[kSPL]) {
@@ -103,12 +112,23 @@ struct PrevState {
 
 // One unit, executed by one full warp.  sp: shared [8][256] section
 // parameters; sg / sgs: shared gamma and gamma*S_ohc of the unit's profile.
-template <bool PREV_SMEM>
+//
+// TOL 0: fixed sweep counts (the reference schedule).  TOL 1: tolerance
+// mode; each solve sweeps in pairs until max|p2 - p1| <= jtol * max|p2|
+// (jcap sweeps at most), and the first solve of a step starts from the
+// previous step's pressure (guess 0) or from its linear extrapolation
+// p1 + rho (p1 - p2), rho = dt / dt_prev (guess 1).  TOL 2: as 1, with the
+// network's correction of the extrapolation every learn_every-th step.
+// hist: two 256-float slots per warp holding the pressure at the start of
+// the last two steps; ws_scratch / wblob: inference scratch and weights.
+template <bool PREV_SMEM, int TOL>
 __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
                                          const float* __restrict__ sp,
                                          const float* __restrict__ sg,
                                          const float* __restrict__ sgs, float* prev_slice,
-                                         int lane, cgb_unit_stats* st) {
+                                         float* hist, unsigned char* ws_scratch,
+                                         const unsigned char* wblob, int lane,
+                                         cgb_unit_stats* st) {
   const int base = lane * kSPL;
   float rm[kSPL];
   load8(sp + 1 * 256 + base, rm);
@@ -141,6 +161,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   long long n_sub = 0, n_it = 0, n_sw = 0;
   int n_failed = 0, n_written = 0, status = 0, sub_in_sample = 0;
   float smp_dt = 0.0f, smp_sub = 0.0f, smp_it = 0.0f;  // per-sample sums
+  float dt_prev = dt, rho = 1.0f;
 
   while (n < un.end) {
     if (++sub_in_sample > A.max_sub) {  // dt collapsed: stop this unit, flag it
@@ -148,6 +169,13 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       break;
     }
     int out_loop = 0, reset = 1, another = 1;
+    if (TOL) {
+      // rotate the pressure history: slot (n_sub & 1) receives p at the start
+      // of this step, the other slot holds the start of the previous one
+      rho = __fdiv_rn(dt, dt_prev);
+      dt_prev = dt;
+      store8(hist + (n_sub & 1) * 256 + base, p);
+    }
     const float delta = (float)(tau * A.invts);
     const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
     do {
@@ -227,10 +255,47 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // sections duplicate exactly what the neighbours compute) and the
       // second on its own sections, so one shuffle round serves two sweeps.
       // Sections 254 and 255 carry no lower coefficient; p_{-1} = p_256 = 0.
-      const int J = tm_update ? A.jslow : A.jfast;
+      const int J = TOL ? A.jcap : (tm_update ? A.jslow : A.jfast);
       const float YrmL = __shfl_up_sync(kFull, Yrm[kSPL - 1], 1);
       const float YrmR = __shfl_down_sync(kFull, Yrm[0], 1);
       const bool first = lane == 0, last = lane == 31;
+      if (TOL && out_loop == 0 && n_sub >= 2) {
+        float p2[kSPL];
+        load8(hist + ((n_sub + 1) & 1) * 256 + base, p2);
+        if (A.log && n_sub % A.log_every == 0) {
+          int idx = 0;
+          if (lane == 0) idx = atomicAdd(A.log_count, 1);
+          idx = __shfl_sync(kFull, idx, 0);
+          if (idx < A.log_cap) {
+            float* rec = A.log + (long long)idx * 6 * 256;
+            store8(rec + 0 * 256 + base, Yrm);
+            store8(rec + 1 * 256 + base, p);
+            store8(rec + 2 * 256 + base, p2);
+            store8(rec + 3 * 256 + base, v);
+            store8(rec + 4 * 256 + base, x);
+            float meta[kSPL] = {lane == 0 ? rho : 0.0f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            store8(rec + 5 * 256 + base, meta);
+          }
+        }
+        if (TOL == 2 && n_sub % A.learn_every == 0) {
+          const float* wb = reinterpret_cast<const float*>(wblob + ws::kOffBias);
+          float pe[kSPL];
+          const float nr = ws::make_features(Yrm, p, p2, v, x, rm, rho, wb[201], pe, ws_scratch,
+                                             8, lane);
+          __syncwarp();
+          ws::infer_unit(wblob, ws_scratch, lane);
+          float o[kSPL];
+          load8(reinterpret_cast<const float*>(ws_scratch + ws::kOffOut) + base, o);
+          const float sc = __fmul_rn(nr, wb[200]);
+#pragma unroll
+          for (int k = 0; k < kSPL; ++k) p[k] = __fmaf_rn(sc, o[k], pe[k]);
+          n_sw += 1;  // the residual sweep of the features
+          __syncwarp();
+        } else if (A.guess >= 1) {
+#pragma unroll
+          for (int k = 0; k < kSPL; ++k) p[k] = __fmaf_rn(rho, __fsub_rn(p[k], p2[k]), p[k]);
+        }
+      }
       int it = 0;
       for (; it + 1 < J; it += 2) {
         const float L1 = __shfl_up_sync(kFull, p[kSPL - 1], 1);
@@ -258,8 +323,22 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         const float u7 = last ? 0.0f : __fadd_rn(q[kSPL - 2], qR);
         p[kSPL - 2] = __fmaf_rn(-u6, rm[kSPL - 2], Yrm[kSPL - 2]);
         p[kSPL - 1] = __fmaf_rn(-u7, rm[kSPL - 1], Yrm[kSPL - 1]);
+        if (TOL) {
+          float dm = 0.0f, pm = 0.0f;
+#pragma unroll
+          for (int k = 0; k < kSPL; ++k) {
+            dm = fmaxf(dm, fabsf(__fsub_rn(p[k], q[k])));
+            pm = fmaxf(pm, fabsf(p[k]));
+          }
+          dm = warp_max_xor(dm);
+          pm = warp_max_xor(pm);
+          if (dm <= __fmul_rn(A.jtol, pm)) {
+            it += 2;
+            break;
+          }
+        }
       }
-      if (it < J) {
+      if (!TOL && it < J) {
         float left = __shfl_up_sync(kFull, p[kSPL - 1], 1);
         float right = __shfl_down_sync(kFull, p[0], 1);
         if (first) left = 0.0f;
@@ -276,7 +355,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
 #pragma unroll
         for (int k = 0; k < kSPL; ++k) p[k] = __fmaf_rn(-t[k], rm[k], Yrm[k]);
       }
-      n_sw += J;
+      n_sw += TOL ? it : J;
 
       const float p0 = __shfl_sync(kFull, p[0], 0);
       float da[kSPL];
@@ -376,14 +455,39 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   }
 }
 
-template <int WARPS, int MINB, bool PREV_SMEM>
+// Dynamic shared memory (TOL >= 1): per warp two 256-float history slots;
+// TOL 2 adds the packed weights and the per-warp inference scratch.
+template <int WARPS, int TOL>
+constexpr int bm_dyn_smem() {
+  return WARPS * 2 * 256 * 4 + (TOL == 2 ? ws::kBlobBytes + WARPS * ws::kWarpScratch : 0);
+}
+
+template <int WARPS, int MINB, bool PREV_SMEM, int TOL>
 __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs A) {
   __shared__ __align__(16) float s_par[8 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
   __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 7 * 256 : 4];
+  extern __shared__ __align__(16) unsigned char s_dyn[];
   for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) s_par[i] = A.secp[i];
-  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* hist = nullptr;
+  unsigned char* wblob = nullptr;
+  unsigned char* scratch = nullptr;
+  if (TOL) {
+    hist = reinterpret_cast<float*>(s_dyn) + warp * 512;
+    for (int i = lane; i < 512; i += 32) hist[i] = 0.0f;
+  }
+  if (TOL == 2) {
+    wblob = s_dyn + WARPS * 2 * 256 * 4;
+    scratch = wblob + ws::kBlobBytes + warp * ws::kWarpScratch;
+    const uint4* src = reinterpret_cast<const uint4*>(A.ws_blob);
+    uint4* dst = reinterpret_cast<uint4*>(wblob);
+    for (int i = threadIdx.x; i < ws::kBlobBytes / 16; i += blockDim.x) dst[i] = src[i];
+    // zero rows stay zero: feature rows outside the unit, hidden-buffer tails
+    uint4* z = reinterpret_cast<uint4*>(scratch);
+    for (int i = lane; i < ws::kWarpScratch / 16; i += 32) z[i] = make_uint4(0, 0, 0, 0);
+  }
+  __syncthreads();
   for (;;) {
     int uid = 0;
     if (lane == 0) uid = atomicAdd(A.work, 1);
@@ -399,9 +503,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs 
       s_gam[warp][1][s] = __fmul_rn(gm, s_par[5 * 256 + s]);
     }
     __syncwarp();
-    run_unit<PREV_SMEM>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
-                        PREV_SMEM ? s_prev[warp] : nullptr, lane,
-                        A.stats ? A.stats + uid : nullptr);
+    run_unit<PREV_SMEM, TOL>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
+                             PREV_SMEM ? s_prev[warp] : nullptr, hist, scratch, wblob, lane,
+                             A.stats ? A.stats + uid : nullptr);
     __syncwarp();
   }
 }
@@ -416,19 +520,27 @@ constexpr int kWarpsPerCta = 4;
 struct LaunchShape {
   const void* fn;
   void (*launch)(unsigned, cudaStream_t, const BMArgs&);
+  int dyn_smem;
 };
 
-template <int W, int M, bool PS>
+template <int W, int M, bool PS, int TOL>
 void launch_shape(unsigned grid, cudaStream_t st, const BMArgs& A) {
-  bm_warp_kernel<W, M, PS><<<grid, W * 32, 0, st>>>(A);
+  bm_warp_kernel<W, M, PS, TOL><<<grid, W * 32, bm_dyn_smem<W, TOL>(), st>>>(A);
 }
 
+#define CGB_SHAPE(W, M, PS, TOL)                                                  \
+  {reinterpret_cast<const void*>(bm_warp_kernel<W, M, PS, TOL>), launch_shape<W, M, PS, TOL>, \
+   bm_dyn_smem<W, TOL>()}
+
 const LaunchShape kShapes[] = {
-    {reinterpret_cast<const void*>(bm_warp_kernel<4, 1, false>), launch_shape<4, 1, false>},
-    {reinterpret_cast<const void*>(bm_warp_kernel<4, 3, false>), launch_shape<4, 3, false>},
-    {reinterpret_cast<const void*>(bm_warp_kernel<4, 1, true>), launch_shape<4, 1, true>},
-    {reinterpret_cast<const void*>(bm_warp_kernel<4, 3, true>), launch_shape<4, 3, true>},
+    CGB_SHAPE(4, 1, false, 0),
+    CGB_SHAPE(4, 3, false, 0),
+    CGB_SHAPE(4, 1, true, 0),
+    CGB_SHAPE(4, 3, true, 0),
 };
+// Tolerance-mode kernels: plain / extrapolated guess, and the learned guess.
+const LaunchShape kTolShape = CGB_SHAPE(4, 1, false, 1);
+const LaunchShape kLearnedShape = CGB_SHAPE(4, 1, false, 2);
 int g_shape = 0;
 
 }  // namespace cgb
@@ -450,17 +562,42 @@ extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_p
                               int64_t out_rows, int32_t* d_failed, float* d_conv,
                               cgb_unit_stats* d_stats,
                               int32_t* d_work, void* stream) {
+  return cgb_bm_run_ex_dev(d_secp, d_gamma, n_profiles, sc, d_units, n_units, d_in, in_len, d_out,
+                           out_rows, d_failed, d_conv, d_stats, d_work, nullptr, stream);
+}
+
+extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int n_profiles,
+                                 const cgb_bm_scalars* sc, const cgb_unit* d_units, int n_units,
+                                 const float* d_in, int64_t in_len, float* d_out,
+                                 int64_t out_rows, int32_t* d_failed, float* d_conv,
+                                 cgb_unit_stats* d_stats, int32_t* d_work,
+                                 const cgb_bm_extras* ex, void* stream) {
   using namespace cgb;
   if (n_units == 0) return CGB_OK;  // an empty table enqueues nothing
   if (!d_secp || !d_gamma || !sc || !d_units || !d_in || !d_out || !d_work)
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: null pointer argument");
   if (n_units < 0 || n_profiles <= 0 || in_len <= 0 || out_rows <= 0)
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: bad sizes");
-  if (sc->red_lanes != 32 || sc->jacobi_mode != 0)
-    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: only red_lanes=32, jacobi_mode=0 are built");
+  if (sc->red_lanes != 32 || (sc->jacobi_mode != 0 && sc->jacobi_mode != 2))
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: only red_lanes=32, jacobi_mode 0 or 2 are built");
   if (sc->jacobi_fast < 0 || sc->jacobi_slow < 0 || sc->max_outer < 1 ||
       sc->max_substeps_per_sample < 1)
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: bad loop counts");
+  const bool tol = sc->jacobi_mode == 2;
+  if (tol && (sc->jacobi_cap < 2 || (sc->jacobi_cap & 1) || !(sc->jacobi_tol >= 0.0f) ||
+              sc->guess_mode < 0 || sc->guess_mode > 2))
+    return fail(CGB_ERR_ARG,
+                "cgb_bm_run_dev: jacobi_mode 2 needs an even jacobi_cap >= 2, jacobi_tol >= 0 "
+                "and guess_mode 0, 1 or 2");
+  const bool learned = tol && sc->guess_mode == 2;
+  if (learned && (!ex || !ex->d_ws_blob || sc->learned_every < 1))
+    return fail(CGB_ERR_ARG,
+                "cgb_bm_run_dev: guess_mode 2 needs network weights and learned_every >= 1");
+  if (ex && ex->d_log && (!tol || !ex->d_log_count || ex->log_every < 1 || ex->log_cap < 0))
+    return fail(CGB_ERR_ARG,
+                "cgb_bm_run_dev: logging needs jacobi_mode 2, a counter and log_every >= 1");
+  if (learned && (reinterpret_cast<uintptr_t>(ex->d_ws_blob) & 15))
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: the weight blob must be 16-byte aligned");
   if ((reinterpret_cast<uintptr_t>(d_out) & 15) || (reinterpret_cast<uintptr_t>(d_secp) & 15))
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: d_out and d_secp must be 16-byte aligned");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -497,14 +634,32 @@ extern "C" int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_p
   A.max_sub = sc->max_substeps_per_sample;
   A.tout = (double)sc->time_step_out;
   A.invts = 1.0 / (double)sc->Ts;
+  A.jtol = sc->jacobi_tol;
+  A.jcap = sc->jacobi_cap;
+  A.guess = tol ? sc->guess_mode : 0;
+  A.learn_every = sc->learned_every < 1 ? 1 : sc->learned_every;
+  A.ws_blob = learned ? static_cast<const unsigned char*>(ex->d_ws_blob) : nullptr;
+  A.log = ex && tol ? ex->d_log : nullptr;
+  A.log_cap = ex ? ex->log_cap : 0;
+  A.log_every = ex && ex->log_every > 0 ? ex->log_every : 1;
+  A.log_count = ex ? ex->d_log_count : nullptr;
 
   int dev = 0, n_sm = 0, per_sm = 0;
   CGB_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
   CGB_TRY_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev),
                "cudaDeviceGetAttribute");
-  const LaunchShape& shape = kShapes[g_shape];
+  const LaunchShape& shape = learned ? kLearnedShape : tol ? kTolShape : kShapes[g_shape];
+  if (shape.dyn_smem > 48 * 1024) {
+    static int configured[64] = {};
+    if (dev < 64 && !configured[dev]) {
+      CGB_TRY_CUDA(cudaFuncSetAttribute(shape.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        shape.dyn_smem),
+                   "cudaFuncSetAttribute(bm learned)");
+      configured[dev] = 1;
+    }
+  }
   CGB_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shape.fn,
-                                                             kWarpsPerCta * 32, 0),
+                                                             kWarpsPerCta * 32, shape.dyn_smem),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
   if (per_sm < 1) per_sm = 1;
   long long want = (n_units + kWarpsPerCta - 1) / kWarpsPerCta;

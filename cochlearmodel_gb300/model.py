@@ -157,7 +157,35 @@ def bm_scalars(cfg: RunConfig, mv: ModelVectors) -> native.BMScalars:
     sc.red_lanes = 32
     sc.jacobi_mode = 0
     sc.max_substeps_per_sample = 1 << 20
+    sc.jacobi_tol = 0.0
+    sc.jacobi_cap = 0
+    sc.guess_mode = 0
+    sc.learned_every = 1
     return sc
+
+
+# Tolerance of the tolerance-mode Jacobi solve: the corrector's acceptance
+# test compares successive velocities to |v| dt, so the pressure must settle
+# to about 1e-6 of its maximum; at 1e-5 outer iterations grow and steps fail.
+JACOBI_TOL = 1e-6
+JACOBI_CAP = 400
+
+
+def tolerance_mode(sc: native.BMScalars, guess: int = 1, tol: float = JACOBI_TOL,
+                   cap: int = JACOBI_CAP, learned_every: int = 1) -> native.BMScalars:
+    """A copy of `sc` in jacobi_mode 2: every pressure solve sweeps (in pairs)
+    until max|p2 - p1| <= tol * max|p2|, at most `cap` sweeps; the first solve
+    of a step starts from the previous pressure (guess 0), its linear
+    extrapolation (1) or the extrapolation plus the network's correction (2,
+    every learned_every-th step).  The reference runs fixed sweep counts
+    (JACOBBY_Loops_Slow/Fast) instead."""
+    o = native.BMScalars.from_buffer_copy(sc)
+    o.jacobi_mode = 2
+    o.jacobi_tol = tol
+    o.jacobi_cap = cap
+    o.guess_mode = guess
+    o.learned_every = learned_every
+    return o
 
 
 def block_partition(time_blocks: int, samples_p1: int, overlap: int, decouple: int):

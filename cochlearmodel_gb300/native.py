@@ -35,7 +35,9 @@ class BMScalars(C.Structure):
         "alpha_l", "alpha_s", "Gme", "a0", "a1", "a2", "sigma_ow", "eta_1", "eta_2",
         "dt_min", "dt_max")] + [(n, C.c_int32) for n in (
             "jacobi_fast", "jacobi_slow", "max_outer", "red_lanes", "jacobi_mode",
-            "max_substeps_per_sample")]
+            "max_substeps_per_sample")] + [("jacobi_tol", C.c_float), ("jacobi_cap", C.c_int32),
+                                           ("guess_mode", C.c_int32),
+                                           ("learned_every", C.c_int32)]
 
 
 class CGBError(RuntimeError):
@@ -74,7 +76,27 @@ _SIGS = {
     "cgb_bm_launch_shape_count": (_i, []),
     "cgb_bm_run_dev": (_i, [_p, _p, _i, C.POINTER(BMScalars), _p, _i, _p, _i64, _p, _i64,
                             _p, _p, _p, _p, _p]),
+    "cgb_bm_run_ex_dev": (_i, [_p, _p, _i, C.POINTER(BMScalars), _p, _i, _p, _i64, _p, _i64,
+                               _p, _p, _p, _p, C.c_void_p, _p]),
+    "cgb_ws_blob_bytes": (_i, []),
+    "cgb_ws_blobT_bytes": (_i, []),
+    "cgb_ws_param_count": (_i, []),
+    "cgb_ws_pack_dev": (_i, [_p, C.c_float, C.c_float, _p, _p, _p]),
+    "cgb_ws_prepare_dev": (_i, [_p, _i, _p, C.c_float, _p, _p, _p, _p, _p]),
+    "cgb_ws_forward_dev": (_i, [_p, _p, _i, _p, _p, _p]),
+    "cgb_ws_loss_dev": (_i, [_p, _p, _i, C.c_float, _p, _p, _p]),
+    "cgb_ws_backward_dev": (_i, [_p, _p, _p, _i, _p, _p]),
+    "cgb_ws_wgrad_dev": (_i, [_p, _p, _p, _p, _i, _p, _i, _p, _p]),
+    "cgb_ws_adam_dev": (_i, [_p, _p, _p, _p, _i, C.c_float, C.c_float, C.c_float, C.c_float,
+                             _p]),
+    "cgb_ws_infer_dev": (_i, [_p, _p, _i, _p, _p]),
 }
+
+
+class BMExtras(C.Structure):
+    """cgb_bm_extras: network weights and training-record logging."""
+    _fields_ = [("d_ws_blob", C.c_void_p), ("d_log", C.c_void_p), ("log_cap", C.c_int64),
+                ("log_every", C.c_int32), ("pad_", C.c_int32), ("d_log_count", C.c_void_p)]
 
 
 def lib_path() -> Path:

@@ -44,20 +44,25 @@ class BMSolver:
     def run_dev(self, sc: native.BMScalars, gamma: torch.Tensor, units: torch.Tensor,
                 n_units: int, inp: torch.Tensor, out: torch.Tensor,
                 failed: torch.Tensor | None = None, stats: torch.Tensor | None = None,
-                stream: torch.cuda.Stream | None = None, conv: torch.Tensor | None = None) -> None:
+                stream: torch.cuda.Stream | None = None, conv: torch.Tensor | None = None,
+                extras: native.BMExtras | None = None) -> None:
         """Enqueues the solver on `stream` (default: torch's current stream).
         All tensors live on this solver's device; `units` holds cgb_unit
-        records (see units_to_device) already validated by check_units."""
+        records (see units_to_device) already validated by check_units.
+        extras: network weights / training-record logging of the tolerance
+        mode (jacobi_mode 2)."""
         st = stream if stream is not None else torch.cuda.current_stream(self.device)
-        native.check(self.lib.cgb_bm_run_dev(
+        native.check(self.lib.cgb_bm_run_ex_dev(
             native.ptr(self.secp), native.ptr(gamma), int(gamma.shape[0]), C.byref(sc),
             native.ptr(units), int(n_units), native.ptr(inp), int(inp.numel()),
             native.ptr(out), int(out.shape[0]), native.ptr(failed), native.ptr(conv),
-            native.ptr(stats),
-            native.ptr(self.work), C.c_void_p(st.cuda_stream)), "cgb_bm_run_dev")
+            native.ptr(stats), native.ptr(self.work),
+            C.cast(C.byref(extras), C.c_void_p) if extras is not None else None,
+            C.c_void_p(st.cuda_stream)), "cgb_bm_run_dev")
 
     def run(self, sc: native.BMScalars, gamma: np.ndarray, units: np.ndarray,
-            inp: np.ndarray, out_rows: int, want_conv: bool = False):
+            inp: np.ndarray, out_rows: int, want_conv: bool = False,
+            extras: native.BMExtras | None = None):
         """Host-buffer call: validates, uploads, solves, downloads.
         Returns (velocity float32[out_rows,256], failed int32[out_rows], stats)
         and, with want_conv, the per-sample statistics float32[out_rows,3]."""
@@ -73,7 +78,7 @@ class BMSolver:
         stats = torch.zeros((len(units), native.STATS_DTYPE.itemsize), dtype=torch.uint8,
                             device=d)
         conv = torch.zeros((out_rows, 3), dtype=torch.float32, device=d) if want_conv else None
-        self.run_dev(sc, g, u, len(units), x, out, failed, stats, conv=conv)
+        self.run_dev(sc, g, u, len(units), x, out, failed, stats, conv=conv, extras=extras)
         torch.cuda.synchronize(d)
         st = stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
         if want_conv:

@@ -81,9 +81,28 @@ typedef struct cgb_bm_scalars {
   int32_t jacobi_slow;  /* sweeps on outer iterations 0-1 (JACOBBY_Loops_Slow)  */
   int32_t max_outer;    /* Cuda_Outern_Loops                                   */
   int32_t red_lanes;    /* reduction tree width; must be 32                    */
-  int32_t jacobi_mode;  /* must be 0 (fixed sweeps, reference semantics)       */
+  int32_t jacobi_mode;  /* 0: fixed sweeps (reference semantics);
+                           2: sweep pairs until max|dp| <= jacobi_tol * max|p|
+                              or jacobi_cap sweeps                            */
   int32_t max_substeps_per_sample; /* guard against a collapsed dt (>= 1)       */
+  float jacobi_tol;     /* mode 2 stopping tolerance (relative, infinity norm) */
+  int32_t jacobi_cap;   /* mode 2 sweep cap per solve (even, >= 2)             */
+  int32_t guess_mode;   /* mode 2 first-solve guess of a step: 0 previous
+                           pressure, 1 linear extrapolation of the last two,
+                           2 extrapolation + the network's correction        */
+  int32_t learned_every;/* guess 2: network every n-th step (others: 1)      */
 } cgb_bm_scalars;
+
+/* Optional inputs of cgb_bm_run_ex_dev. */
+typedef struct cgb_bm_extras {
+  const void* d_ws_blob;  /* packed network weights (cgb_ws_pack_dev), guess 2 */
+  float* d_log;           /* training records float[log_cap][6][256]: Y/m, p,
+                             p_prev, v, x, {rho, 0...}; NULL: no logging     */
+  int64_t log_cap;
+  int32_t log_every;      /* record every n-th step start of each unit       */
+  int32_t pad_;
+  int32_t* d_log_count;   /* records claimed (may exceed log_cap)            */
+} cgb_bm_extras;
 
 /* One frame of the IHC/lambda stage: a run of consecutive velocity rows that
  * the reference filters as one buffer (one Run_Cuda chunk, or one signal of a
@@ -160,6 +179,50 @@ int cgb_bm_run_dev(const float* d_secp, const float* d_gamma, int n_profiles,
                    const float* d_in, int64_t in_len, float* d_out, int64_t out_rows,
                    int32_t* d_failed, float* d_conv, cgb_unit_stats* d_stats, int32_t* d_work,
                    void* stream);
+
+/* cgb_bm_run_dev with the tolerance-mode extras (jacobi_mode 2): the network
+ * weights of guess_mode 2 and the logging of training records.  ex may be
+ * NULL.  No counterpart in the reference (it runs fixed sweep counts). */
+int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int n_profiles,
+                      const cgb_bm_scalars* sc, const cgb_unit* d_units, int n_units,
+                      const float* d_in, int64_t in_len, float* d_out, int64_t out_rows,
+                      int32_t* d_failed, float* d_conv, cgb_unit_stats* d_stats,
+                      int32_t* d_work, const cgb_bm_extras* ex, void* stream);
+
+/* Learned Jacobi warm start: training and inference of the 4-layer 1-D
+ * convolution network (8 -> 64 -> 64 -> 64 -> 1 channels, width 5, BF16
+ * weights and activations, FP32 accumulation on the tensor cores).  No
+ * counterpart in the reference.
+ *   params   float[cgb_ws_param_count()] canonical FP32 parameters:
+ *            W1[5][64][8], b1[64], W2[5][64][64], b2[64], W3[5][64][64],
+ *            b3[64], W4[5][64], b4[1]   (W[tap][out][in])
+ *   blob     packed BF16 forward weights (cgb_ws_blob_bytes(), 16-B aligned)
+ *   blobT    transposed weights for the backward pass (cgb_ws_blobT_bytes())
+ *   records  float[n][6][256] logged by cgb_bm_run_ex_dev
+ *   feat     BF16 [n][280][8] features (section s at row s + 8)
+ *   target   float[n][256] (p* - pe) / max|rt|; nr float[n] = max|rt|
+ *   hid      BF16 [3][n][256][64] hidden activations (64-channel rows)
+ *   dout     BF16 [n][256][8] dL/d(output); dpre BF16 [3][n][256][64]
+ *   partial  float[n_parts][cgb_ws_param_count()]; grad float[param_count] */
+int cgb_ws_blob_bytes(void);
+int cgb_ws_blobT_bytes(void);
+int cgb_ws_param_count(void);
+int cgb_ws_pack_dev(const float* d_params, float s_out, float rm_scale, void* d_blob,
+                    void* d_blobT, void* stream);
+int cgb_ws_prepare_dev(const float* d_records, int n, const float* d_rm, float rm_scale,
+                       void* d_feat, float* d_target, float* d_nr, double* d_work, void* stream);
+int cgb_ws_forward_dev(const void* d_blob, const void* d_feat, int n, void* d_hid, float* d_out,
+                       void* stream);
+int cgb_ws_loss_dev(const float* d_out, const float* d_target, int n, float s_out, void* d_dout,
+                    double* d_loss_part, void* stream);
+int cgb_ws_backward_dev(const void* d_blobT, const void* d_dout, const void* d_hid, int n,
+                        void* d_dpre, void* stream);
+int cgb_ws_wgrad_dev(const void* d_feat, const void* d_hid, const void* d_dpre,
+                     const void* d_dout, int n, float* d_partial, int n_parts, float* d_grad,
+                     void* stream);
+int cgb_ws_adam_dev(float* d_params, const float* d_grad, float* d_m, float* d_v, int step,
+                    float lr, float beta1, float beta2, float eps, void* stream);
+int cgb_ws_infer_dev(const void* d_blob, const void* d_feat, int n, float* d_out, void* stream);
 
 /* IHC + lambda over n_frames frames (host frame table, device buffers).
  *   d_v      float[v_rows][256]  BM velocity (16-byte aligned)

@@ -204,8 +204,14 @@ typedef struct {
   float dt_min, dt_max;
   int32_t jacobi_fast, jacobi_slow, max_outer;
   int32_t red_lanes;   // reduction tree width (sections per lane = 256/red_lanes)
-  int32_t jacobi_mode; // 0 fixed sweeps (reference), 1 exact tridiagonal solve
+  int32_t jacobi_mode; // 0 fixed sweeps (reference), 1 exact tridiagonal solve,
+                       // 2 sweep pairs to a tolerance
   int32_t max_substeps_per_sample;  // a unit stops (status 1) past this many steps in a sample
+  float jacobi_tol;    // mode 2: stop when max|p2 - p1| <= jacobi_tol * max|p2|
+  int32_t jacobi_cap;  // mode 2: at most this many sweeps per solve (even)
+  int32_t guess_mode;  // mode 2 first-solve guess: 0 previous pressure, 1 extrapolated
+                       // (2, the network's guess, is GPU-only and treated as 1 here)
+  int32_t learned_every;
 } orc_bm_scalars;
 
 float orc_tanhf(float x) { return own_tanhf(x); }
@@ -337,6 +343,19 @@ T tree_sum(const T* term, int lanes) {
   return part[0];
 }
 
+// One Jacobi sweep, src -> dst: dst_s = fma(-(l_s src_{s-1} + src_{s+1}), 1/m_s, Y_s/m_s)
+// with l_s = 0 on sections 254 and 255 and src_{-1} = src_256 = 0.
+template <typename T>
+void jacobi_sweep(const T* src, T* dst, const T* Yrm, const T* rm) {
+  using A = Ar<T>;
+  for (int s = 0; s < NS; ++s) {
+    T pm1 = s > 0 ? src[s - 1] : (T)0;
+    T pp1 = s < NS - 1 ? src[s + 1] : (T)0;
+    T t = s < NS - 2 ? pm1 + pp1 : pp1;
+    dst[s] = A::fma(-t, rm[s], Yrm[s]);
+  }
+}
+
 template <typename T>
 void exact_solve(const T* Y, const T* rm, T* p) {
   // kernel matrix: row s: l_s p_{s-1} + m_s p_s + p_{s+1} = Y_s,
@@ -383,6 +402,9 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
   T dt = (T)sc.time_step;
   double tau = 0.0;
   int64_t n = un.start;
+  // tolerance mode: pressure at the start of the last two steps, dt ratio
+  T hist[2][NS] = {};
+  T dt_prev = dt, rho = (T)1;
   T sx0 = (T)inb[n], sx1 = (T)inb[n + 1];
   int fail_flag = 0;
   int64_t sub_in_sample = 0;
@@ -393,6 +415,11 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
       break;
     }
     int out_loop = 0, reset = 1, another = 1;
+    if (sc.jacobi_mode == 2) {
+      rho = dt / dt_prev;
+      dt_prev = dt;
+      for (int s = 0; s < NS; ++s) hist[S.substeps & 1][s] = p[s];
+    }
     const T delta = std::is_same<T, float>::value ? (T)(float)(tau * invTs) : (T)(tau * invTs);
     const T smp = A::fma(sx1, delta, sx0 * ((T)1 - delta));
     while (another) {
@@ -450,6 +477,31 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
       int J = out_loop < 2 ? sc.jacobi_slow : sc.jacobi_fast;
       if (sc.jacobi_mode == 1) {
         exact_solve<T>(Y, md.rm, p);
+      } else if (sc.jacobi_mode == 2) {
+        // Tolerance mode: sweeps run in pairs; after each pair the update of
+        // the second sweep and the pressure are measured in the infinity
+        // norm, and the solve stops when max|p2 - p1| <= tol * max|p2| or at
+        // the sweep cap.  The GPU kernel checks at the same points.
+        for (int s = 0; s < NS; ++s) Yrm[s] = Y[s] * md.rm[s];
+        if (out_loop == 0 && S.substeps >= 2 && sc.guess_mode >= 1) {
+          // p1 + rho (p1 - p2): linear extrapolation of the last two steps
+          const T* p2 = hist[(S.substeps + 1) & 1];
+          for (int s = 0; s < NS; ++s) p[s] = A::fma(rho, p[s] - p2[s], p[s]);
+        }
+        const T tol = (T)sc.jacobi_tol;
+        int done = 0;
+        while (done < sc.jacobi_cap) {
+          jacobi_sweep<T>(p, tmp, Yrm, md.rm);
+          jacobi_sweep<T>(tmp, p, Yrm, md.rm);
+          done += 2;
+          T dmax = 0, pmax = 0;
+          for (int s = 0; s < NS; ++s) {
+            dmax = A::max(dmax, A::abs(p[s] - tmp[s]));
+            pmax = A::max(pmax, A::abs(p[s]));
+          }
+          if (dmax <= tol * pmax) break;
+        }
+        S.sweeps += done;
       } else {
         // p_s <- (Y_s - (l_s p_{s-1} + p_{s+1})) / m_s, evaluated as
         // fma(-t, 1/m_s, Y_s/m_s) with Y_s/m_s formed once per iteration.

@@ -31,7 +31,9 @@ class OrcScalars(C.Structure):
         "alpha_l", "alpha_s", "Gme", "a0", "a1", "a2", "sigma_ow", "eta_1", "eta_2",
         "dt_min", "dt_max")] + [(n, C.c_int32) for n in (
             "jacobi_fast", "jacobi_slow", "max_outer", "red_lanes", "jacobi_mode",
-            "max_substeps_per_sample")]
+            "max_substeps_per_sample")] + [("jacobi_tol", C.c_float), ("jacobi_cap", C.c_int32),
+                                           ("guess_mode", C.c_int32),
+                                           ("learned_every", C.c_int32)]
 
 
 _lib = None
@@ -39,8 +41,8 @@ _p = C.c_void_p
 
 
 def build(force: bool = False) -> Path:
-    src = HERE / "cochlea_oracle.cpp"
-    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+    srcs = [HERE / "cochlea_oracle.cpp", HERE / "warmstart_oracle.cpp", HERE / "build.sh"]
+    if force or not LIB.exists() or any(LIB.stat().st_mtime < f.stat().st_mtime for f in srcs):
         subprocess.run(["sh", str(HERE / "build.sh")], check=True)
     return LIB
 
@@ -68,6 +70,9 @@ def load():
                                 _p, C.c_double, C.c_double, _p, _p, C.c_int]
         lib.orc_jnd_db.restype = C.c_double
         lib.orc_jnd_db.argtypes = [C.c_double, C.c_double, C.c_double]
+        lib.orc_ws_param_count.restype = C.c_int
+        lib.orc_ws_forward_backward.argtypes = [_p, _p, _p, C.c_int, C.c_float, C.c_int, _p, _p,
+                                                _p]
         lib.orc_input_gen.argtypes = [_p, C.c_int, _p, C.c_int, C.c_int, C.c_float,
                                       C.c_double, C.c_double, C.c_double, _p]
         _lib = lib
@@ -180,3 +185,19 @@ def input_gen(prof, wn, interval_len, head, Fs, wn_dc, wn_norm, sig_norm):
     load().orc_input_gen(_ptr(prof), prof.shape[0], _ptr(wn), interval_len, head, Fs, wn_dc,
                          wn_norm, sig_norm, _ptr(out))
     return out
+
+
+def ws_forward_backward(params, feat, target, s_out, round_bf16=True, want_grad=True):
+    """The warm-start network in FP64 (cochlearmodel_gb300/csrc/warmstart.cu):
+    returns (output[n,256], mean loss, grad[param_count] or None).
+    feat: float[n,256,8]; target: float[n,256]."""
+    params = np.ascontiguousarray(params, np.float32)
+    feat = np.ascontiguousarray(feat, np.float32)
+    target = np.ascontiguousarray(target, np.float32)
+    n = feat.shape[0]
+    out = np.zeros((n, 256), np.float64)
+    loss = np.zeros(1, np.float64)
+    grad = np.zeros(load().orc_ws_param_count(), np.float64) if want_grad else None
+    load().orc_ws_forward_backward(_ptr(params), _ptr(feat), _ptr(target), n, s_out,
+                                   1 if round_bf16 else 0, _ptr(out), _ptr(loss), _ptr(grad))
+    return out, float(loss[0]), grad

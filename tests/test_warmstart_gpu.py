@@ -1,0 +1,147 @@
+"""Tolerance-mode Jacobi and the learned warm start on the GPU.
+
+* tolerance mode (jacobi_mode 2) with the previous-step and the extrapolated
+  guess: bit-exact against the FP32 oracle (same sweeps, same stopping points);
+* the network: the BM kernel's fused per-warp inference equals the training
+  forward bit for bit, and forward, loss and gradients of the training
+  kernels match the FP64 oracle restatement (oracle/warmstart_oracle.cpp);
+* the learned guess runs inside the BM kernel to the same tolerance.
+"""
+import numpy as np
+import pytest
+
+from cochlearmodel_gb300 import model
+from oracle import oracle as orc
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("guess", [0, 1])
+@pytest.mark.parametrize("db,freq", [(60.0, 1000.0), (100.0, 4000.0)])
+def test_tolerance_mode_bit_exact(mv, bm_solver, guess, db, freq):
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=2.0, db=db, freq=freq)
+    tsc = model.tolerance_mode(sc, guess=guess)
+    o_v, o_f, o_st = orc.bm_run(mv.section_params(), gamma, tsc, units, x, rows)
+    g_v, g_f, g_st = bm_solver.run(tsc, gamma, units, x, rows)
+    assert np.array_equal(g_v.view(np.uint32), o_v.view(np.uint32)), np.abs(g_v - o_v).max()
+    assert np.array_equal(g_f, o_f)
+    for k in ("substeps", "iterations", "sweeps", "status"):
+        assert np.array_equal(g_st[k], o_st[k]), k
+    assert g_st["sweeps"].sum() > 0
+
+
+@pytest.fixture(scope="module")
+def ws_data(bm_solver):
+    """Records logged by the solver on a few warm-start signals, prepared."""
+    from cochlearmodel_gb300 import warmstart as W
+    batch = W.signal_batch(6, ms=4.0, seed=11)
+    rec = W.log_records(bm_solver, batch, cap=96, every=37)
+    assert rec.shape[0] >= 48
+    net = W.WarmStartNet(seed=3)
+    feat, target, nr = net.prepare(rec)
+    net.s_out = W.fit_output_scale(target)
+    net.pack()
+    return W, net, rec, feat, target, nr
+
+
+def test_features_and_targets(ws_data):
+    W, net, rec, feat, target, nr = ws_data
+    f = feat.float().cpu().numpy()
+    assert np.all(f[:, :8] == 0) and np.all(f[:, 264:] == 0)
+    body = f[:, 8:264]
+    # normalised channels lie in [-1, 1] and reach 1 in magnitude
+    for c in (0, 1, 3, 5, 6):
+        m = np.abs(body[:, :, c]).max(axis=1)
+        assert np.all(m <= 1.0 + 1e-6)
+        assert np.all((m > 0.99) | (m == 0))
+    assert np.all(np.isfinite(target.cpu().numpy()))
+    assert float(nr.min().item()) > 0.0
+    # the exact pressure solves the scaled tridiagonal system
+    r = rec.cpu().numpy().astype(np.float64)
+    rm = mv_rm()
+    t = target.cpu().numpy().astype(np.float64)
+    i = 0
+    Yrm, p1, p2 = r[i, 0:256], r[i, 256:512], r[i, 512:768]
+    rho = r[i, 1280]
+    pe = (np.float32(rho) * (p1 - p2).astype(np.float32) + p1.astype(np.float32)).astype(
+        np.float64)
+    pstar = pe + t[i] * float(nr[i].item())
+    lo = np.where(np.arange(256) < 254, 1.0, 0.0)
+    res = pstar + rm * (np.concatenate([[0.0], pstar[:-1]]) * lo +
+                        np.concatenate([pstar[1:], [0.0]])) - Yrm
+    assert np.abs(res).max() <= 1e-4 * np.abs(Yrm).max()
+
+
+def mv_rm():
+    return model.ModelVectors.build().section_params()[1].astype(np.float64)
+
+
+def test_fused_inference_equals_training_forward(ws_data):
+    W, net, rec, feat, target, nr = ws_data
+    a = net.forward(feat).cpu().numpy()
+    b = net.infer(feat).cpu().numpy()
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), np.abs(a - b).max()
+
+
+def test_forward_and_gradients_match_oracle(ws_data):
+    W, net, rec, feat, target, nr = ws_data
+    n = min(32, feat.shape[0])
+    f = feat[:n].contiguous()
+    t = target[:n].contiguous()
+    loss, grad = net.gradients(f, t)
+    g_out = net.forward(f).cpu().numpy()
+    g_grad = grad.cpu().numpy().astype(np.float64)
+    fnp = f[:, 8:264].float().cpu().numpy()
+    o_out, o_loss, o_grad = orc.ws_forward_backward(net.params.cpu().numpy(), fnp,
+                                                    t.cpu().numpy(), net.s_out, round_bf16=True)
+    assert np.abs(g_out - o_out).max() <= 1e-3 * np.abs(o_out).max()
+    assert abs(float(loss.item()) - o_loss) <= 1e-3 * o_loss
+    # per tensor: W1, b1, W2, b2, W3, b3, W4, b4
+    bounds = np.cumsum([0, 2560, 64, 20480, 64, 20480, 64, 320, 1])
+    for k in range(8):
+        a, b = g_grad[bounds[k]:bounds[k + 1]], o_grad[bounds[k]:bounds[k + 1]]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert rel <= 5e-3, (k, rel)
+
+
+def test_learned_guess_in_the_solver(mv, bm_solver, ws_data):
+    """The network's guess inside the BM kernel: the solve still runs to the
+    tolerance, so the velocity agrees with the extrapolated-guess run to the
+    tolerance's effect, and every step still converges."""
+    W, net, rec, feat, target, nr = ws_data
+    batch = W.signal_batch(4, ms=3.0, seed=5)
+    r1 = W.evaluate(bm_solver, batch, guess=1)
+    r2 = W.evaluate(bm_solver, batch, guess=2, net=net)
+    assert r1["status"] == 0 and r2["status"] == 0
+    assert W.max_rel(r2["velocity"], r1["velocity"]) <= 2e-2
+    assert r2["failed"].sum() <= r1["failed"].sum() + 2
+
+
+def test_trained_network_gain(mv, bm_solver):
+    """What the trained network (weights trained on the GPU by the library's
+    own kernels, cochlearmodel_gb300/warmstart_weights.npz) gains on held-out
+    seeds at the unchanged tolerance:
+      * its prediction of the exact-pressure correction on held-out records
+        leaves < 5 % of the error of no correction;
+      * the first solve of every step started from its guess needs fewer
+        Jacobi sweeps per step than from the plain previous-step guess.
+    The extrapolation alone (guess 1) is measured beside it."""
+    import torch
+    from cochlearmodel_gb300 import warmstart as W
+    net = W.WarmStartNet.load(W.WEIGHTS)
+    held = W.signal_batch(16, ms=10.0, seed=4321)
+    rec = W.log_records(bm_solver, held, cap=2000, every=53)
+    feat, target, nr = net.prepare(rec)
+    with torch.no_grad():
+        o = net.forward(feat)
+        mse = float(((net.s_out * o - target) ** 2).mean().item())
+        zero = float((target ** 2).mean().item())
+    assert mse < 0.05 * zero, (mse, zero)
+    r0 = W.evaluate(bm_solver, held, guess=0)
+    r1 = W.evaluate(bm_solver, held, guess=1)
+    r2 = W.evaluate(bm_solver, held, guess=2, net=net)
+    print("sweeps per step: previous %.2f extrapolated %.2f learned %.2f" %
+          (r0["sweeps_per_step"], r1["sweeps_per_step"], r2["sweeps_per_step"]))
+    assert r0["status"] == r1["status"] == r2["status"] == 0
+    assert r2["sweeps_per_step"] < 0.85 * r0["sweeps_per_step"]
