@@ -137,17 +137,24 @@ class BatchSweep:
         self.W = np.asarray(self.nerve.W, np.float32)
         self.d_nihc = torch.from_numpy(self.nerve.nihc()).to(d)
         self.per_group = []
-        for g in self.groups:
+        ivs = []
+        for gi, g in enumerate(self.groups):
             head, length = self.jnd_win.nodes(Fs, g.L)
             n = len(g.prof)
             self.per_group.append(dict(
                 d_prof=torch.from_numpy(g.prof.view(np.uint8).copy()).to(d),
                 d_wn=None if g.noise is None else torch.from_numpy(g.noise).to(d),
-                d_dA=torch.from_numpy(np.ascontiguousarray(g.prof["dA"])).to(d),
-                d_ref=torch.from_numpy(np.ascontiguousarray(g.ref_of, np.int32)).to(d),
-                d_FRA=torch.zeros((3, n), dtype=torch.float64, device=d),
-                d_FAI=torch.zeros((3, n), dtype=torch.float64, device=d),
-                head=head, len=length, n=n))
+                head=head, len=length, n=n, out0=len(ivs)))
+            # the group's lambda rows start at its frame's first row; interval
+            # i's window at + i * L + head
+            r0 = int(self.frames["lam_row0"][gi])
+            for i in range(n):
+                ivs.append((r0 + i * g.L + head, r0 + int(g.ref_of[i]) * g.L + head,
+                            float(g.prof["dA"][i]), length, len(ivs)))
+        self.jnd_iv = np.array(ivs, dtype=native.JND_INTERVAL_DTYPE)
+        self.d_jnd_iv = torch.from_numpy(self.jnd_iv.view(np.uint8).copy()).to(d)
+        self.d_FRA = torch.zeros((3, len(ivs)), dtype=torch.float64, device=d)
+        self.d_FAI = torch.zeros((3, len(ivs)), dtype=torch.float64, device=d)
         self.graph = None
 
     @property
@@ -184,14 +191,12 @@ class BatchSweep:
             native.ptr(self.ihc.status), self._stream(stream)), "cgb_ihc_lambda_launch_dev")
 
     def jnd_sums(self, stream=None):
-        for gi, (g, pg) in enumerate(zip(self.groups, self.per_group)):
-            lam = native.ptr(self.d_lam) + 4 * 256 * int(self.frames["lam_row0"][gi])
-            native.check(self.lib.cgb_jnd_dev(
-                lam, self.lam_rows, pg["n"], g.L, pg["head"], pg["len"], native.ptr(pg["d_dA"]),
-                native.ptr(pg["d_ref"]), native.ptr(self.d_nihc), native.ptr(self.W),
-                float(self.Fs), self.jnd_win.delta_alpha_time_factor * self.Fs,
-                native.ptr(pg["d_FRA"]), native.ptr(pg["d_FAI"]), None, self._stream(stream)),
-                "cgb_jnd_dev")
+        """Fisher sums of every interval of every group in one launch."""
+        native.check(self.lib.cgb_jnd_batch_dev(
+            native.ptr(self.d_lam), self.lam_rows, native.ptr(self.d_jnd_iv), len(self.jnd_iv),
+            len(self.jnd_iv), native.ptr(self.d_nihc), native.ptr(self.W), float(self.Fs),
+            self.jnd_win.delta_alpha_time_factor * self.Fs, native.ptr(self.d_FRA),
+            native.ptr(self.d_FAI), None, self._stream(stream)), "cgb_jnd_batch_dev")
 
     def step(self, stream=None):
         self.generate_input(stream)
@@ -219,10 +224,12 @@ class BatchSweep:
     def jnd_db(self):
         """Per group: (rate dB, AI dB) of every interval (NaN on references)."""
         out = []
+        FRA_all = self.d_FRA.cpu().numpy()
+        FAI_all = self.d_FAI.cpu().numpy()
         for g, pg in zip(self.groups, self.per_group):
-            F_RA = pg["d_FRA"].cpu().numpy()
-            F_AI = pg["d_FAI"].cpu().numpy()
             n = pg["n"]
+            F_RA = np.ascontiguousarray(FRA_all[:, pg["out0"]:pg["out0"] + n])
+            F_AI = np.ascontiguousarray(FAI_all[:, pg["out0"]:pg["out0"] + n])
             rate, ai = np.zeros(n), np.zeros(n)
             ref = np.ascontiguousarray(g.ref_of, np.int32)
             native.check(self.lib.cgb_jnd_final(native.ptr(F_RA), native.ptr(F_AI), n,

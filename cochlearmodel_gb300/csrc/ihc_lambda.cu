@@ -7,6 +7,11 @@
 //   AC  = sum_{i<tu(t)} b_i v[t-i]          (AC low-pass, taps pre-scaled)
 //   dS  = (scale v - AC)^2
 //   DC  = sum_{i<tu(t)} d_i dS[t-i]         (DC moving average)
+//         with uniform taps d (the reference's DC filter): d * S(t), S the
+//         window sum, re-summed at every 32nd frame row (and where the
+//         look-back rule restarts the window) and otherwise updated by
+//         adding dS[t] and removing dS[t-tu]; all in compensated (TwoSum)
+//         arithmetic
 //   IHC = log10(max(10^ihc_s (eta_AC AC + eta_DC DC), 0) + 1e-20)
 //   lambda_j = s ? min(SAT, max(A_js IHC, spont_j)) : spont_j,  j = 0..2
 // in FP32, each FIR accumulated with a compensated dot product (Dot2).
@@ -53,6 +58,7 @@ struct IHCArgs {
   float* ihc;                  // [lam rows][256] or null
   int TR, xrows;               // output rows per tile, staged rows (multiple of 64)
   int32_t* status;
+  int dc_uniform;              // all DC taps equal: running window sum
 };
 
 __device__ __forceinline__ int taps_used(int k, const cgb_ihc_frame& f, int taps) {
@@ -110,6 +116,17 @@ __device__ __forceinline__ void fir_block8(const float* __restrict__ src,
 #pragma unroll
   for (int r = 0; r < kRB; ++r) out[r] = acc[r].result();
 }
+
+// s + c += x exactly (Knuth's TwoSum; the rounding error goes to c).
+__device__ __forceinline__ void two_sum_add(float& s, float& c, float x) {
+  const float t = __fadd_rn(s, x);
+  const float z = __fsub_rn(t, s);
+  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
+  s = t;
+  c = __fadd_rn(c, e);
+}
+
+constexpr int kDcAnchor = 32;  // DC window re-summed at frame rows k % 32 == 0
 
 __device__ __forceinline__ float fir_row(const float* __restrict__ src,
                                          const float* __restrict__ b, int tu) {
@@ -224,6 +241,48 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
   const float dmg = A.dmg[(size_t)f.ihc_profile * 256 + s];
   const float a0 = A.aihc[0 * 256 + s], a1 = A.aihc[1 * 256 + s], a2 = A.aihc[2 * 256 + s];
   const bool sec0 = s == 0;
+  auto emit = [&](int k, float dc) {
+    const float ac = ACb[(size_t)(k - row0) * kSecTile + lane];
+    const float pre = __fmaf_rn(ac, A.eta_ac, __fmul_rn(dc, A.eta_dc));
+    const float y = __fmul_rn(dmg, pre);
+    const float lg = own_log10f(__fadd_rn(fmaxf(y, 0.0f), 1e-20f));
+    const int64_t row = f.lam_row0 + k;
+    if (A.ihc) A.ihc[row * 256 + s] = lg;
+    const float l0 = sec0 ? A.spont0 : fminf(A.sat, fmaxf(__fmul_rn(a0, lg), A.spont0));
+    const float l1 = sec0 ? A.spont1 : fminf(A.sat, fmaxf(__fmul_rn(a1, lg), A.spont1));
+    const float l2 = sec0 ? A.spont2 : fminf(A.sat, fmaxf(__fmul_rn(a2, lg), A.spont2));
+    A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
+    A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
+    A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
+  };
+  if (A.dc_uniform) {
+    // tiles start on multiples of 32 rows, so every 32-row block opens on
+    // an anchor row
+    const float d = bdc[0];
+    const float* col = DS + lane;
+    for (int kb = row0 + warp * kDcAnchor; kb < k_hi; kb += kIhcWarps * kDcAnchor) {
+      const int ke = min(kb + kDcAnchor, k_hi);
+      float ws = 0.0f, wc = 0.0f;
+      int tu_prev = -1;
+      for (int k = kb; k < ke; ++k) {
+        const int tu = taps_used(k, f, A.n_dc);
+        if (k == kb || (tu != tu_prev && tu != tu_prev + 1)) {
+          ws = wc = 0.0f;
+          for (int j = 0; j < tu; ++j)
+            two_sum_add(ws, wc, col[(size_t)(k - j - dsbase) * kSecTile]);
+        } else {
+          two_sum_add(ws, wc, col[(size_t)(k - dsbase) * kSecTile]);
+          if (tu == tu_prev) two_sum_add(ws, wc, -col[(size_t)(k - tu - dsbase) * kSecTile]);
+        }
+        tu_prev = tu;
+        // d * (ws + wc), rounded once
+        const float p = __fmul_rn(d, ws);
+        const float q = __fmaf_rn(d, ws, -p);
+        emit(k, __fadd_rn(p, __fmaf_rn(d, wc, q)));
+      }
+    }
+    return;
+  }
   for (int kb = row0 + warp * kRB; kb < k_hi; kb += kIhcWarps * kRB) {
     const int nr = min(kRB, k_hi - kb);
     bool fast = nr == kRB;
@@ -240,23 +299,8 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
         acc[r] = r < nr ? fir_row(src + r * kSecTile, bdc, taps_used(kb + r, f, A.n_dc)) : 0.0f;
     }
 #pragma unroll
-    for (int r = 0; r < kRB; ++r) {
-      if (r < nr) {
-        const int k = kb + r;
-        const float ac = ACb[(size_t)(k - row0) * kSecTile + lane];
-        const float pre = __fmaf_rn(ac, A.eta_ac, __fmul_rn(acc[r], A.eta_dc));
-        const float y = __fmul_rn(dmg, pre);
-        const float lg = own_log10f(__fadd_rn(fmaxf(y, 0.0f), 1e-20f));
-        const int64_t row = f.lam_row0 + k;
-        if (A.ihc) A.ihc[row * 256 + s] = lg;
-        const float l0 = sec0 ? A.spont0 : fminf(A.sat, fmaxf(__fmul_rn(a0, lg), A.spont0));
-        const float l1 = sec0 ? A.spont1 : fminf(A.sat, fmaxf(__fmul_rn(a1, lg), A.spont1));
-        const float l2 = sec0 ? A.spont2 : fminf(A.sat, fmaxf(__fmul_rn(a2, lg), A.spont2));
-        A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
-        A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
-        A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
-      }
-    }
+    for (int r = 0; r < kRB; ++r)
+      if (r < nr) emit(kb + r, acc[r]);
   }
 }
 
@@ -316,11 +360,11 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   int max_tr = 384;
   // shrink the tile until the staged window fits 227 KB of shared memory
   int TR = max_tr, xrows = 0;
-  for (; TR >= 8; TR -= 8) {
+  for (; TR >= 32; TR -= 32) {  // multiples of 32: the DC anchor grid
     xrows = (TR + n_ac + n_dc - 1 + kBoxRows - 1) / kBoxRows * kBoxRows;
     if (smem_bytes(TR, xrows, n_ac, n_dc) <= 227 * 1024) break;
   }
-  if (TR < 8) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
+  if (TR < 32) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
   for (int i = 0; i < n_frames; ++i) {
     const cgb_ihc_frame& fr = frames[i];
     const bool ok = fr.v_row0 >= 0 && fr.lam_rows >= 0 && fr.lam_rows <= fr.rows &&
@@ -391,6 +435,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   A.TR = TR;
   A.xrows = xrows;
   A.status = d_status;
+  A.dc_uniform = 1;
+  for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
   const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
   CGB_TRY_CUDA(cudaFuncSetAttribute(ihc_lambda_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -516,11 +562,11 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   if (v_rows > INT32_MAX)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: more than 2^31-1 velocity rows");
   int TR = 384, xrows = 0;
-  for (; TR >= 8; TR -= 8) {
+  for (; TR >= 32; TR -= 32) {  // multiples of 32: the DC anchor grid
     xrows = (TR + n_ac + n_dc - 1 + kBoxRows - 1) / kBoxRows * kBoxRows;
     if (smem_bytes(TR, xrows, n_ac, n_dc) <= 227 * 1024) break;
   }
-  if (TR < 8)
+  if (TR < 32)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: filters too long for one tile");
   int32_t prefix[kNoAllocMaxFrames + 1];
   prefix[0] = 0;
@@ -588,6 +634,8 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   A.TR = TR;
   A.xrows = xrows;
   A.status = d_status;
+  A.dc_uniform = 1;
+  for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
   const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
   CGB_TRY_CUDA(cudaFuncSetAttribute(ihc_lambda_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),

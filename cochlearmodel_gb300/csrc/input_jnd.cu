@@ -40,28 +40,34 @@ __global__ void input_gen_kernel(const cgb_profile* __restrict__ prof, int n_pro
   }
 }
 
-constexpr int kJndThreads = 256;
-constexpr int kJndRows = 8;  // rows folded in FP32 before an FP64 add
+constexpr int kJndSections = 256;
+constexpr int kJndGroups = 4;   // row groups per CTA (threads = 4 x 256)
+constexpr int kJndThreads = kJndSections * kJndGroups;
+constexpr int kJndRows = 8;     // rows folded in FP32 before an FP64 add
 
-// One CTA per (interval i, lambda plane j), one thread per section.  Each
-// thread walks the interval's window and its reference interval's window
-// once: FP64 sums of lambda and lambda_ref (the two mean rates) and of
-// (lambda - lambda_ref)^2 / lambda_ref (the AI term); each term is formed in
-// FP32 and 8 rows are folded in FP32 before the FP64 add.  The 256 section
-// terms are then reduced in FP64.
-__global__ void __launch_bounds__(kJndThreads)
-    jnd_kernel(const float* __restrict__ lam, int64_t plane_rows, int interval_nodes, int head,
-               int len, const double* __restrict__ dA, const int32_t* __restrict__ ref_of,
-               const double* __restrict__ nihc, double w0, double w1, double w2, double Fs,
-               double T, double* __restrict__ F_RA, double* __restrict__ F_AI,
-               double* __restrict__ MR, int n_int) {
-  const int i = blockIdx.x, j = blockIdx.y, s = threadIdx.x;
-  const int r = ref_of[i];
-  const float* c = lam + ((int64_t)j * plane_rows + (int64_t)i * interval_nodes + head) * 256 + s;
-  const float* rf = lam + ((int64_t)j * plane_rows + (int64_t)r * interval_nodes + head) * 256 + s;
+// The Fisher sums of one (interval, lambda plane): thread (g, s) walks the
+// 8-row blocks b = g, g + 4, ... of the window of section s and of the same
+// rows of the reference window, accumulating in FP64 the sums of lambda and
+// lambda_ref (the two mean rates) and of (lambda - lambda_ref)^2 / lambda_ref
+// (the AI term); each term is formed in FP32 and 8 rows are folded in FP32
+// before the FP64 add.  Rows past the last full block are added one by one
+// by the group that owns the next block.  The four groups' sums are then
+// combined in group order and the 256 section terms reduced in FP64, so
+// the result does not depend on scheduling.
+__device__ __forceinline__ void jnd_interval(const float* __restrict__ lam, int64_t plane_rows,
+                                             int j, int64_t row, int64_t ref_row, int len,
+                                             double da, int out, int n_out,
+                                             const double* __restrict__ nihc, double w,
+                                             double Fs, double T, double* __restrict__ F_RA,
+                                             double* __restrict__ F_AI,
+                                             double* __restrict__ MR) {
+  const int s = threadIdx.x & (kJndSections - 1), g = threadIdx.x / kJndSections;
+  const float* c = lam + ((int64_t)j * plane_rows + row) * 256 + s;
+  const float* rf = lam + ((int64_t)j * plane_rows + ref_row) * 256 + s;
   double sum_c = 0.0, sum_r = 0.0, sum_ai = 0.0;
-  int t = 0;
-  for (; t + kJndRows <= len; t += kJndRows) {
+  const int nb = len / kJndRows;
+  for (int b = g; b < nb; b += kJndGroups) {
+    const int t = b * kJndRows;
     float pc = 0.0f, pr = 0.0f, pa = 0.0f;
 #pragma unroll
     for (int k = 0; k < kJndRows; ++k) {
@@ -76,46 +82,85 @@ __global__ void __launch_bounds__(kJndThreads)
     sum_r += (double)pr;
     sum_ai += (double)pa;
   }
-  for (; t < len; ++t) {
-    const float lc = c[(int64_t)t * 256];
-    const float lr = rf[(int64_t)t * 256];
-    const float d = __fsub_rn(lc, lr);
-    sum_c += (double)lc;
-    sum_r += (double)lr;
-    sum_ai += (double)__fmul_rn(__fmul_rn(d, d), own_rcpf(lr));
+  if (g == nb % kJndGroups) {
+    for (int t = nb * kJndRows; t < len; ++t) {
+      const float lc = c[(int64_t)t * 256];
+      const float lr = rf[(int64_t)t * 256];
+      const float d = __fsub_rn(lc, lr);
+      sum_c += (double)lc;
+      sum_r += (double)lr;
+      sum_ai += (double)__fmul_rn(__fmul_rn(d, d), own_rcpf(lr));
+    }
   }
-  const double da = dA[i];
-  const double mr = sum_c / len, mrr = sum_r / len;
-  if (MR) MR[((int64_t)j * n_int + i) * 256 + s] = mr;
-  const double tl = (double)len / Fs;
-  double rate = 0.0, ai = 0.0;
-  if (da > 0.0) {
-    const double dmr = (mr - mrr) / da;
-    rate = nihc[s] * T * dmr * dmr / mrr;
-    ai = nihc[s] * (T / tl) * sum_ai / (Fs * da * da);
-  }
-  // FP64 block reduction over the 256 sections
-  __shared__ double sh_r[kJndThreads / 32], sh_a[kJndThreads / 32];
+  __shared__ double sh[3][kJndGroups][kJndSections];
+  __shared__ double red[2][kJndSections / 32];
+  sh[0][g][s] = sum_c;
+  sh[1][g][s] = sum_r;
+  sh[2][g][s] = sum_ai;
+  __syncthreads();
+  if (g == 0) {
+    for (int k = 1; k < kJndGroups; ++k) {
+      sum_c += sh[0][k][s];
+      sum_r += sh[1][k][s];
+      sum_ai += sh[2][k][s];
+    }
+    const double mr = sum_c / len, mrr = sum_r / len;
+    if (MR) MR[((int64_t)j * n_out + out) * 256 + s] = mr;
+    const double tl = (double)len / Fs;
+    double rate = 0.0, ai = 0.0;
+    if (da > 0.0) {
+      const double dmr = (mr - mrr) / da;
+      rate = nihc[s] * T * dmr * dmr / mrr;
+      ai = nihc[s] * (T / tl) * sum_ai / (Fs * da * da);
+    }
 #pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    rate += __shfl_xor_sync(kFull, rate, o);
-    ai += __shfl_xor_sync(kFull, ai, o);
-  }
-  if ((s & 31) == 0) {
-    sh_r[s >> 5] = rate;
-    sh_a[s >> 5] = ai;
+    for (int o = 16; o >= 1; o >>= 1) {
+      rate += __shfl_xor_sync(kFull, rate, o);
+      ai += __shfl_xor_sync(kFull, ai, o);
+    }
+    if ((s & 31) == 0) {
+      red[0][s >> 5] = rate;
+      red[1][s >> 5] = ai;
+    }
   }
   __syncthreads();
-  if (s == 0) {
+  if (threadIdx.x == 0) {
     double tr = 0.0, ta = 0.0;
-    for (int k = 0; k < kJndThreads / 32; ++k) {
-      tr += sh_r[k];
-      ta += sh_a[k];
+    for (int k = 0; k < kJndSections / 32; ++k) {
+      tr += red[0][k];
+      ta += red[1][k];
     }
-    const double w = j == 0 ? w0 : (j == 1 ? w1 : w2);
-    F_RA[(int64_t)j * n_int + i] = tr * w;
-    F_AI[(int64_t)j * n_int + i] = ta * w;
+    F_RA[(int64_t)j * n_out + out] = tr * w;
+    F_AI[(int64_t)j * n_out + out] = ta * w;
   }
+}
+
+// Intervals of one run: interval i's window starts at row i * interval_nodes
+// + head, its reference's at ref_of[i] * interval_nodes + head.
+__global__ void __launch_bounds__(kJndThreads)
+    jnd_kernel(const float* __restrict__ lam, int64_t plane_rows, int interval_nodes, int head,
+               int len, const double* __restrict__ dA, const int32_t* __restrict__ ref_of,
+               const double* __restrict__ nihc, double w0, double w1, double w2, double Fs,
+               double T, double* __restrict__ F_RA, double* __restrict__ F_AI,
+               double* __restrict__ MR, int n_int) {
+  const int i = blockIdx.x, j = blockIdx.y;
+  jnd_interval(lam, plane_rows, j, (int64_t)i * interval_nodes + head,
+               (int64_t)ref_of[i] * interval_nodes + head, len, dA[i], i, n_int, nihc,
+               j == 0 ? w0 : (j == 1 ? w1 : w2), Fs, T, F_RA, F_AI, MR);
+}
+
+// Intervals of any number of runs (groups of signals of different lengths)
+// in one launch, from a descriptor table.
+__global__ void __launch_bounds__(kJndThreads)
+    jnd_batch_kernel(const float* __restrict__ lam, int64_t plane_rows,
+                     const cgb_jnd_interval* __restrict__ iv, int n_out,
+                     const double* __restrict__ nihc, double w0, double w1, double w2, double Fs,
+                     double T, double* __restrict__ F_RA, double* __restrict__ F_AI,
+                     double* __restrict__ MR) {
+  const cgb_jnd_interval d = iv[blockIdx.x];
+  const int j = blockIdx.y;
+  jnd_interval(lam, plane_rows, j, d.row, d.ref_row, d.len, d.dA, d.out, n_out, nihc,
+               j == 0 ? w0 : (j == 1 ? w1 : w2), Fs, T, F_RA, F_AI, MR);
 }
 
 }  // namespace
@@ -157,7 +202,7 @@ extern "C" int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, in
     return fail(CGB_ERR_ARG, "cgb_jnd_dev: bad arguments");
   if ((int64_t)n_int * interval_nodes > plane_rows || head + len > interval_nodes)
     return fail(CGB_ERR_RANGE, "cgb_jnd_dev: intervals reach outside the lambda planes");
-  if (n_int > 65535 * 32) return fail(CGB_ERR_RANGE, "cgb_jnd_dev: too many intervals");
+  if (n_int > 2147483647 / 2) return fail(CGB_ERR_RANGE, "cgb_jnd_dev: too many intervals");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const double T = delta_alpha_len_factor / Fs;
   dim3 grid((unsigned)n_int, 3);
@@ -165,6 +210,28 @@ extern "C" int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, in
                                            d_ref_of, d_nihc, (double)W[0], (double)W[1],
                                            (double)W[2], Fs, T, d_F_RA, d_F_AI, d_MR, n_int);
   CGB_TRY_CUDA(cudaGetLastError(), "jnd_kernel launch");
+  note_launch();
+  return CGB_OK;
+}
+
+extern "C" int cgb_jnd_batch_dev(const float* d_lam, int64_t plane_rows,
+                                 const cgb_jnd_interval* d_iv, int n_iv, int n_out,
+                                 const double* d_nihc, const float* W, double Fs,
+                                 double delta_alpha_len_factor, double* d_F_RA, double* d_F_AI,
+                                 double* d_MR, void* stream) {
+  using namespace cgb;
+  if (n_iv == 0) return CGB_OK;
+  if (!d_lam || !d_iv || !d_nihc || !W || !d_F_RA || !d_F_AI || n_iv < 0 || n_out <= 0 ||
+      plane_rows <= 0)
+    return fail(CGB_ERR_ARG, "cgb_jnd_batch_dev: bad arguments");
+  if (n_iv > 2147483647 / 2) return fail(CGB_ERR_RANGE, "cgb_jnd_batch_dev: too many intervals");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const double T = delta_alpha_len_factor / Fs;
+  dim3 grid((unsigned)n_iv, 3);
+  jnd_batch_kernel<<<grid, kJndThreads, 0, st>>>(d_lam, plane_rows, d_iv, n_out, d_nihc,
+                                                 (double)W[0], (double)W[1], (double)W[2], Fs, T,
+                                                 d_F_RA, d_F_AI, d_MR);
+  CGB_TRY_CUDA(cudaGetLastError(), "jnd_batch_kernel launch");
   note_launch();
   return CGB_OK;
 }

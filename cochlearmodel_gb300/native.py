@@ -71,6 +71,7 @@ _SIGS = {
     "cgb_noise_normalization": (_i, [_p, _i, _d, _d, _i, _i, _i, _i, C.c_float, _p, _p]),
     "cgb_jnd_dev": (_i, [_p, _i64, _i, _i, _i, _i, _p, _p, _p, _p, _d, _d, _p, _p, _p, _p]),
     "cgb_jnd_final": (_i, [_p, _p, _i, _p, _d, _d, _p, _p]),
+    "cgb_jnd_batch_dev": (_i, [_p, _i64, _p, _i, _i, _p, _p, _d, _d, _p, _p, _p, _p]),
     "cgb_ihc_lambda_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64, _p,
                                 _p, _i64, _p, _p]),
     "cgb_bm_launch_shape_count": (_i, []),
@@ -91,6 +92,11 @@ _SIGS = {
                              _p]),
     "cgb_ws_infer_dev": (_i, [_p, _p, _i, _p, _p]),
 }
+
+
+JND_INTERVAL_DTYPE = np.dtype([("row", np.int64), ("ref_row", np.int64), ("dA", np.float64),
+                               ("len", np.int32), ("out", np.int32)])
+assert JND_INTERVAL_DTYPE.itemsize == 32
 
 
 class BMExtras(C.Structure):

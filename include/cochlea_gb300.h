@@ -308,6 +308,25 @@ int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, int interval_
                 const float* W, double Fs, double delta_alpha_len_factor, double* d_F_RA,
                 double* d_F_AI, double* d_MR, void* stream);
 
+/* One interval of cgb_jnd_batch_dev (rows index each lambda plane). */
+typedef struct cgb_jnd_interval {
+  int64_t row;      /* first row of the interval's window                   */
+  int64_t ref_row;  /* first row of its reference interval's window         */
+  double dA;        /* tone amplitude; <= 0 gives zero Fisher terms         */
+  int32_t len;      /* window rows                                          */
+  int32_t out;      /* output slot in F_RA / F_AI / MR                      */
+} cgb_jnd_interval;
+
+/* cgb_jnd_dev over intervals of any number of runs (signal groups of
+ * different lengths) in one launch; d_iv is a device table of n_iv
+ * descriptors, outputs are double[3][n_out] (MR double[3][n_out][256]).
+ * Same arithmetic as cgb_jnd_dev.  No counterpart in the reference, which
+ * runs one interval length per call. */
+int cgb_jnd_batch_dev(const float* d_lam, int64_t plane_rows, const cgb_jnd_interval* d_iv,
+                      int n_iv, int n_out, const double* d_nihc, const float* W, double Fs,
+                      double delta_alpha_len_factor, double* d_F_RA, double* d_F_AI,
+                      double* d_MR, void* stream);
+
 /* Final JND in dB SPL per interval from the Fisher sums (host arrays):
  * 20 log10((1/sqrt(sum_j F_j)) / spl_ref), bounded at max_db; NaN for
  * reference intervals. */

@@ -715,10 +715,42 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
         dsf[(size_t)k * NS + s] = ms * ms;
       }
     }
+    // DC with uniform taps d: d * (window sum), the window re-summed at
+    // rows k % 32 == 0 and where the look-back rule restarts it, otherwise
+    // updated by +dS[k] (and -dS[k-tu] once full), in TwoSum arithmetic.
+    bool uniform = true;
+    for (int i = 1; i < n_dc; ++i) uniform = uniform && dt[i] == dt[0];
+    auto two_sum_add = [](float& ws, float& wc, float x) {
+      float t = ws + x;
+      float z = t - ws;
+      float e = (ws - (t - z)) + (x - z);
+      ws = t;
+      wc = wc + e;
+    };
+    std::vector<float> wsum(NS, 0.0f), wcomp(NS, 0.0f);
+    int tu_prev = -1;
     for (int k = 0; k < lam_rows; ++k) {
       int tu = fir_taps_used(k, seg, frdp, total, n_dc);
+      const bool anchor = k % 32 == 0 || (tu != tu_prev && tu != tu_prev + 1);
       for (int s = 0; s < NS; ++s) {
-        float acc = dot2(dt.data(), dsf.data() + (size_t)k * NS + s, tu);
+        float acc;
+        if (uniform) {
+          float& ws = wsum[s];
+          float& wc = wcomp[s];
+          if (anchor) {
+            ws = wc = 0.0f;
+            for (int j = 0; j < tu; ++j) two_sum_add(ws, wc, dsf[(size_t)(k - j) * NS + s]);
+          } else {
+            two_sum_add(ws, wc, dsf[(size_t)k * NS + s]);
+            if (tu == tu_prev) two_sum_add(ws, wc, -dsf[(size_t)(k - tu) * NS + s]);
+          }
+          const float d = dt[0];
+          const float p = d * ws;
+          const float q = fmaf(d, ws, -p);
+          acc = p + fmaf(d, wc, q);
+        } else {
+          acc = dot2(dt.data(), dsf.data() + (size_t)k * NS + s, tu);
+        }
         float pre = fmaf(acf[(size_t)k * NS + s], ea, acc * ed);
         float y = (float)ihc_damage[s] * pre;
         float lg = own_log10f(fmaxf(y, 0.0f) + 1e-20f);
@@ -729,6 +761,7 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
           lam[(size_t)j * lam_stride * NS + (size_t)k * NS + s] = val;
         }
       }
+      tu_prev = tu;
     }
     return;
   }

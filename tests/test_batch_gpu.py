@@ -56,7 +56,7 @@ def test_graph_replay_matches_eager(sweep):
     b, _ = sweep
     v0 = b.d_v.clone()
     lam0 = b.d_lam.clone()
-    F0 = [pg["d_FRA"].clone() for pg in b.per_group]
+    F0 = b.d_FRA.clone()
     b.d_v.zero_()
     b.d_lam.zero_()
     b.capture()
@@ -65,8 +65,7 @@ def test_graph_replay_matches_eager(sweep):
     b.replay()
     torch.cuda.synchronize()
     assert torch.equal(b.d_v, v0) and torch.equal(b.d_lam, lam0)
-    for f, pg in zip(F0, b.per_group):
-        assert torch.equal(f, pg["d_FRA"])
+    assert torch.equal(b.d_FRA, F0)
 
 
 def test_units_longest_first(sweep):

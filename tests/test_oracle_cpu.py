@@ -73,3 +73,29 @@ def test_threads_do_not_change_results(mv):
     a = orc.bm_run(secp, gamma, sc, units, x, rows, threads=1)[0]
     b = orc.bm_run(secp, gamma, sc, units, x, rows, threads=4)[0]
     assert np.array_equal(a, b)
+
+
+def test_ihc_kernel_arithmetic_within_lambda_bar():
+    """The GPU kernel's IHC/lambda arithmetic (oracle mode 2: Dot2 AC FIR,
+    running compensated DC window sum) against the reference's mixed
+    precision (mode 0): every lambda plane within 1e-4 max-rel, on a frame
+    whose look-back rule restarts the windows (seg 700, frdp 2)."""
+    from cochlearmodel_gb300 import ihc
+    rng = np.random.default_rng(7)
+    rows = 1600
+    t = np.arange(rows)[:, None] / 1e5
+    f = 200.0 * 40.0 ** (np.arange(256)[None, :] / 255.0)
+    env = np.exp(-np.arange(256) / 90.0)[None, :]
+    v = (1e-3 * env * np.sin(2 * np.pi * f * t) + 1e-6 * rng.normal(size=(rows, 256)))
+    v = v.astype(np.float32)
+    nerve = ihc.NerveConfig()
+    ac = ihc.design_ac_lowpass().astype(np.float64)
+    dc = np.full(200, np.float32(1.0 / (np.float32(100000) * np.float32(0.002))), np.float64)
+    dmg = np.full(256, 10.0 ** 8, np.float64)
+    args = (v, 700, 2, 1400, rows, ac, dc, nerve.scale, nerve.eta_AC, nerve.eta_DC, dmg,
+            nerve.aihc(), np.asarray(nerve.spontRate, np.float32), nerve.Lambda_SAT)
+    _, lam2 = orc.ihc_lambda(*args, mode=2)
+    _, lam0 = orc.ihc_lambda(*args, mode=0)
+    for j in range(3):
+        d = np.abs(lam2[j] - lam0[j]).max() / np.abs(lam0[j]).max()
+        assert d <= 1e-4, (j, d)
