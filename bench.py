@@ -12,6 +12,18 @@ Workloads (--workload):
   tone_sweep (configuration 2): 64 log-spaced tones 125 Hz-8 kHz x {20..100}
       dB SPL = 320 signals of 80 ms, Decouple_Filter 8 blocks of 10 ms; input,
       BM, IHC + lambda.
+  mixed_batch (configuration 5): 1,024 signals of lengths log-uniform
+      10 ms - 1 s, a seeded mix of tones, harmonic complexes and tones in
+      white noise, each with its own smooth random OHC (0-0.5) and IHC (5-8)
+      profile; BM, IHC + lambda and JND (tone in noise against the noise
+      alone, the others against silence) in one graph; the value counts the
+      1,024 test signals only.  Its e2e copies the input samples in and the
+      Fisher sums and failure flags out (the 120 GB of velocity and lambda
+      stay in HBM).
+
+--jacobi selects the pressure solve: reference (the reference's fixed
+20/2 sweep schedule, default), or the tolerance mode (|dp| <= 1e-6 |p|)
+started from the previous pressure, its extrapolation, or the learned guess.
 
 Every step recomputes everything from the profile table in HBM.  Reported
 beside the batched value: the same kernels run one signal at a time ("plain
@@ -47,8 +59,8 @@ UNIT = "audio-s/s"
 # ----------------------------------------------------------------------------
 # workloads
 # ----------------------------------------------------------------------------
-def make_workload(name, device, n_freq=64, n_seeds=4):
-    from cochlearmodel_gb300 import batch, model
+def make_workload(name, device, n_freq=64, n_seeds=4, n_signals=1024):
+    from cochlearmodel_gb300 import batch, mixed, model
     from cochlearmodel_gb300.pipeline import ProfileRun, ProfileSweep
     if name == "tone_sweep":
         cfg = model.RunConfig(Time_Block_Length=0.01, Decouple_Filter=8, Overlap_Time=0.005)
@@ -61,19 +73,40 @@ def make_workload(name, device, n_freq=64, n_seeds=4):
         run = batch.BatchSweep(device, batch.jnd_sweep_spec(n_seeds=n_seeds))
         run.kind = "jnd_sweep"
         return run
+    if name == "mixed_batch":
+        run = mixed.MixedBatch(device, mixed.mixed_batch_spec(n_signals=n_signals))
+        run.kind = "mixed_batch"
+        return run
     raise ValueError(name)
 
 
+JACOBI = {"reference": None, "previous": 0, "extrapolated": 1, "learned": 2}
+
+
+def set_jacobi(run, mode, device):
+    """Switches the workload's BM scalars to the chosen pressure solve."""
+    from cochlearmodel_gb300 import model
+    guess = JACOBI[mode]
+    if guess is None:
+        return None
+    run.sc = model.tolerance_mode(run.sc, guess=guess)
+    if guess == 2:
+        from cochlearmodel_gb300 import warmstart
+        run.net = warmstart.WarmStartNet.load(warmstart.WEIGHTS, device)
+        run.extras = run.net.extras()
+    return guess
+
+
 def stages(run):
-    s = [("input_gen", run.generate_input), ("bm_solver", run.solve_bm),
-         ("ihc_lambda", run.ihc_lambda)]
-    if run.kind == "jnd_sweep":
+    s = [] if run.kind == "mixed_batch" else [("input_gen", run.generate_input)]
+    s += [("bm_solver", run.solve_bm), ("ihc_lambda", run.ihc_lambda)]
+    if run.kind in ("jnd_sweep", "mixed_batch"):
         s.append(("jnd", run.jnd_sums))
     return s
 
 
 def n_signals(run):
-    return run.n_signals if run.kind == "jnd_sweep" else run.n_int
+    return run.n_signals if run.kind in ("jnd_sweep", "mixed_batch") else run.n_int
 
 
 # ----------------------------------------------------------------------------
@@ -277,6 +310,9 @@ def run_reference(args, rank, world):
     import torch
     if not torch.cuda.is_available():
         return {"impl": "reference", "unavailable": "needs the generated input of the sweep"}
+    if args.workload == "mixed_batch":
+        return {"impl": "reference", "unavailable": "the host-core arm times the default "
+                                                    "workload (jnd_sweep) and tone_sweep"}
     run = make_workload(args.workload, "cuda:0", args.n_freq, args.n_seeds)
     run.generate_input()
     torch.cuda.synchronize()
@@ -303,7 +339,8 @@ def run_ours(args, rank, world, device):
     import torch
     from cochlearmodel_gb300 import native
 
-    run = make_workload(args.workload, device, args.n_freq, args.n_seeds)
+    run = make_workload(args.workload, device, args.n_freq, args.n_seeds, args.n_signals)
+    set_jacobi(run, args.jacobi, device)
     native.check(native.load().cgb_bm_set_launch_shape(args.shape), "launch shape")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
@@ -355,12 +392,19 @@ def run_ours(args, rank, world, device):
         t_total = float(tt.item())
     value = run.audio_seconds * args.steps * world / t_total
 
-    # e2e: profile tables in from pinned host memory, the path, velocity and the
-    # three lambda planes back to pinned host memory, through the C ABI
-    tables = [pg["d_prof"] for pg in run.per_group] if run.kind == "jnd_sweep" else [run.d_prof]
-    h_tables = [t.cpu().pin_memory() for t in tables]
-    h_v = torch.empty(run.d_v.shape, dtype=torch.float32).pin_memory()
-    h_lam = torch.empty(run.d_lam.shape, dtype=torch.float32).pin_memory()
+    # e2e: inputs in from pinned host memory (profile tables, or the samples of
+    # the mixed batch), the path, results back to pinned host memory (velocity
+    # and the three lambda planes; for the mixed batch the Fisher sums and
+    # failure flags), through the C ABI
+    if run.kind == "mixed_batch":
+        tables, h_tables = [run.d_in], [run.h_in]
+        outs = [run.d_FRA, run.d_FAI, run.d_failed]
+    else:
+        tables = [pg["d_prof"] for pg in run.per_group] if run.kind == "jnd_sweep" \
+            else [run.d_prof]
+        h_tables = [t.cpu().pin_memory() for t in tables]
+        outs = [run.d_v, run.d_lam]
+    h_outs = [torch.empty(o.shape, dtype=o.dtype).pin_memory() for o in outs]
     e_steps = max(1, args.steps // 2)
     e_ms = 0.0
     for i in range(e_steps):
@@ -370,15 +414,16 @@ def run_ours(args, rank, world, device):
         for d_t, h_t in zip(tables, h_tables):
             d_t.copy_(h_t, non_blocking=True)
         run.step()
-        h_v.copy_(run.d_v, non_blocking=True)
-        h_lam.copy_(run.d_lam, non_blocking=True)
+        for h_o, d_o in zip(h_outs, outs):
+            h_o.copy_(d_o, non_blocking=True)
         b.record(stream)
         torch.cuda.synchronize(device)
         e_ms += a.elapsed_time(b)
         flush.fill_(float(i))
     e2e = run.audio_seconds * e_steps * world / (e_ms / 1000.0)
 
-    plain = plain_single_signal(run, device) if rank == 0 and not args.no_plain else None
+    plain = plain_single_signal(run, device) \
+        if rank == 0 and not args.no_plain and run.kind != "mixed_batch" else None
 
     peaks, peak_kind = measured_peaks()
     clock_mhz = peaks.get("sm_max_mhz", 2070.0)
@@ -394,13 +439,14 @@ def run_ours(args, rank, world, device):
                    "audio_s_per_step": run.audio_seconds, "fs": 100000,
                    "l2": "flushed between timed steps (256 MB write)",
                    "path": " -> ".join(nm for nm, _ in stages(run)),
-                   "bm_semantics": "reference (20/2 Jacobi sweeps)",
+                   "bm_semantics": "reference (20/2 Jacobi sweeps)" if args.jacobi == "reference"
+                   else f"tolerance mode 1e-6, {args.jacobi} guess",
                    "cuda_graph": use_graph, "launch_shape": args.shape,
                    "stage_ms": stage_ms},
         "gpu_launches": int(per_step_launches * args.steps),
         "e2e": {"value": e2e, "unit": UNIT,
-                "h2d_bytes_per_step": int(sum(t.numel() for t in h_tables)),
-                "d2h_bytes_per_step": int(h_v.numel() * 4 + h_lam.numel() * 4)},
+                "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_tables)),
+                "d2h_bytes_per_step": int(sum(o.numel() * o.element_size() for o in h_outs))},
         "roofline": {"bound": "fp32", "kernel": "bm_warp_kernel", "achieved": achieved,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "traffic": BM_TRAFFIC_PER_UNIT * len(run.units),
@@ -420,7 +466,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="jnd_sweep", choices=["jnd_sweep", "tone_sweep"])
+    ap.add_argument("--workload", default="jnd_sweep",
+                    choices=["jnd_sweep", "tone_sweep", "mixed_batch"])
+    ap.add_argument("--n-signals", type=int, default=1024, help="mixed_batch signals")
+    ap.add_argument("--jacobi", default="reference", choices=list(JACOBI),
+                    help="pressure solve: reference schedule or tolerance-mode guess")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -447,7 +497,7 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=device)
     line, run = run_ours(args, rank, world, device)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and run.kind != "mixed_batch":
         v, cores, sample = cpu_sample(run, target_s=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": sample}

@@ -156,6 +156,7 @@ class BatchSweep:
         self.d_FRA = torch.zeros((3, len(ivs)), dtype=torch.float64, device=d)
         self.d_FAI = torch.zeros((3, len(ivs)), dtype=torch.float64, device=d)
         self.graph = None
+        self.extras = None  # tolerance-mode extras (network weights), see solver.run_dev
 
     @property
     def n_signals(self) -> int:
@@ -179,7 +180,7 @@ class BatchSweep:
 
     def solve_bm(self, stream=None):
         self.bm.run_dev(self.sc, self.d_gamma, self.d_units, len(self.units), self.d_in,
-                        self.d_v, self.d_failed, self.d_stats, stream)
+                        self.d_v, self.d_failed, self.d_stats, stream, extras=self.extras)
 
     def ihc_lambda(self, stream=None):
         sc = self.ihc.scratch(len(self.frames))

@@ -462,8 +462,8 @@ constexpr int bm_dyn_smem() {
   return WARPS * 2 * 256 * 4 + (TOL == 2 ? ws::kBlobBytes + WARPS * ws::kWarpScratch : 0);
 }
 
-template <int WARPS, int MINB, bool PREV_SMEM, int TOL>
-__global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs A) {
+template <int WARPS, bool PREV_SMEM, int TOL>
+__device__ __forceinline__ void bm_body(const BMArgs& A) {
   __shared__ __align__(16) float s_par[8 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
   __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 7 * 256 : 4];
@@ -510,17 +510,22 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs 
   }
 }
 
-constexpr int kWarpsPerCta = 4;
+template <int WARPS, int MINB, bool PREV_SMEM, int TOL>
+__global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs A) {
+  bm_body<WARPS, PREV_SMEM, TOL>(A);
+}
 
 // Launch shapes built: (warps per CTA, minimum resident CTAs per SM the
 // register allocation is bounded for, previous-step state in shared
 // memory).  Shape 0: registers only, up to 255 per thread (2 CTAs of 4 warps
 // per SM); 1: bounded for 3 CTAs; 2, 3: the same with the previous-step
-// state in shared memory.
+// state in shared memory.  (Tighter register caps spill and measure
+// slower: 10 warps per SM at 200 registers 1.7x, 12 warps at 168 1.06x.)
 struct LaunchShape {
   const void* fn;
   void (*launch)(unsigned, cudaStream_t, const BMArgs&);
   int dyn_smem;
+  int warps;
 };
 
 template <int W, int M, bool PS, int TOL>
@@ -530,7 +535,7 @@ void launch_shape(unsigned grid, cudaStream_t st, const BMArgs& A) {
 
 #define CGB_SHAPE(W, M, PS, TOL)                                                  \
   {reinterpret_cast<const void*>(bm_warp_kernel<W, M, PS, TOL>), launch_shape<W, M, PS, TOL>, \
-   bm_dyn_smem<W, TOL>()}
+   bm_dyn_smem<W, TOL>(), W}
 
 const LaunchShape kShapes[] = {
     CGB_SHAPE(4, 1, false, 0),
@@ -659,10 +664,10 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
     }
   }
   CGB_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shape.fn,
-                                                             kWarpsPerCta * 32, shape.dyn_smem),
+                                                             shape.warps * 32, shape.dyn_smem),
                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
   if (per_sm < 1) per_sm = 1;
-  long long want = (n_units + kWarpsPerCta - 1) / kWarpsPerCta;
+  long long want = (n_units + shape.warps - 1) / shape.warps;
   long long grid = (long long)n_sm * per_sm;
   if (grid > want) grid = want;
   CGB_TRY_CUDA(cudaMemsetAsync(d_work, 0, sizeof(int32_t), st), "cudaMemsetAsync(work)");
