@@ -42,10 +42,11 @@ constexpr int kBoxRows = 64;   // rows per TMA box
 constexpr int kIhcWarps = 8;
 constexpr int kRB = 8;         // output rows per register block
 constexpr long long kWaitPolls = 1ll << 26;
+constexpr int kTilesPerRun = 8;  // consecutive tiles per CTA
 
 struct IHCArgs {
   const cgb_ihc_frame* frames;
-  const int32_t* tile_prefix;  // [n_frames + 1]
+  const int32_t* tile_prefix;  // [n_frames + 1] runs of tiles before each frame
   int n_frames;
   const float* taps;           // [n_ac] AC taps (x scale) then [n_dc] DC taps
   int n_ac, n_dc;
@@ -59,6 +60,7 @@ struct IHCArgs {
   int TR, xrows;               // output rows per tile, staged rows (multiple of 64)
   int32_t* status;
   int dc_uniform;              // all DC taps equal: running window sum
+  int run;                     // tiles per CTA (consecutive, one frame)
 };
 
 __device__ __forceinline__ int taps_used(int k, const cgb_ihc_frame& f, int taps) {
@@ -136,6 +138,49 @@ __device__ __forceinline__ float fir_row(const float* __restrict__ src,
   return acc.result();
 }
 
+// Stages velocity rows [y0, y0 + boxes * 64) of sections s0..s0+31 into X
+// (TMA, completion on mbar).  Called by one thread after a block barrier that
+// ends all reads of X; the proxy fence orders those generic-proxy reads
+// before the asynchronous writes.
+__device__ __forceinline__ void stage_rows(const CUtensorMap* vmap, float* X, uint64_t* mbar,
+                                           int boxes, int y0, int s0) {
+  const uint32_t bytes = (uint32_t)boxes * kBoxRows * kSecTile * 4;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
+               "r"(bytes)
+               : "memory");
+  for (int bxi = 0; bxi < boxes; ++bxi) {
+    const int y = y0 + bxi * kBoxRows;  // may be negative or past the end: zero fill
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(X + (size_t)bxi * kBoxRows * kSecTile)),
+        "l"(vmap), "r"(s0), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+  }
+}
+
+// Bounded wait on phase `parity` of mbar by every thread, then a block-wide
+// vote so that all threads take the same branch.
+__device__ __forceinline__ bool wait_stage(uint64_t* mbar, uint32_t parity) {
+  uint32_t done = 0;
+  long long polls = 0;
+  while (!done && polls < kWaitPolls) {
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity)
+        : "memory");
+    ++polls;
+  }
+  return __syncthreads_and(done) != 0;
+}
+
+// One CTA = 32 sections x a run of up to A.run consecutive tiles of TR rows
+// of one frame, processed in order.  The first tile of the run computes AC
+// and dS on the DC filter's look-back rows as well; later tiles inherit those
+// n_dc - 1 rows of dS from the previous tile (shifted down in shared memory)
+// and stage only the AC filter's look-back, the next tile's rows being copied
+// by TMA while the current tile's DC/IHC/lambda phase runs.
 __global__ void __launch_bounds__(kIhcWarps * 32)
     ihc_lambda_kernel(const __grid_constant__ CUtensorMap vmap, const IHCArgs A) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -147,7 +192,7 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
   uint64_t* mbar = reinterpret_cast<uint64_t*>(
       (reinterpret_cast<uintptr_t>(TP + A.n_ac + A.n_dc) + 15) & ~uintptr_t(15));
 
-  // locate the frame and the tile
+  // locate the frame and the run
   const int bx = blockIdx.x;
   int lo = 0, hi = A.n_frames;
   while (hi - lo > 1) {
@@ -155,13 +200,13 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
     if (A.tile_prefix[mid] <= bx) lo = mid; else hi = mid;
   }
   const cgb_ihc_frame f = A.frames[lo];
-  const int row0 = (bx - A.tile_prefix[lo]) * A.TR;
-  const int TRt = min(A.TR, f.lam_rows - row0);
+  const int tiles = (f.lam_rows + A.TR - 1) / A.TR;
+  const int t0 = (bx - A.tile_prefix[lo]) * A.run;
+  const int t1 = min(t0 + A.run, tiles);
   const int s0 = blockIdx.y * kSecTile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // staged rows start one row below the oldest row any filter reads
-  const int xbase = row0 - A.n_ac - A.n_dc + 1;
-  const int dsbase = row0 - A.n_dc;
+  const int boxes_first = A.xrows / kBoxRows;
+  const int boxes_next = (A.TR + A.n_ac - 1 + kBoxRows - 1) / kBoxRows;
 
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
@@ -170,137 +215,132 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
   }
   for (int i = threadIdx.x; i < A.n_ac + A.n_dc; i += blockDim.x) TP[i] = A.taps[i];
   __syncthreads();
-  const int boxes = A.xrows / kBoxRows;
-  if (threadIdx.x == 0) {
-    const uint32_t bytes = (uint32_t)boxes * kBoxRows * kSecTile * 4;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
-                 "r"(bytes)
-                 : "memory");
-    for (int bxi = 0; bxi < boxes; ++bxi) {
-      const int y = (int)f.v_row0 + xbase + bxi * kBoxRows;  // may be negative: zero fill
-      asm volatile(
-          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-          " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(X + (size_t)bxi * kBoxRows * kSecTile)),
-          "l"(&vmap), "r"(s0), "r"(y), "r"(smem_u32(mbar))
-          : "memory");
-    }
-  }
-  // bounded wait on the TMA transaction
-  {
-    uint32_t done = 0;
-    long long polls = 0;
-    while (!done && polls < kWaitPolls) {
-      asm volatile(
-          "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-          : "=r"(done)
-          : "r"(smem_u32(mbar))
-          : "memory");
-      ++polls;
-    }
-    if (!done) {
-      if (threadIdx.x == 0) atomicOr(A.status, 1);
-      return;
-    }
-  }
+  // staged rows of the first tile start one row below the oldest row either
+  // filter reads; those of later tiles below the oldest row the AC filter reads
+  if (threadIdx.x == 0)
+    stage_rows(&vmap, X, mbar, boxes_first, (int)f.v_row0 + t0 * A.TR - A.n_ac - A.n_dc + 1, s0);
 
   const float* bac = TP;
   const float* bdc = TP + A.n_ac;
   const float scale = A.scale;
-
-  // phase 1: AC and dS on rows [max(0, row0 - n_dc + 1), row0 + TRt)
-  const int k_lo = max(0, row0 - A.n_dc + 1), k_hi = row0 + TRt;
-  for (int kb = k_lo + warp * kRB; kb < k_hi; kb += kIhcWarps * kRB) {
-    const int nr = min(kRB, k_hi - kb);
-    bool fast = nr == kRB;
-#pragma unroll
-    for (int r = 0; r < kRB; ++r)
-      fast = fast && taps_used(kb + r, f, A.n_ac) == A.n_ac;
-    float acc[kRB];
-    const float* src = X + (size_t)(kb - xbase) * kSecTile + lane;
-    if (fast) {
-      fir_block8(src, bac, A.n_ac, acc);
-    } else {
-#pragma unroll
-      for (int r = 0; r < kRB; ++r)
-        acc[r] = r < nr ? fir_row(src + r * kSecTile, bac, taps_used(kb + r, f, A.n_ac)) : 0.0f;
-    }
-#pragma unroll
-    for (int r = 0; r < kRB; ++r) {
-      if (r < nr) {
-        const int k = kb + r;
-        const float ms = __fmaf_rn(src[r * kSecTile], scale, -acc[r]);
-        DS[(size_t)(k - dsbase) * kSecTile + lane] = __fmul_rn(ms, ms);
-        if (k >= row0) ACb[(size_t)(k - row0) * kSecTile + lane] = acc[r];
-      }
-    }
-  }
-  __syncthreads();
-
-  // phase 2: DC, IHC and lambda on rows [row0, row0 + TRt)
   const int s = s0 + lane;
   const float dmg = A.dmg[(size_t)f.ihc_profile * 256 + s];
   const float a0 = A.aihc[0 * 256 + s], a1 = A.aihc[1 * 256 + s], a2 = A.aihc[2 * 256 + s];
   const bool sec0 = s == 0;
-  auto emit = [&](int k, float dc) {
-    const float ac = ACb[(size_t)(k - row0) * kSecTile + lane];
-    const float pre = __fmaf_rn(ac, A.eta_ac, __fmul_rn(dc, A.eta_dc));
-    const float y = __fmul_rn(dmg, pre);
-    const float lg = own_log10f(__fadd_rn(fmaxf(y, 0.0f), 1e-20f));
-    const int64_t row = f.lam_row0 + k;
-    if (A.ihc) A.ihc[row * 256 + s] = lg;
-    const float l0 = sec0 ? A.spont0 : fminf(A.sat, fmaxf(__fmul_rn(a0, lg), A.spont0));
-    const float l1 = sec0 ? A.spont1 : fminf(A.sat, fmaxf(__fmul_rn(a1, lg), A.spont1));
-    const float l2 = sec0 ? A.spont2 : fminf(A.sat, fmaxf(__fmul_rn(a2, lg), A.spont2));
-    A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
-    A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
-    A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
-  };
-  if (A.dc_uniform) {
-    // tiles start on multiples of 32 rows, so every 32-row block opens on
-    // an anchor row
-    const float d = bdc[0];
-    const float* col = DS + lane;
-    for (int kb = row0 + warp * kDcAnchor; kb < k_hi; kb += kIhcWarps * kDcAnchor) {
-      const int ke = min(kb + kDcAnchor, k_hi);
-      float ws = 0.0f, wc = 0.0f;
-      int tu_prev = -1;
-      for (int k = kb; k < ke; ++k) {
-        const int tu = taps_used(k, f, A.n_dc);
-        if (k == kb || (tu != tu_prev && tu != tu_prev + 1)) {
-          ws = wc = 0.0f;
-          for (int j = 0; j < tu; ++j)
-            two_sum_add(ws, wc, col[(size_t)(k - j - dsbase) * kSecTile]);
-        } else {
-          two_sum_add(ws, wc, col[(size_t)(k - dsbase) * kSecTile]);
-          if (tu == tu_prev) two_sum_add(ws, wc, -col[(size_t)(k - tu - dsbase) * kSecTile]);
-        }
-        tu_prev = tu;
-        // d * (ws + wc), rounded once
-        const float p = __fmul_rn(d, ws);
-        const float q = __fmaf_rn(d, ws, -p);
-        emit(k, __fadd_rn(p, __fmaf_rn(d, wc, q)));
-      }
+
+  for (int t = t0; t < t1; ++t) {
+    const bool first = t == t0;
+    const int row0 = t * A.TR;
+    const int TRt = min(A.TR, f.lam_rows - row0);
+    const int xbase = first ? row0 - A.n_ac - A.n_dc + 1 : row0 - A.n_ac + 1;
+    const int dsbase = row0 - A.n_dc;
+    if (!wait_stage(mbar, (uint32_t)((t - t0) & 1))) {
+      if (threadIdx.x == 0) atomicOr(A.status, 1);
+      return;
     }
-    return;
-  }
-  for (int kb = row0 + warp * kRB; kb < k_hi; kb += kIhcWarps * kRB) {
-    const int nr = min(kRB, k_hi - kb);
-    bool fast = nr == kRB;
-#pragma unroll
-    for (int r = 0; r < kRB; ++r)
-      fast = fast && taps_used(kb + r, f, A.n_dc) == A.n_dc;
-    float acc[kRB];
-    const float* src = DS + (size_t)(kb - dsbase) * kSecTile + lane;
-    if (fast) {
-      fir_block8(src, bdc, A.n_dc, acc);
-    } else {
+    if (!first) {
+      // dS of rows row0 - n_dc + 1 .. row0 - 1 from the previous tile's buffer
+      for (int i = 1 + warp; i < A.n_dc; i += kIhcWarps)
+        DS[(size_t)i * kSecTile + lane] = DS[(size_t)(i + A.TR) * kSecTile + lane];
+      __syncthreads();
+    }
+
+    // phase 1: AC and dS on rows [k_lo, row0 + TRt)
+    const int k_lo = first ? max(0, row0 - A.n_dc + 1) : row0, k_hi = row0 + TRt;
+    for (int kb = k_lo + warp * kRB; kb < k_hi; kb += kIhcWarps * kRB) {
+      const int nr = min(kRB, k_hi - kb);
+      bool fast = nr == kRB;
 #pragma unroll
       for (int r = 0; r < kRB; ++r)
-        acc[r] = r < nr ? fir_row(src + r * kSecTile, bdc, taps_used(kb + r, f, A.n_dc)) : 0.0f;
-    }
+        fast = fast && taps_used(kb + r, f, A.n_ac) == A.n_ac;
+      float acc[kRB];
+      const float* src = X + (size_t)(kb - xbase) * kSecTile + lane;
+      if (fast) {
+        fir_block8(src, bac, A.n_ac, acc);
+      } else {
 #pragma unroll
-    for (int r = 0; r < kRB; ++r)
-      if (r < nr) emit(kb + r, acc[r]);
+        for (int r = 0; r < kRB; ++r)
+          acc[r] = r < nr ? fir_row(src + r * kSecTile, bac, taps_used(kb + r, f, A.n_ac)) : 0.0f;
+      }
+#pragma unroll
+      for (int r = 0; r < kRB; ++r) {
+        if (r < nr) {
+          const int k = kb + r;
+          const float ms = __fmaf_rn(src[r * kSecTile], scale, -acc[r]);
+          DS[(size_t)(k - dsbase) * kSecTile + lane] = __fmul_rn(ms, ms);
+          if (k >= row0) ACb[(size_t)(k - row0) * kSecTile + lane] = acc[r];
+        }
+      }
+    }
+    __syncthreads();
+    // X is free: stage the next tile while this one finishes
+    if (threadIdx.x == 0 && t + 1 < t1)
+      stage_rows(&vmap, X, mbar, boxes_next, (int)f.v_row0 + (t + 1) * A.TR - A.n_ac + 1, s0);
+
+    // phase 2: DC, IHC and lambda on rows [row0, row0 + TRt)
+    auto emit = [&](int k, float dc) {
+      const float ac = ACb[(size_t)(k - row0) * kSecTile + lane];
+      const float pre = __fmaf_rn(ac, A.eta_ac, __fmul_rn(dc, A.eta_dc));
+      const float y = __fmul_rn(dmg, pre);
+      const float lg = own_log10f(__fadd_rn(fmaxf(y, 0.0f), 1e-20f));
+      const int64_t row = f.lam_row0 + k;
+      if (A.ihc) A.ihc[row * 256 + s] = lg;
+      const float l0 = sec0 ? A.spont0 : fminf(A.sat, fmaxf(__fmul_rn(a0, lg), A.spont0));
+      const float l1 = sec0 ? A.spont1 : fminf(A.sat, fmaxf(__fmul_rn(a1, lg), A.spont1));
+      const float l2 = sec0 ? A.spont2 : fminf(A.sat, fmaxf(__fmul_rn(a2, lg), A.spont2));
+      A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
+      A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
+      A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
+    };
+    if (A.dc_uniform) {
+      // tiles start on multiples of 32 rows, so every 32-row block opens on
+      // an anchor row
+      const float d = bdc[0];
+      const float* col = DS + lane;
+      for (int kb = row0 + warp * kDcAnchor; kb < k_hi; kb += kIhcWarps * kDcAnchor) {
+        const int ke = min(kb + kDcAnchor, k_hi);
+        float ws = 0.0f, wc = 0.0f;
+        int tu_prev = -1;
+        for (int k = kb; k < ke; ++k) {
+          const int tu = taps_used(k, f, A.n_dc);
+          if (k == kb || (tu != tu_prev && tu != tu_prev + 1)) {
+            ws = wc = 0.0f;
+            for (int j = 0; j < tu; ++j)
+              two_sum_add(ws, wc, col[(size_t)(k - j - dsbase) * kSecTile]);
+          } else {
+            two_sum_add(ws, wc, col[(size_t)(k - dsbase) * kSecTile]);
+            if (tu == tu_prev) two_sum_add(ws, wc, -col[(size_t)(k - tu - dsbase) * kSecTile]);
+          }
+          tu_prev = tu;
+          // d * (ws + wc), rounded once
+          const float p = __fmul_rn(d, ws);
+          const float q = __fmaf_rn(d, ws, -p);
+          emit(k, __fadd_rn(p, __fmaf_rn(d, wc, q)));
+        }
+      }
+    } else {
+      for (int kb = row0 + warp * kRB; kb < k_hi; kb += kIhcWarps * kRB) {
+        const int nr = min(kRB, k_hi - kb);
+        bool fast = nr == kRB;
+#pragma unroll
+        for (int r = 0; r < kRB; ++r)
+          fast = fast && taps_used(kb + r, f, A.n_dc) == A.n_dc;
+        float acc[kRB];
+        const float* src = DS + (size_t)(kb - dsbase) * kSecTile + lane;
+        if (fast) {
+          fir_block8(src, bdc, A.n_dc, acc);
+        } else {
+#pragma unroll
+          for (int r = 0; r < kRB; ++r)
+            acc[r] = r < nr ? fir_row(src + r * kSecTile, bdc, taps_used(kb + r, f, A.n_dc))
+                            : 0.0f;
+        }
+#pragma unroll
+        for (int r = 0; r < kRB; ++r)
+          if (r < nr) emit(kb + r, acc[r]);
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -365,6 +405,9 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
     if (smem_bytes(TR, xrows, n_ac, n_dc) <= 227 * 1024) break;
   }
   if (TR < 32) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
+  // runs of tiles inherit the DC look-back rows from the tile before, an
+  // in-place shift that needs TR >= n_dc
+  const int run = TR >= n_dc ? kTilesPerRun : 1;
   for (int i = 0; i < n_frames; ++i) {
     const cgb_ihc_frame& fr = frames[i];
     const bool ok = fr.v_row0 >= 0 && fr.lam_rows >= 0 && fr.lam_rows <= fr.rows &&
@@ -374,7 +417,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
     if (!ok)
       return fail(CGB_ERR_RANGE,
                   "cgb_ihc_lambda_dev: frame " + std::to_string(i) + " out of range");
-    prefix[i + 1] = prefix[i] + (fr.lam_rows + TR - 1) / TR;
+    const int tiles = (fr.lam_rows + TR - 1) / TR;
+    prefix[i + 1] = prefix[i] + (tiles + run - 1) / run;
   }
   const int n_tiles = prefix[n_frames];
   if (n_tiles == 0) return CGB_OK;
@@ -435,6 +479,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   A.TR = TR;
   A.xrows = xrows;
   A.status = d_status;
+  A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
   const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
@@ -568,6 +613,7 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   }
   if (TR < 32)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: filters too long for one tile");
+  const int run = TR >= n_dc ? kTilesPerRun : 1;
   int32_t prefix[kNoAllocMaxFrames + 1];
   prefix[0] = 0;
   for (int i = 0; i < n_frames; ++i) {
@@ -579,7 +625,8 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
     if (!ok)
       return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: frame " + std::to_string(i) +
                                      " out of range");
-    prefix[i + 1] = prefix[i] + (fr.lam_rows + TR - 1) / TR;
+    const int tiles = (fr.lam_rows + TR - 1) / TR;
+    prefix[i + 1] = prefix[i] + (tiles + run - 1) / run;
   }
   const int n_tiles = prefix[n_frames];
   if (n_tiles == 0) return CGB_OK;
@@ -634,6 +681,7 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   A.TR = TR;
   A.xrows = xrows;
   A.status = d_status;
+  A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
   const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
