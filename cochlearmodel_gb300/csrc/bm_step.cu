@@ -57,11 +57,6 @@ struct BMArgs {
   int* log_count;
 };
 
-__device__ __forceinline__ float pair_sum8(const float (&t)[kSPL]) {
-  return __fadd_rn(__fadd_rn(__fadd_rn(t[0], t[1]), __fadd_rn(t[2], t[3])),
-                   __fadd_rn(__fadd_rn(t[4], t[5]), __fadd_rn(t[6], t[7])));
-}
-
 __device__ __forceinline__ void load8(const float* p, float (&r)[kSPL]) {
   const float4 a = reinterpret_cast<const float4*>(p)[0];
   const float4 b = reinterpret_cast<const float4*>(p)[1];
@@ -74,44 +69,79 @@ __device__ __forceinline__ void store8(float* p, const float (&r)[kSPL]) {
   reinterpret_cast<float4*>(p)[1] = make_float4(r[4], r[5], r[6], r[7]);
 }
 
+// Sections of a lane as four pairs: pair j holds sections 8l+j (x) and
+// 8l+j+4 (y).  With this pairing the Jacobi neighbours of a pair are whole
+// pairs (pair j-1 and j+1), so a sweep is four two-wide adds and four
+// two-wide fmas; only the two edge pairs are assembled from the halo.
+__device__ __forceinline__ void load8p(const float* p, float2 (&r)[4]) {
+  const float4 a = reinterpret_cast<const float4*>(p)[0];
+  const float4 b = reinterpret_cast<const float4*>(p)[1];
+  r[0] = f2(a.x, b.x);
+  r[1] = f2(a.y, b.y);
+  r[2] = f2(a.z, b.z);
+  r[3] = f2(a.w, b.w);
+}
+
+__device__ __forceinline__ void store8p(float* p, const float2 (&r)[4]) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(r[0].x, r[1].x, r[2].x, r[3].x);
+  reinterpret_cast<float4*>(p)[1] = make_float4(r[0].y, r[1].y, r[2].y, r[3].y);
+}
+
+// pairs -> sections 8l..8l+7 in order
+__device__ __forceinline__ void unpair(const float2 (&r)[4], float (&o)[kSPL]) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    o[j] = r[j].x;
+    o[j + 4] = r[j].y;
+  }
+}
+
+// ((t0 + t1) + (t2 + t3)) + ((t4 + t5) + (t6 + t7)) on the pair layout
+__device__ __forceinline__ float pair_sum8p(const float2 (&t)[4]) {
+  const float2 s = add2(add2(t[0], t[1]), add2(t[2], t[3]));
+  return __fadd_rn(s.x, s.y);
+}
+
 // The previous-step state (x, v, a, y, u, psi, psi') of a unit lives either
 // in registers or, with PREV_SMEM, in the warp's slice of shared memory
 // (7 x 256 floats), which frees 56 registers per thread at the cost of
 // reloading it on every outer iteration.
 template <bool PREV_SMEM>
 struct PrevState {
-  float r[7][kSPL];
+  float2 r[7][4];
   float* sm;  // [7][256] slice of this warp (PREV_SMEM only)
   __device__ __forceinline__ void init(float* slice, int base) {
     sm = slice;
 #pragma unroll
     for (int j = 0; j < 7; ++j)
 #pragma unroll
-      for (int k = 0; k < kSPL; ++k) r[j][k] = 0.0f;
+      for (int k = 0; k < 4; ++k) r[j][k] = f2b(0.0f);
     if (PREV_SMEM)
 #pragma unroll
-      for (int j = 0; j < 7; ++j) store8(sm + j * 256 + base, r[j]);
+      for (int j = 0; j < 7; ++j) store8p(sm + j * 256 + base, r[j]);
   }
-  __device__ __forceinline__ void load(int j, int base, float (&o)[kSPL]) const {
+  __device__ __forceinline__ void load(int j, int base, float2 (&o)[4]) const {
     if (PREV_SMEM) {
-      load8(sm + j * 256 + base, o);
+      load8p(sm + j * 256 + base, o);
     } else {
 #pragma unroll
-      for (int k = 0; k < kSPL; ++k) o[k] = r[j][k];
+      for (int k = 0; k < 4; ++k) o[k] = r[j][k];
     }
   }
-  __device__ __forceinline__ void store(int j, int base, const float (&o)[kSPL]) {
+  __device__ __forceinline__ void store(int j, int base, const float2 (&o)[4]) {
     if (PREV_SMEM) {
-      store8(sm + j * 256 + base, o);
+      store8p(sm + j * 256 + base, o);
     } else {
 #pragma unroll
-      for (int k = 0; k < kSPL; ++k) r[j][k] = o[k];
+      for (int k = 0; k < 4; ++k) r[j][k] = o[k];
     }
   }
 };
 
 // One unit, executed by one full warp.  sp: shared [8][256] section
 // parameters; sg / sgs: shared gamma and gamma*S_ohc of the unit's profile.
+// The per-section arithmetic runs on section pairs (two-wide FP32), each
+// element rounding as the scalar sequence the CPU oracle evaluates.
 //
 // TOL 0: fixed sweep counts (the reference schedule).  TOL 1: tolerance
 // mode; each solve sweeps in pairs until max|p2 - p1| <= jtol * max|p2|
@@ -130,20 +160,20 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
                                          const unsigned char* wblob, int lane,
                                          cgb_unit_stats* st) {
   const int base = lane * kSPL;
-  float rm[kSPL];
-  load8(sp + 1 * 256 + base, rm);
+  float2 rm[4];
+  load8p(sp + 1 * 256 + base, rm);
   // 1/m of the halo sections 8l-1 and 8l+8 (used by the paired sweeps)
-  const float rmL = __shfl_up_sync(kFull, rm[kSPL - 1], 1);
-  const float rmR = __shfl_down_sync(kFull, rm[0], 1);
+  const float rmL = __shfl_up_sync(kFull, rm[3].y, 1);
+  const float rmR = __shfl_down_sync(kFull, rm[0].x, 1);
 
   PrevState<PREV_SMEM> prev;
   prev.init(prev_slice, base);
-  float x[kSPL], v[kSPL], a[kSPL], y[kSPL], u[kSPL], ps[kSPL], dp[kSPL];
-  float Ptm[kSPL], p[kSPL], G[kSPL], Yrm[kSPL];
+  float2 x[4], v[4], a[4], y[4], u[4], ps[4], dp[4];
+  float2 Ptm[4], p[4], G[4], Yrm[4];
 #pragma unroll
-  for (int k = 0; k < kSPL; ++k) {
-    x[k] = v[k] = a[k] = y[k] = u[k] = ps[k] = dp[k] = 0.0f;
-    Ptm[k] = p[k] = G[k] = Yrm[k] = 0.0f;
+  for (int k = 0; k < 4; ++k) {
+    x[k] = v[k] = a[k] = y[k] = u[k] = ps[k] = dp[k] = f2b(0.0f);
+    Ptm[k] = p[k] = G[k] = Yrm[k] = f2b(0.0f);
   }
   float w0 = 0.f, wd0 = 0.f, wdd0 = 0.f, w = 0.f, wd = 0.f, wdd = 0.f;
 
@@ -162,6 +192,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   int n_failed = 0, n_written = 0, status = 0, sub_in_sample = 0;
   float smp_dt = 0.0f, smp_sub = 0.0f, smp_it = 0.0f;  // per-sample sums
   float dt_prev = dt, rho = 1.0f;
+  const bool first = lane == 0, last = lane == 31;
 
   while (n < un.end) {
     if (++sub_in_sample > A.max_sub) {  // dt collapsed: stop this unit, flag it
@@ -174,16 +205,17 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // of this step, the other slot holds the start of the previous one
       rho = __fdiv_rn(dt, dt_prev);
       dt_prev = dt;
-      store8(hist + (n_sub & 1) * 256 + base, p);
+      store8p(hist + (n_sub & 1) * 256 + base, p);
     }
     const float delta = (float)(tau * A.invts);
     const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
+    const float2 dt2 = f2b(dt), half = f2b(0.5f);
     do {
       // Predictor.  The first iteration of a step (or one after a reset) is
       // Euler, which is the trapezoid rule with the new-derivative slots
       // holding the previous derivatives: (d0 + d0) * 0.5 == d0 exactly, so
       // one code path serves both.
-      float x0[kSPL], v0[kSPL], a0[kSPL], y0[kSPL], u0[kSPL], ps0[kSPL], dp0[kSPL];
+      float2 x0[4], v0[4], a0[4], y0[4], u0[4], ps0[4], dp0[4];
       prev.load(0, base, x0);
       prev.load(1, base, v0);
       prev.load(2, base, a0);
@@ -194,7 +226,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       if (out_loop == 0 || reset) {
         out_loop = 0;
 #pragma unroll
-        for (int k = 0; k < kSPL; ++k) {
+        for (int k = 0; k < 4; ++k) {
           a[k] = a0[k];
           u[k] = u0[k];
           dp[k] = dp0[k];
@@ -202,51 +234,64 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         wd = wd0;
         wdd = wdd0;
       }
-      float dv[kSPL], fl[kSPL];
+      float2 dv[4], fl[4];
+      const float2 mtt2 = f2b(mtt);
 #pragma unroll
-      for (int k = 0; k < kSPL; ++k) {
-        const float vn = __fmaf_rn(__fmul_rn(__fadd_rn(a0[k], a[k]), 0.5f), dt, v0[k]);
-        dv[k] = fabsf(__fsub_rn(vn, v[k]));
-        fl[k] = __fsub_rn(dv[k], fmaxf(mtt, __fmul_rn(vn, dt)));
+      for (int k = 0; k < 4; ++k) {
+        const float2 vn = fma2(mul2(add2(a0[k], a[k]), half), dt2, v0[k]);
+        dv[k] = abs2(sub2(vn, v[k]));
+        fl[k] = sub2(dv[k], max2(mtt2, mul2(vn, dt2)));
         v[k] = vn;
-        x[k] = __fmaf_rn(__fmul_rn(__fadd_rn(v0[k], vn), 0.5f), dt, x0[k]);
-        y[k] = __fmaf_rn(__fmul_rn(__fadd_rn(u0[k], u[k]), 0.5f), dt, y0[k]);
-        ps[k] = __fmaf_rn(__fmul_rn(__fadd_rn(dp0[k], dp[k]), 0.5f), dt, ps0[k]);
+        x[k] = fma2(mul2(add2(v0[k], vn), half), dt2, x0[k]);
+        y[k] = fma2(mul2(add2(u0[k], u[k]), half), dt2, y0[k]);
+        ps[k] = fma2(mul2(add2(dp0[k], dp[k]), half), dt2, ps0[k]);
       }
       w = __fmaf_rn(__fmul_rn(__fadd_rn(wd0, wd), 0.5f), dt, w0);
       wd = __fmaf_rn(__fmul_rn(__fadd_rn(wdd0, wdd), 0.5f), dt, wd0);
-      const float evp = pair_sum8(dv), fp = pair_sum8(fl);
+      const float evp = pair_sum8p(dv), fp = pair_sum8p(fl);
 
       // OHC / TM coupling, G and the right-hand side Y (scaled by 1/m).
       const bool tm_update = out_loop < 2;
-#pragma unroll
-      for (int k = 0; k < kSPL; ++k) {
-        const int s = base + k;
-        const float d = __fsub_rn(y[k], x[k]);
-        const float Pohc = __fmul_rn(sgs[s], d);
-        const float Stm = sp[6 * 256 + s], Rtm = sp[7 * 256 + s];
+      {
+        float2 Stm[4], Rtm[4], gs[4], Rs[4], Ss[4], Qs[4];
+        load8p(sp + 6 * 256 + base, Stm);
+        load8p(sp + 7 * 256 + base, Rtm);
+        load8p(sgs + base, gs);
+        load8p(sp + 2 * 256 + base, Rs);
+        load8p(sp + 3 * 256 + base, Ss);
+        load8p(sp + 4 * 256 + base, Qs);
         if (tm_update) {
-          const float gm = sg[s];
-          const float t = own_tanhf(__fmul_rn(A.ratio, ps[k]));
-          const float dL = __fmul_rn(A.nas, t);
-          const float Aa = __fmul_rn(A.al, __fmaf_rn(t, t, -1.0f));
-          const float N1 = __fmaf_rn(A.e1, d, __fmaf_rn(A.e2, v[k], __fmul_rn(A.nw, ps[k])));
-          const float N = __fmaf_rn(Stm, dL, __fmul_rn(__fmul_rn(N1, Rtm), Aa));
-          const float Pp = __fmaf_rn(Stm, y[k], Pohc);
-          const float num = __fmaf_rn(-gm, N, Pp);
-          const float den = __fmul_rn(Rtm, __fmaf_rn(__fmul_rn(gm, Aa), A.e2, -1.0f));
-          const float q = __fmul_rn(num, own_rcpf(fabsf(den)));
-          u[k] = den < 0.0f ? -q : q;
-          Ptm[k] = __fmaf_rn(Rtm, u[k], __fmul_rn(Stm, y[k]));
+          float2 gm[4];
+          load8p(sg + base, gm);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float2 d = sub2(y[k], x[k]);
+            const float2 Pohc = mul2(gs[k], d);
+            const float2 t = own_tanhf2(mul2(f2b(A.ratio), ps[k]));
+            const float2 dL = mul2(f2b(A.nas), t);
+            const float2 Aa = mul2(f2b(A.al), fma2(t, t, f2b(-1.0f)));
+            const float2 N1 = fma2(f2b(A.e1), d, fma2(f2b(A.e2), v[k], mul2(f2b(A.nw), ps[k])));
+            const float2 N = fma2(Stm[k], dL, mul2(mul2(N1, Rtm[k]), Aa));
+            const float2 Pp = fma2(Stm[k], y[k], Pohc);
+            const float2 num = fma2(neg2(gm[k]), N, Pp);
+            const float2 den = mul2(Rtm[k], fma2(mul2(gm[k], Aa), f2b(A.e2), f2b(-1.0f)));
+            const float2 q = mul2(num, own_rcpf2(abs2(den)));
+            u[k] = f2(den.x < 0.0f ? -q.x : q.x, den.y < 0.0f ? -q.y : q.y);
+            Ptm[k] = fma2(Rtm[k], u[k], mul2(Stm[k], y[k]));
+          }
         }
-        float g = __fmul_rn(sp[2 * 256 + s], __fmaf_rn(A.ar, __fmul_rn(v[k], v[k]), 1.0f));
-        g = __fmaf_rn(g, v[k], __fmul_rn(sp[3 * 256 + s], x[k]));
-        G[k] = __fsub_rn(-g, Ptm[k]);
-        float Yk = __fmul_rn(__fmul_rn(A.dx2, G[k]), sp[4 * 256 + s]);
-        if (k == 0 && lane == 0)
-          Yk = __fmul_rn(A.dxa0, __fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmul_rn(A.gme, smp))));
-        if (k == kSPL - 1 && lane == 31) Yk = 0.0f;
-        Yrm[k] = __fmul_rn(Yk, rm[k]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float2 g = mul2(Rs[k], fma2(f2b(A.ar), mul2(v[k], v[k]), f2b(1.0f)));
+          g = fma2(g, v[k], mul2(Ss[k], x[k]));
+          G[k] = sub2(neg2(g), Ptm[k]);
+          float2 Yk = mul2(mul2(f2b(A.dx2), G[k]), Qs[k]);
+          if (k == 0 && first)  // section 0
+            Yk.x = __fmul_rn(A.dxa0,
+                             __fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmul_rn(A.gme, smp))));
+          if (k == 3 && last) Yk.y = 0.0f;  // section 255
+          Yrm[k] = mul2(Yk, rm[k]);
+        }
       }
 
       // Jacobi sweeps on the pressure; p persists across iterations and steps.
@@ -256,79 +301,93 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // second on its own sections, so one shuffle round serves two sweeps.
       // Sections 254 and 255 carry no lower coefficient; p_{-1} = p_256 = 0.
       const int J = TOL ? A.jcap : (tm_update ? A.jslow : A.jfast);
-      const float YrmL = __shfl_up_sync(kFull, Yrm[kSPL - 1], 1);
-      const float YrmR = __shfl_down_sync(kFull, Yrm[0], 1);
-      const bool first = lane == 0, last = lane == 31;
+      const float YrmL = __shfl_up_sync(kFull, Yrm[3].y, 1);
+      const float YrmR = __shfl_down_sync(kFull, Yrm[0].x, 1);
       if (TOL && out_loop == 0 && n_sub >= 2) {
-        float p2[kSPL];
-        load8(hist + ((n_sub + 1) & 1) * 256 + base, p2);
+        float2 p2[4];
+        load8p(hist + ((n_sub + 1) & 1) * 256 + base, p2);
         if (A.log && n_sub % A.log_every == 0) {
           int idx = 0;
           if (lane == 0) idx = atomicAdd(A.log_count, 1);
           idx = __shfl_sync(kFull, idx, 0);
           if (idx < A.log_cap) {
             float* rec = A.log + (long long)idx * 6 * 256;
-            store8(rec + 0 * 256 + base, Yrm);
-            store8(rec + 1 * 256 + base, p);
-            store8(rec + 2 * 256 + base, p2);
-            store8(rec + 3 * 256 + base, v);
-            store8(rec + 4 * 256 + base, x);
+            store8p(rec + 0 * 256 + base, Yrm);
+            store8p(rec + 1 * 256 + base, p);
+            store8p(rec + 2 * 256 + base, p2);
+            store8p(rec + 3 * 256 + base, v);
+            store8p(rec + 4 * 256 + base, x);
             float meta[kSPL] = {lane == 0 ? rho : 0.0f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             store8(rec + 5 * 256 + base, meta);
           }
         }
         if (TOL == 2 && n_sub % A.learn_every == 0) {
           const float* wb = reinterpret_cast<const float*>(wblob + ws::kOffBias);
-          float pe[kSPL];
-          const float nr = ws::make_features(Yrm, p, p2, v, x, rm, rho, wb[201], pe, ws_scratch,
-                                             8, lane);
+          float cY[kSPL], cp[kSPL], cp2[kSPL], cv[kSPL], cx[kSPL], crm[kSPL], pe[kSPL];
+          unpair(Yrm, cY);
+          unpair(p, cp);
+          unpair(p2, cp2);
+          unpair(v, cv);
+          unpair(x, cx);
+          unpair(rm, crm);
+          const float nr = ws::make_features(cY, cp, cp2, cv, cx, crm, rho, wb[201], pe,
+                                             ws_scratch, 8, lane);
           __syncwarp();
           ws::infer_unit(wblob, ws_scratch, lane);
-          float o[kSPL];
-          load8(reinterpret_cast<const float*>(ws_scratch + ws::kOffOut) + base, o);
+          float2 o[4];
+          load8p(reinterpret_cast<const float*>(ws_scratch + ws::kOffOut) + base, o);
           const float sc = __fmul_rn(nr, wb[200]);
 #pragma unroll
-          for (int k = 0; k < kSPL; ++k) p[k] = __fmaf_rn(sc, o[k], pe[k]);
+          for (int k = 0; k < 4; ++k)
+            p[k] = fma2(f2b(sc), o[k], f2(pe[k], pe[k + 4]));
           n_sw += 1;  // the residual sweep of the features
           __syncwarp();
         } else if (A.guess >= 1) {
 #pragma unroll
-          for (int k = 0; k < kSPL; ++k) p[k] = __fmaf_rn(rho, __fsub_rn(p[k], p2[k]), p[k]);
+          for (int k = 0; k < 4; ++k) p[k] = fma2(f2b(rho), sub2(p[k], p2[k]), p[k]);
         }
       }
       int it = 0;
       for (; it + 1 < J; it += 2) {
-        const float L1 = __shfl_up_sync(kFull, p[kSPL - 1], 1);
-        const float L2 = __shfl_up_sync(kFull, p[kSPL - 2], 1);
-        const float R1 = __shfl_down_sync(kFull, p[0], 1);
-        const float R2 = __shfl_down_sync(kFull, p[1], 1);
-        float q[kSPL];
-        float qL = __fmaf_rn(-__fadd_rn(L2, p[0]), rmL, YrmL);
-        float qR = __fmaf_rn(-__fadd_rn(p[kSPL - 1], R2), rmR, YrmR);
+        const float L1 = __shfl_up_sync(kFull, p[3].y, 1);   // section 8l-1
+        const float L2 = __shfl_up_sync(kFull, p[2].y, 1);   // section 8l-2
+        const float R1 = __shfl_down_sync(kFull, p[0].x, 1); // section 8l+8
+        const float R2 = __shfl_down_sync(kFull, p[1].x, 1); // section 8l+9
+        float qL = __fmaf_rn(-__fadd_rn(L2, p[0].x), rmL, YrmL);
+        float qR = __fmaf_rn(-__fadd_rn(p[3].y, R2), rmR, YrmR);
         if (first) qL = 0.0f;
         if (last) qR = 0.0f;
-        q[0] = __fmaf_rn(-__fadd_rn(first ? 0.0f : L1, p[1]), rm[0], Yrm[0]);
+        // t_k = p_{k-1} + p_{k+1} on the pairs (k, k+4)
+        float2 T[4];
+        T[0] = add2(f2(first ? 0.0f : L1, p[3].x), p[1]);
+        T[1] = add2(p[0], p[2]);
+        T[2] = add2(p[1], p[3]);
+        T[3] = add2(p[2], f2(p[0].y, R1));
+        if (last) {
+          T[2].y = p[3].y;
+          T[3].y = 0.0f;
+        }
+        float2 q[4];
 #pragma unroll
-        for (int k = 1; k < kSPL - 2; ++k)
-          q[k] = __fmaf_rn(-__fadd_rn(p[k - 1], p[k + 1]), rm[k], Yrm[k]);
-        const float t6 = last ? p[kSPL - 1] : __fadd_rn(p[kSPL - 3], p[kSPL - 1]);
-        const float t7 = last ? 0.0f : __fadd_rn(p[kSPL - 2], R1);
-        q[kSPL - 2] = __fmaf_rn(-t6, rm[kSPL - 2], Yrm[kSPL - 2]);
-        q[kSPL - 1] = __fmaf_rn(-t7, rm[kSPL - 1], Yrm[kSPL - 1]);
-        p[0] = __fmaf_rn(-__fadd_rn(qL, q[1]), rm[0], Yrm[0]);
+        for (int k = 0; k < 4; ++k) q[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
+        T[0] = add2(f2(qL, q[3].x), q[1]);
+        T[1] = add2(q[0], q[2]);
+        T[2] = add2(q[1], q[3]);
+        T[3] = add2(q[2], f2(q[0].y, qR));
+        if (last) {
+          T[2].y = q[3].y;
+          T[3].y = 0.0f;
+        }
 #pragma unroll
-        for (int k = 1; k < kSPL - 2; ++k)
-          p[k] = __fmaf_rn(-__fadd_rn(q[k - 1], q[k + 1]), rm[k], Yrm[k]);
-        const float u6 = last ? q[kSPL - 1] : __fadd_rn(q[kSPL - 3], q[kSPL - 1]);
-        const float u7 = last ? 0.0f : __fadd_rn(q[kSPL - 2], qR);
-        p[kSPL - 2] = __fmaf_rn(-u6, rm[kSPL - 2], Yrm[kSPL - 2]);
-        p[kSPL - 1] = __fmaf_rn(-u7, rm[kSPL - 1], Yrm[kSPL - 1]);
+        for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
         if (TOL) {
           float dm = 0.0f, pm = 0.0f;
 #pragma unroll
-          for (int k = 0; k < kSPL; ++k) {
-            dm = fmaxf(dm, fabsf(__fsub_rn(p[k], q[k])));
-            pm = fmaxf(pm, fabsf(p[k]));
+          for (int k = 0; k < 4; ++k) {
+            const float2 e = abs2(sub2(p[k], q[k]));
+            const float2 ap = abs2(p[k]);
+            dm = fmaxf(dm, fmaxf(e.x, e.y));
+            pm = fmaxf(pm, fmaxf(ap.x, ap.y));
           }
           dm = warp_max_xor(dm);
           pm = warp_max_xor(pm);
@@ -339,40 +398,43 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         }
       }
       if (!TOL && it < J) {
-        float left = __shfl_up_sync(kFull, p[kSPL - 1], 1);
-        float right = __shfl_down_sync(kFull, p[0], 1);
+        float left = __shfl_up_sync(kFull, p[3].y, 1);
+        float right = __shfl_down_sync(kFull, p[0].x, 1);
         if (first) left = 0.0f;
         if (last) right = 0.0f;
-        float t[kSPL];
-        t[0] = __fadd_rn(left, p[1]);
-#pragma unroll
-        for (int k = 1; k < kSPL - 1; ++k) t[k] = __fadd_rn(p[k - 1], p[k + 1]);
-        t[kSPL - 1] = __fadd_rn(p[kSPL - 2], right);
+        float2 T[4];
+        T[0] = add2(f2(left, p[3].x), p[1]);
+        T[1] = add2(p[0], p[2]);
+        T[2] = add2(p[1], p[3]);
+        T[3] = add2(p[2], f2(p[0].y, right));
         if (last) {
-          t[kSPL - 2] = p[kSPL - 1];
-          t[kSPL - 1] = right;
+          T[2].y = p[3].y;
+          T[3].y = right;
         }
 #pragma unroll
-        for (int k = 0; k < kSPL; ++k) p[k] = __fmaf_rn(-t[k], rm[k], Yrm[k]);
+        for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
       }
       n_sw += TOL ? it : J;
 
-      const float p0 = __shfl_sync(kFull, p[0], 0);
-      float da[kSPL];
+      const float p0 = __shfl_sync(kFull, p[0].x, 0);
+      float2 da[4];
+      {
+        float2 invM[4];
+        load8p(sp + 0 * 256 + base, invM);
 #pragma unroll
-      for (int k = 0; k < kSPL; ++k) {
-        const int s = base + k;
-        const float an = __fmul_rn(__fadd_rn(p[k], G[k]), sp[0 * 256 + s]);
-        da[k] = fabsf(__fsub_rn(a[k], an));
-        a[k] = an;
-        const float d = __fsub_rn(y[k], x[k]);
-        dp[k] = __fmaf_rn(A.e1, d, __fmaf_rn(A.e2, __fsub_rn(u[k], v[k]), __fmul_rn(A.nw, ps[k])));
+        for (int k = 0; k < 4; ++k) {
+          const float2 an = mul2(add2(p[k], G[k]), invM[k]);
+          da[k] = abs2(sub2(a[k], an));
+          a[k] = an;
+          const float2 d = sub2(y[k], x[k]);
+          dp[k] = fma2(f2b(A.e1), d, fma2(f2b(A.e2), sub2(u[k], v[k]), mul2(f2b(A.nw), ps[k])));
+        }
       }
       wdd = __fdiv_rn(__fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmaf_rn(A.gme, smp, p0))), A.sow);
 
       if (reset == 0) {
-        const float eap = fmaxf(0.0f, fmaxf(fmaxf(fmaxf(da[0], da[1]), fmaxf(da[2], da[3])),
-                                            fmaxf(fmaxf(da[4], da[5]), fmaxf(da[6], da[7]))));
+        const float2 m = max2(max2(da[0], da[1]), max2(da[2], da[3]));
+        const float eap = fmaxf(0.0f, fmaxf(m.x, m.y));
         const float ea = warp_max_xor(eap);
         const float ev = warp_sum_xor(evp);
         const float F = warp_sum_xor(fp);
@@ -416,9 +478,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       sx0 = sx1;
       sx1 = inb[n + 2];
       if (n >= un.out_first) {
-        float4* o = reinterpret_cast<float4*>(outb + (int64_t)n * 256 + base);
-        o[0] = make_float4(v[0], v[1], v[2], v[3]);
-        o[1] = make_float4(v[4], v[5], v[6], v[7]);
+        store8p(outb + (int64_t)n * 256 + base, v);
         if (fb && lane == 0) fb[n] = fail_flag;
         if (cb && lane == 0) {
           cb[(int64_t)n * 3 + 0] = __fdiv_rn(smp_dt, smp_sub);
@@ -459,7 +519,9 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
 // TOL 2 adds the packed weights and the per-warp inference scratch.
 template <int WARPS, int TOL>
 constexpr int bm_dyn_smem() {
-  return WARPS * 2 * 256 * 4 + (TOL == 2 ? ws::kBlobBytes + WARPS * ws::kWarpScratch : 0);
+  return TOL == 0 ? 0
+                  : WARPS * 2 * 256 * 4 +
+                        (TOL == 2 ? ws::kBlobBytes + WARPS * ws::kWarpScratch : 0);
 }
 
 template <int WARPS, bool PREV_SMEM, int TOL>

@@ -95,16 +95,97 @@ __device__ __forceinline__ float own_log10f(float x) {
   return __fmaf_rn(ef, l2hi, __fmaf_rn(ef, l2lo, __fmul_rn(lnm, 0.43429448190325182f)));
 }
 
+// Packed pairs of FP32 values: Blackwell's two-wide FP32 add / multiply /
+// fma (add.rn.f32x2 and friends).  Every element rounds exactly like the
+// scalar instruction, so a pair computation equals two scalar ones bit for
+// bit; only the instruction count halves.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2b(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, b, c);
+}
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// a - b == a + (-b) exactly (negation is exact), signed zeros included
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+__device__ __forceinline__ float2 max2(float2 a, float2 b) {
+  return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y));
+}
+
+// own_expf_pos on a pair: the same operation sequence per element.
+__device__ __forceinline__ float2 own_expf_pos2(float2 y) {
+  const float log2e = 1.44269504088896341f;
+  const float ln2_hi = 0.693145751953125f;
+  const float ln2_lo = 1.42860682030941723e-06f;
+  const float2 kk = mul2(y, f2b(log2e));
+  const float2 k = f2(rintf(kk.x), rintf(kk.y));
+  float2 r = fma2(neg2(k), f2b(ln2_hi), y);
+  r = fma2(neg2(k), f2b(ln2_lo), r);
+  float2 p = f2b(1.0f / 40320.0f);
+  p = fma2(p, r, f2b(1.0f / 5040.0f));
+  p = fma2(p, r, f2b(1.0f / 720.0f));
+  p = fma2(p, r, f2b(1.0f / 120.0f));
+  p = fma2(p, r, f2b(1.0f / 24.0f));
+  p = fma2(p, r, f2b(1.0f / 6.0f));
+  p = fma2(p, r, f2b(0.5f));
+  p = fma2(p, r, f2b(1.0f));
+  p = fma2(p, r, f2b(1.0f));
+  const float2 scale = f2(__int_as_float(((int)k.x + 127) << 23),
+                          __int_as_float(((int)k.y + 127) << 23));
+  return mul2(p, scale);
+}
+
+// own_rcpf on a pair.
+__device__ __forceinline__ float2 own_rcpf2(float2 d) {
+  float2 r = f2(__int_as_float(0x7EF311C3 - __float_as_int(d.x)),
+                __int_as_float(0x7EF311C3 - __float_as_int(d.y)));
+  const float2 nd = neg2(d);
+  r = fma2(r, fma2(nd, r, f2b(1.0f)), r);
+  r = fma2(r, fma2(nd, r, f2b(1.0f)), r);
+  r = fma2(r, fma2(nd, r, f2b(1.0f)), r);
+  return r;
+}
+
+// own_tanhf on a pair.
+__device__ __forceinline__ float2 own_tanhf2(float2 x) {
+  const float2 ax = abs2(x);
+  const float2 x2 = mul2(x, x);
+  float2 p = f2b((float)(18888466084.0 / 194896477400625.0));
+  p = fma2(p, x2, f2b((float)(-443861162.0 / 1856156927625.0)));
+  p = fma2(p, x2, f2b((float)(6404582.0 / 10854718875.0)));
+  p = fma2(p, x2, f2b((float)(-929569.0 / 638512875.0)));
+  p = fma2(p, x2, f2b((float)(21844.0 / 6081075.0)));
+  p = fma2(p, x2, f2b((float)(-1382.0 / 155925.0)));
+  p = fma2(p, x2, f2b((float)(62.0 / 2835.0)));
+  p = fma2(p, x2, f2b((float)(-17.0 / 315.0)));
+  p = fma2(p, x2, f2b((float)(2.0 / 15.0)));
+  p = fma2(p, x2, f2b((float)(-1.0 / 3.0)));
+  p = mul2(p, x2);
+  const float2 tp = fma2(p, x, x);
+  const float2 e = own_expf_pos2(mul2(f2b(2.0f), f2(fminf(ax.x, 20.0f), fminf(ax.y, 20.0f))));
+  float2 te = fma2(f2b(-2.0f), own_rcpf2(add2(e, f2b(1.0f))), f2b(1.0f));
+  te.x = ax.x < 20.0f ? te.x : 1.0f;
+  te.y = ax.y < 20.0f ? te.y : 1.0f;
+  te.x = x.x < 0.0f ? -te.x : te.x;
+  te.y = x.y < 0.0f ? -te.y : te.y;
+  return f2(ax.x < 0.55f ? tp.x : te.x, ax.y < 0.55f ? tp.y : te.y);
+}
+
 __device__ __forceinline__ float warp_sum_xor(float v) {
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));
   return v;
 }
 
+// Maximum over the full warp in one instruction (redux.sync on f32, a
+// Blackwell addition); callers pass no NaNs, so it equals the fmaxf
+// butterfly exactly.
 __device__ __forceinline__ float warp_max_xor(float v) {
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
-  return v;
+  float r;
+  asm volatile("redux.sync.max.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+  return r;
 }
 
 }  // namespace cgb
