@@ -93,30 +93,56 @@ struct Dot2 {
   __device__ __forceinline__ float result() const { return __fadd_rn(s, c); }
 };
 
+// Dot2 on two independent sums at once (two-wide FP32); each element
+// performs exactly the scalar Dot2 sequence.
+struct Dot2x2 {
+  float2 s, c;
+  __device__ __forceinline__ void init() { s = c = f2b(0.0f); }
+  __device__ __forceinline__ void add(float2 b, float2 x) {
+    const float2 p = mul2(b, x);
+    const float2 q = fma2(b, x, neg2(p));
+    const float2 t = add2(s, p);
+    const float2 z = sub2(t, s);
+    const float2 e = add2(sub2(s, sub2(t, z)), sub2(p, z));
+    s = t;
+    c = add2(c, add2(e, q));
+  }
+  __device__ __forceinline__ float2 result() const { return add2(s, c); }
+};
+
 // FIR of one 8-row block, rows kb..kb+7 all using `taps` taps.  src points at
 // the staged row of output kb (lane's column); rows above it are older.  One
-// shared-memory load feeds the eight rows' accumulators.
+// shared-memory load feeds the eight rows' accumulators.  Rows r and r+4 form
+// pair r, so the per-tap shift of the window moves whole pairs and only pair
+// 0 is assembled from the newly loaded row.  The last step loads one row
+// beyond the oldest tap (unused; the caller stages it).
 __device__ __forceinline__ void fir_block8(const float* __restrict__ src,
                                            const float* __restrict__ b, int taps,
                                            float (&out)[kRB]) {
-  float w[kRB];
-  Dot2 acc[kRB];
+  float2 W[4];
+  Dot2x2 acc[4];
 #pragma unroll
-  for (int r = 0; r < kRB; ++r) {
-    acc[r].init();
-    w[r] = src[r * kSecTile];
+  for (int j = 0; j < 4; ++j) {
+    acc[j].init();
+    W[j] = f2(src[j * kSecTile], src[(j + 4) * kSecTile]);
   }
 #pragma unroll 4
   for (int i = 0; i < taps; ++i) {
-    const float bi = b[i];
+    const float2 bi = f2b(b[i]);
 #pragma unroll
-    for (int r = 0; r < kRB; ++r) acc[r].add(bi, w[r]);
-#pragma unroll
-    for (int r = kRB - 1; r > 0; --r) w[r] = w[r - 1];
-    w[0] = src[-(i + 1) * kSecTile];
+    for (int j = 0; j < 4; ++j) acc[j].add(bi, W[j]);
+    const float w3 = W[3].x;
+    W[3] = W[2];
+    W[2] = W[1];
+    W[1] = W[0];
+    W[0] = f2(src[-(i + 1) * kSecTile], w3);
   }
 #pragma unroll
-  for (int r = 0; r < kRB; ++r) out[r] = acc[r].result();
+  for (int j = 0; j < 4; ++j) {
+    const float2 r = acc[j].result();
+    out[j] = r.x;
+    out[j + 4] = r.y;
+  }
 }
 
 // s + c += x exactly (Knuth's TwoSum; the rounding error goes to c).
@@ -179,7 +205,7 @@ __device__ __forceinline__ bool wait_stage(uint64_t* mbar, uint32_t parity) {
 // of one frame, processed in order.  The first tile of the run computes AC
 // and dS on the DC filter's look-back rows as well; later tiles inherit those
 // n_dc - 1 rows of dS from the previous tile (shifted down in shared memory)
-// and stage only the AC filter's look-back, the next tile's rows being copied
+// and stage only the AC filter's look-back (plus one row), the next tile's rows being copied
 // by TMA while the current tile's DC/IHC/lambda phase runs.
 __global__ void __launch_bounds__(kIhcWarps * 32)
     ihc_lambda_kernel(const __grid_constant__ CUtensorMap vmap, const IHCArgs A) {
@@ -206,7 +232,10 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
   const int s0 = blockIdx.y * kSecTile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int boxes_first = A.xrows / kBoxRows;
-  const int boxes_next = (A.TR + A.n_ac - 1 + kBoxRows - 1) / kBoxRows;
+  // later tiles stage rows from row0 - n_ac: the register-blocked FIR loads
+  // one row beyond its oldest tap on its last step (a value it never uses),
+  // and that row must lie inside the staged window
+  const int boxes_next = (A.TR + A.n_ac + kBoxRows - 1) / kBoxRows;
 
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
@@ -232,7 +261,7 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
     const bool first = t == t0;
     const int row0 = t * A.TR;
     const int TRt = min(A.TR, f.lam_rows - row0);
-    const int xbase = first ? row0 - A.n_ac - A.n_dc + 1 : row0 - A.n_ac + 1;
+    const int xbase = first ? row0 - A.n_ac - A.n_dc + 1 : row0 - A.n_ac;
     const int dsbase = row0 - A.n_dc;
     if (!wait_stage(mbar, (uint32_t)((t - t0) & 1))) {
       if (threadIdx.x == 0) atomicOr(A.status, 1);
@@ -275,7 +304,7 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
     __syncthreads();
     // X is free: stage the next tile while this one finishes
     if (threadIdx.x == 0 && t + 1 < t1)
-      stage_rows(&vmap, X, mbar, boxes_next, (int)f.v_row0 + (t + 1) * A.TR - A.n_ac + 1, s0);
+      stage_rows(&vmap, X, mbar, boxes_next, (int)f.v_row0 + (t + 1) * A.TR - A.n_ac, s0);
 
     // phase 2: DC, IHC and lambda on rows [row0, row0 + TRt)
     auto emit = [&](int k, float dc) {
