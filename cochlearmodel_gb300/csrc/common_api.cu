@@ -160,7 +160,9 @@ struct Holder {
   float* d_aihc = nullptr;     size_t d_aihc_n = 0;
   // IHC / lambda
   bool ihc_ready = false;
-  std::vector<float> ac_taps, dc_taps;
+  std::vector<float> ac_taps, dc_taps, ac_a_taps;
+  bool ac_iir = false;
+  float* ac_buf = nullptr;     size_t ac_buf_n = 0;   // AC by velocity row (IIR path)
   cgb_ihc_params ihc_prm{};
   float W[3] = {0.61f, 0.23f, 0.16f};
   float* dmg = nullptr;        size_t dmg_n = 0;
@@ -492,7 +494,7 @@ extern "C" void calculateBoundariesForNonGeneratedInput(int, int, int, float, fl
 // ---------------------------------------------------------------- IHC / lambda
 extern "C" void IHCNewKernel(double* IHC_Damage_Factor, float Nerves_Clusters[3 * LAMBDA_COUNT],
                              double* dc_filter, int order_of_dc_filter, double* ac_b_filter,
-                             double*, bool is_ac_iir_filter, int order_of_ac_filter,
+                             double* ac_a_filter, bool is_ac_iir_filter, int order_of_ac_filter,
                              int cochlea_sections, int time_blocks, double, float*, int,
                              int calcTime, int, int allocateTime, int intervalTimeNodes, int,
                              int lambda_offset, float Lambda_SAT, float eta_AC, float eta_DC, bool,
@@ -501,14 +503,18 @@ extern "C" void IHCNewKernel(double* IHC_Damage_Factor, float Nerves_Clusters[3 
                              int maxJNDIntervals, int, int Decouple_Filter, int, Log&) {
   if (cochlea_sections != 256)
     throw std::runtime_error("cochlea_gb300: 256 cochlear sections are built");
-  if (is_ac_iir_filter)
-    throw std::runtime_error("cochlea_gb300: IIR AC filters are not built (FIR only)");
+  if (is_ac_iir_filter && (!ac_a_filter || order_of_ac_filter < 1 || order_of_ac_filter > 64))
+    throw std::runtime_error("cochlea_gb300: IIR AC filter needs 1..64 a/b coefficients");
   if (lambda_offset != 0)
     throw std::runtime_error("cochlea_gb300: lambda_offset must be 0");
   ensure(H.lam, H.lam_n, (size_t)LAMBDA_COUNT * allocateTime * 256, "lambda buffer");
   if (asMemoryHandlingOnly) return;
   H.ac_taps.assign(order_of_ac_filter, 0.0f);
   for (int i = 0; i < order_of_ac_filter; ++i) H.ac_taps[i] = (float)ac_b_filter[i];
+  H.ac_iir = is_ac_iir_filter;
+  H.ac_a_taps.assign(is_ac_iir_filter ? order_of_ac_filter : 0, 0.0f);
+  for (int i = 0; is_ac_iir_filter && i < order_of_ac_filter; ++i)
+    H.ac_a_taps[i] = (float)ac_a_filter[i];
   H.dc_taps.assign(order_of_dc_filter, 0.0f);
   for (int i = 0; i < order_of_dc_filter; ++i) H.dc_taps[i] = (float)dc_filter[i];
   std::vector<float> dmg(256);
@@ -543,7 +549,8 @@ extern "C" void RunIHCKernel(JNDFloat* host_backup, int, int save_lambda, int ba
   if (!H.ihc_ready) throw std::runtime_error("cochlea_gb300: RunIHCKernel before IHCNewKernel");
   if (!H.d_aihc) throw std::runtime_error("cochlea_gb300: RunIHCKernel before loadAihc");
   const bool want_ihc = backup_stage == 13 || backup_stage == 14;
-  if (backup_stage >= 9 && backup_stage <= 12)
+  const bool want_ac = backup_stage == 9 && H.ac_iir;  // the IIR path keeps AC
+  if (backup_stage >= 9 && backup_stage <= 12 && !want_ac)
     throw std::runtime_error("cochlea_gb300: the fused IHC kernel exposes no AC/DC/dS stage");
   const int64_t v_rows = (int64_t)(H.speeds_n / 256);
   cgb_ihc_frame fr{};
@@ -558,7 +565,10 @@ extern "C" void RunIHCKernel(JNDFloat* host_backup, int, int save_lambda, int ba
   if (fr.lam_rows > fr.rows)
     throw std::runtime_error("cochlea_gb300: lambda rows exceed the velocity buffer");
   const int64_t need =
-      cgb_ihc_lambda_scratch_bytes(1, (int)H.ac_taps.size(), (int)H.dc_taps.size());
+      H.ac_iir ? cgb_ihc_lambda_iir_scratch_bytes(&fr, 1, (int)H.ac_taps.size(),
+                                                  (int)H.dc_taps.size())
+               : cgb_ihc_lambda_scratch_bytes(1, (int)H.ac_taps.size(), (int)H.dc_taps.size());
+  if (need < 0) throw std::runtime_error("cochlea_gb300: bad IIR filter");
   ensure(H.scratch, H.scratch_n, (size_t)need, "IHC scratch");
   float* ihc = nullptr;
   if (want_ihc) {
@@ -566,15 +576,29 @@ extern "C" void RunIHCKernel(JNDFloat* host_backup, int, int save_lambda, int ba
     ihc = H.buffer1;
   }
   gpu_check(cudaMemset(H.status, 0, sizeof(int32_t)), "reset status");
-  cgb_check(cgb_ihc_lambda_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(), (int)H.ac_taps.size(),
-                               H.dc_taps.data(), (int)H.dc_taps.size(), &H.ihc_prm, H.dmg, 1,
-                               H.d_aihc, H.lam, H.calc_time, ihc, H.scratch,
-                               (int64_t)H.scratch_n, H.status, nullptr),
-            "IHC/lambda");
+  if (H.ac_iir) {
+    ensure(H.ac_buf, H.ac_buf_n, (size_t)v_rows * 256, "AC buffer");
+    cgb_check(cgb_ihc_lambda_iir_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
+                                     H.ac_a_taps.data(), (int)H.ac_taps.size(),
+                                     H.dc_taps.data(), (int)H.dc_taps.size(), &H.ihc_prm, H.dmg,
+                                     1, H.d_aihc, H.lam, H.calc_time, ihc, H.ac_buf, H.scratch,
+                                     (int64_t)H.scratch_n, H.status, nullptr),
+              "IHC/lambda (IIR AC)");
+  } else {
+    cgb_check(cgb_ihc_lambda_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
+                                 (int)H.ac_taps.size(), H.dc_taps.data(), (int)H.dc_taps.size(),
+                                 &H.ihc_prm, H.dmg, 1, H.d_aihc, H.lam, H.calc_time, ihc,
+                                 H.scratch, (int64_t)H.scratch_n, H.status, nullptr),
+              "IHC/lambda");
+  }
   gpu_check(cudaDeviceSynchronize(), "IHC/lambda");
   int32_t status = 0;
   gpu_check(cudaMemcpy(&status, H.status, sizeof(int32_t), cudaMemcpyDeviceToHost), "status");
   if (status) throw std::runtime_error("cochlea_gb300: IHC staging copy timed out");
+  if (want_ac && host_backup)
+    gpu_check(cudaMemcpy(host_backup, H.ac_buf, (size_t)fr.rows * 256 * sizeof(float),
+                         cudaMemcpyDeviceToHost),
+              "AC backup");
   if (want_ihc && host_backup)
     gpu_check(cudaMemcpy(host_backup, H.buffer1, (size_t)H.calc_time * 256 * sizeof(float),
                          cudaMemcpyDeviceToHost),
@@ -589,6 +613,7 @@ extern "C" void RunIHCKernel(JNDFloat* host_backup, int, int save_lambda, int ba
 
 extern "C" void IHCKernel_Free() {
   release(H.lam, H.lam_n);
+  release(H.ac_buf, H.ac_buf_n);
   release(H.dmg, H.dmg_n);
   release(H.scratch, H.scratch_n);
   release(H.status, H.status_n);

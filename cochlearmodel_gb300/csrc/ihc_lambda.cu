@@ -61,6 +61,7 @@ struct IHCArgs {
   int32_t* status;
   int dc_uniform;              // all DC taps equal: running window sum
   int run;                     // tiles per CTA (consecutive, one frame)
+  const float* ac_ext;         // AC by velocity row (the IIR path), or null: the FIR
 };
 
 __device__ __forceinline__ int taps_used(int k, const cgb_ihc_frame& f, int taps) {
@@ -284,7 +285,11 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
         fast = fast && taps_used(kb + r, f, A.n_ac) == A.n_ac;
       float acc[kRB];
       const float* src = X + (size_t)(kb - xbase) * kSecTile + lane;
-      if (fast) {
+      if (A.ac_ext) {
+#pragma unroll
+        for (int r = 0; r < kRB; ++r)
+          acc[r] = r < nr ? A.ac_ext[((int64_t)f.v_row0 + kb + r) * 256 + s] : 0.0f;
+      } else if (fast) {
         fir_block8(src, bac, A.n_ac, acc);
       } else {
 #pragma unroll
@@ -412,7 +417,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
                     const cgb_ihc_params* prm, const float* d_dmg, int n_dmg_profiles,
                     const float* d_aihc, float* d_lam, int64_t lam_plane_rows, float* d_ihc,
                     void* d_scratch, int64_t scratch_bytes, int32_t* d_status, void* stream,
-                    int mode) {
+                    int mode,
+                    const float* ac_ext = nullptr) {
   if (n_frames == 0) return CGB_OK;
   if (!frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_scratch ||
       ((mode & kLaunch) && (!d_v || !d_dmg || !d_aihc || !d_lam || !d_status)))
@@ -508,6 +514,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   A.TR = TR;
   A.xrows = xrows;
   A.status = d_status;
+  A.ac_ext = ac_ext;
   A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
@@ -710,6 +717,7 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   A.TR = TR;
   A.xrows = xrows;
   A.status = d_status;
+  A.ac_ext = nullptr;
   A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
@@ -722,4 +730,150 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   CGB_TRY_CUDA(cudaGetLastError(), "ihc_lambda_kernel launch");
   note_launch();
   return CGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// AC by IIR (the reference's is_ac_iir_filter path, DeviceCudaIIRFilter,
+// src/cochlea.cu:2745-2775):
+//   Y[k] = sum_{i<ob} b_i X[k-i] - sum_{1<=j<ob} a_j Y[k-j]
+// with ob the FIR look-back bound.  The reference keeps Y in float (lambdaFloat)
+// and adds each double-tap term in double before rounding back to float; the
+// kernel performs those FP64 operations in the same order (products and sums
+// rounded separately).  The recursion is sequential in time, so one CTA walks
+// one segment of a frame -- rows between two points where the look-back rule
+// gives zero taps, which start the recursion afresh -- with one thread per
+// section.
+// ---------------------------------------------------------------------------
+namespace cgb {
+namespace {
+
+struct IIRSeg {
+  int64_t v_row0;  // the frame's first velocity row
+  int32_t k0, k1;  // frame rows [k0, k1)
+  int32_t frame;
+  int32_t pad;
+};
+
+__global__ void __launch_bounds__(256)
+    iir_ac_kernel(const float* __restrict__ v, float* __restrict__ ac,
+                  const IIRSeg* __restrict__ segs, const cgb_ihc_frame* __restrict__ frames,
+                  const double* __restrict__ b, const double* __restrict__ a, int n) {
+  const IIRSeg sg = segs[blockIdx.x];
+  const cgb_ihc_frame f = frames[sg.frame];
+  const int s = threadIdx.x;
+  const float* x = v + sg.v_row0 * 256 + s;
+  float* y = ac + sg.v_row0 * 256 + s;
+  for (int k = sg.k0; k < sg.k1; ++k) {
+    const int ob = taps_used(k, f, n);
+    float yk = 0.0f;
+    for (int i = 0; i < ob; ++i)
+      yk = __double2float_rn(__dadd_rn((double)yk, __dmul_rn(b[i], (double)x[(int64_t)(k - i) * 256])));
+    for (int j = 1; j < ob; ++j)
+      yk = __double2float_rn(__dsub_rn((double)yk, __dmul_rn(a[j], (double)y[(int64_t)(k - j) * 256])));
+    y[(int64_t)k * 256] = yk;
+  }
+}
+
+constexpr int kMaxIIR = 64;
+
+// Segments of every frame's lambda rows that the recursion can run
+// independently: candidate starts are rows whose look-back bound is zero;
+// a candidate is dropped when a later row's recursion reaches back across it
+// (where the rule switches to the frame total, the bound can jump up).
+std::vector<IIRSeg> iir_segments(const cgb_ihc_frame* frames, int n_frames, int n) {
+  std::vector<IIRSeg> out;
+  std::vector<int> starts;
+  for (int fi = 0; fi < n_frames; ++fi) {
+    const cgb_ihc_frame& f = frames[fi];
+    starts.assign(1, 0);
+    for (int k = 0; k < f.lam_rows; ++k) {
+      const int sg = k < f.frdp - 1 ? f.seg : f.total;
+      const int lim = (k + 1) % sg;
+      const int ob = lim < n ? lim : n;
+      if (ob == 0) {
+        if (k > starts.back()) starts.push_back(k);
+      } else if (ob >= 2) {
+        const int lo = k - ob + 1;  // oldest output row this row reads
+        while (starts.size() > 1 && starts.back() > lo) starts.pop_back();
+      }
+    }
+    for (size_t i = 0; i < starts.size(); ++i) {
+      const int k1 = i + 1 < starts.size() ? starts[i + 1] : f.lam_rows;
+      if (k1 > starts[i]) out.push_back({f.v_row0, starts[i], k1, fi, 0});
+    }
+  }
+  return out;
+}
+
+size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+}  // namespace
+}  // namespace cgb
+
+extern "C" int64_t cgb_ihc_lambda_iir_scratch_bytes(const cgb_ihc_frame* frames, int n_frames,
+                                                    int n_iir, int n_dc) {
+  using namespace cgb;
+  if (!frames || n_frames < 0 || n_iir < 1 || n_iir > kMaxIIR) return -1;
+  const size_t segs = iir_segments(frames, n_frames, n_iir).size();
+  return cgb_ihc_lambda_scratch_bytes(n_frames, 1, n_dc) +
+         (int64_t)(align256(segs * sizeof(IIRSeg)) + align256((size_t)2 * n_iir * 8));
+}
+
+extern "C" int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows,
+                                      const cgb_ihc_frame* frames, int n_frames,
+                                      const float* b_taps, const float* a_taps, int n_iir,
+                                      const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+                                      const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
+                                      float* d_lam, int64_t lam_plane_rows, float* d_ihc,
+                                      float* d_ac, void* d_scratch, int64_t scratch_bytes,
+                                      int32_t* d_status, void* stream) {
+  using namespace cgb;
+  if (n_frames == 0) return CGB_OK;
+  if (!frames || n_frames < 0 || !b_taps || !a_taps || !d_ac || !d_v || !prm || !d_scratch)
+    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_iir_dev: null pointer argument");
+  if (n_iir < 1 || n_iir > kMaxIIR)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_iir_dev: IIR length must be in [1, 64]");
+  const int64_t need = cgb_ihc_lambda_iir_scratch_bytes(frames, n_frames, n_iir, n_dc);
+  if (scratch_bytes < need)
+    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_iir_dev: scratch buffer too small");
+  for (int i = 0; i < n_frames; ++i) {
+    const cgb_ihc_frame& fr = frames[i];
+    if (fr.v_row0 < 0 || fr.lam_rows < 0 || fr.lam_rows > fr.rows || fr.v_row0 + fr.rows > v_rows ||
+        fr.seg <= 0 || fr.frdp <= 0 || fr.total <= 0)
+      return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_iir_dev: frame outside the velocity rows");
+  }
+  const std::vector<IIRSeg> segs = iir_segments(frames, n_frames, n_iir);
+  const int64_t base_bytes = cgb_ihc_lambda_scratch_bytes(n_frames, 1, n_dc);
+  unsigned char* sc = static_cast<unsigned char*>(d_scratch) + base_bytes;
+  const size_t seg_bytes = align256(segs.size() * sizeof(IIRSeg));
+  std::vector<double> taps(2 * (size_t)n_iir);
+  for (int i = 0; i < n_iir; ++i) {
+    taps[i] = (double)b_taps[i] * (double)prm->scale;
+    taps[n_iir + i] = (double)a_taps[i];
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  // the fused kernel's tables first (its frame table is the IIR kernel's too)
+  const float one = 1.0f;
+  int rc = ihc_lambda_impl(d_v, v_rows, frames, n_frames, &one, 1, dc_taps, n_dc, prm, d_dmg,
+                           n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc, d_scratch,
+                           base_bytes, d_status, stream, kUpload);
+  if (rc) return rc;
+  if (!segs.empty()) {
+    CGB_TRY_CUDA(cudaMemcpyAsync(sc, segs.data(), segs.size() * sizeof(IIRSeg),
+                                 cudaMemcpyHostToDevice, st),
+                 "upload IIR segments");
+    CGB_TRY_CUDA(cudaMemcpyAsync(sc + seg_bytes, taps.data(), taps.size() * 8,
+                                 cudaMemcpyHostToDevice, st),
+                 "upload IIR taps");
+    iir_ac_kernel<<<(unsigned)segs.size(), 256, 0, st>>>(
+        d_v, d_ac, reinterpret_cast<const IIRSeg*>(sc),
+        reinterpret_cast<const cgb_ihc_frame*>(d_scratch),
+        reinterpret_cast<const double*>(sc + seg_bytes),
+        reinterpret_cast<const double*>(sc + seg_bytes) + n_iir, n_iir);
+    CGB_TRY_CUDA(cudaGetLastError(), "iir_ac_kernel launch");
+    note_launch();
+  }
+  return ihc_lambda_impl(d_v, v_rows, frames, n_frames, &one, 1, dc_taps, n_dc, prm, d_dmg,
+                         n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc, d_scratch,
+                         base_bytes, d_status, stream, kLaunch, d_ac);
 }

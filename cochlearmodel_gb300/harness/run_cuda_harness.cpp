@@ -221,6 +221,16 @@ int main(int argc, char** argv) {
     // IHC + lambda (AudioGramCreator::runInCuda)
     const auto ac = read_f32(P.str("AC_Filter_File", ""));
     std::vector<double> acd(ac.begin(), ac.end());
+    // AC_Filter_A_File (raw float32 a coefficients, a[0] = 1) makes the AC
+    // filter an IIR of the same length (is_ac_iir_filter)
+    const std::string a_file = P.str("AC_Filter_A_File", "");
+    const bool ac_iir = !a_file.empty();
+    std::vector<double> acd_a = acd;
+    if (ac_iir) {
+      const auto aa = read_f32(a_file);
+      if (aa.size() != ac.size()) throw std::runtime_error("AC_Filter_A_File length != AC_Filter_File");
+      acd_a.assign(aa.begin(), aa.end());
+    }
     const int dc_n = (int)std::round((float)Fs * 2e-3f);
     std::vector<double> dcd(dc_n, (double)(1.0f / ((float)Fs * 2e-3f)));
     std::vector<double> dmg(256);
@@ -231,7 +241,7 @@ int main(int argc, char** argv) {
     const int calc_time = (write_time + 63) / 64 * 64;
     enableloadAihc();
     loadAihc(aihc.data());
-    IHCNewKernel(dmg.data(), clusters, dcd.data(), dc_n, acd.data(), acd.data(), false,
+    IHCNewKernel(dmg.data(), clusters, dcd.data(), dc_n, acd.data(), acd_a.data(), ac_iir,
                  (int)acd.size(), 256, TB, spl_ref, nullptr, 0, calc_time, write_time,
                  (int)(samples_p1 + 4), N, 0, 0, 500.0f, 1.0f, 100.0f, true, true, false, true,
                  false, false, 1.0f, calc_jnd, n_int, overlap, D, 0, log);

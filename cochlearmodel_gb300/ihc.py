@@ -81,6 +81,27 @@ def design_ac_lowpass(fc: float = 800.0, fs: float = 100000.0, ntaps: int = 255)
     return h.astype(np.float32)
 
 
+def design_ac_iir_lowpass(fc: float = 800.0, fs: float = 100000.0, order: int = 2):
+    """AC low-pass IIR for the reference's is_ac_iir_filter path: a Butterworth
+    low-pass of even `order`, by the bilinear transform with the cutoff
+    prewarped, as cascaded second-order sections multiplied out into one
+    direct-form (b, a) of order + 1 coefficients each (a[0] = 1)."""
+    if order < 2 or order % 2:
+        raise ValueError("order must be even and >= 2")
+    K = math.tan(math.pi * fc / fs)
+    b = np.array([1.0])
+    a = np.array([1.0])
+    for m in range(order // 2):
+        # pole pair of the analog prototype: q = 1 / (2 sin((2m+1) pi / (2 order)))
+        two_zeta = 2.0 * math.sin((2 * m + 1) * math.pi / (2 * order))
+        norm = 1.0 / (1.0 + two_zeta * K + K * K)
+        bs = np.array([K * K, 2 * K * K, K * K]) * norm
+        as_ = np.array([1.0, 2.0 * (K * K - 1.0) * norm, (1.0 - two_zeta * K + K * K) * norm])
+        b = np.convolve(b, bs)
+        a = np.convolve(a, as_)
+    return b.astype(np.float32), a.astype(np.float32)
+
+
 def round64(n: int) -> int:
     return (n + 63) // 64 * 64
 
@@ -143,10 +164,40 @@ class IHCStage:
             native.ptr(sc), int(sc.numel()), native.ptr(self.status),
             C.c_void_p(st.cuda_stream)), "cgb_ihc_lambda_dev")
 
+    def run_iir(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, b, a,
+                want_ihc: bool = False):
+        """Host-buffer call of the IIR AC path; returns (lambda, ihc or None, ac)."""
+        torch = self.torch
+        frames = np.ascontiguousarray(frames).view(FRAME_DTYPE)
+        b = np.ascontiguousarray(b, np.float32)
+        a = np.ascontiguousarray(a, np.float32)
+        d_v = torch.from_numpy(np.require(v, np.float32, ["C", "W"])).to(self.device)
+        lam = torch.zeros((3, lam_rows, 256), dtype=torch.float32, device=self.device)
+        ihc = torch.zeros((lam_rows, 256), dtype=torch.float32, device=self.device) \
+            if want_ihc else None
+        ac = torch.zeros_like(d_v)
+        need = self.lib.cgb_ihc_lambda_iir_scratch_bytes(native.ptr(frames), len(frames), len(b),
+                                                         len(self.dc))
+        if need < 0:
+            raise native.CGBError("bad IIR filter or frame table")
+        sc = torch.empty(int(need), dtype=torch.uint8, device=self.device)
+        self.status.zero_()
+        st = torch.cuda.current_stream(self.device)
+        native.check(self.lib.cgb_ihc_lambda_iir_dev(
+            native.ptr(d_v), int(d_v.shape[0]), native.ptr(frames), len(frames), native.ptr(b),
+            native.ptr(a), len(b), native.ptr(self.dc), len(self.dc), C.byref(self.prm),
+            native.ptr(self.dmg), int(self.dmg.shape[0]), native.ptr(self.aihc), native.ptr(lam),
+            lam_rows, native.ptr(ihc), native.ptr(ac), native.ptr(sc), int(sc.numel()),
+            native.ptr(self.status), C.c_void_p(st.cuda_stream)), "cgb_ihc_lambda_iir_dev")
+        torch.cuda.synchronize(self.device)
+        if int(self.status[0].item()) != 0:
+            raise native.CGBError("IHC stage: a staged copy did not complete")
+        return lam.cpu().numpy(), (ihc.cpu().numpy() if want_ihc else None), ac.cpu().numpy()
+
     def run(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, want_ihc: bool = False):
         """Host-buffer call; returns (lambda float32[3][lam_rows][256], ihc or None)."""
         torch = self.torch
-        d_v = torch.from_numpy(np.ascontiguousarray(v, np.float32)).to(self.device)
+        d_v = torch.from_numpy(np.require(v, np.float32, ["C", "W"])).to(self.device)
         lam = torch.zeros((3, lam_rows, 256), dtype=torch.float32, device=self.device)
         ihc = torch.zeros((lam_rows, 256), dtype=torch.float32, device=self.device) \
             if want_ihc else None

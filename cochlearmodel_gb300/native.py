@@ -71,6 +71,9 @@ _SIGS = {
     "cgb_noise_normalization": (_i, [_p, _i, _d, _d, _i, _i, _i, _i, C.c_float, _p, _p]),
     "cgb_jnd_dev": (_i, [_p, _i64, _i, _i, _i, _i, _p, _p, _p, _p, _d, _d, _p, _p, _p, _p]),
     "cgb_jnd_final": (_i, [_p, _p, _i, _p, _d, _d, _p, _p]),
+    "cgb_ihc_lambda_iir_scratch_bytes": (_i64, [_p, _i, _i, _i]),
+    "cgb_ihc_lambda_iir_dev": (_i, [_p, _i64, _p, _i, _p, _p, _i, _p, _i, _p, _p, _i, _p, _p,
+                                    _i64, _p, _p, _p, _i64, _p, _p]),
     "cgb_jnd_batch_dev": (_i, [_p, _i64, _p, _i, _i, _p, _p, _d, _d, _p, _p, _p, _p]),
     "cgb_ihc_lambda_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64, _p,
                                 _p, _i64, _p, _p]),

@@ -258,6 +258,27 @@ int cgb_ihc_lambda_launch_dev(const float* d_v, int64_t v_rows, const cgb_ihc_fr
                               int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
                               int64_t scratch_bytes, int32_t* d_status, void* stream);
 
+/* IHC + lambda with the AC stage by IIR (the reference's is_ac_iir_filter
+ * path, DeviceCudaIIRFilter src/cochlea.cu:2745-2775):
+ *   AC[k] = sum_{i<ob} b_i v[k-i] - sum_{1<=j<ob} a_j AC[k-j]
+ * with ob the FIR look-back bound, in the reference's arithmetic (float
+ * accumulator, each double-tap term added in double and rounded).  b_taps
+ * are multiplied by prm->scale; a_taps[0] is not used.  The recursion runs
+ * per section along independent segments of each frame, then the fused
+ * kernel continues from d_ac.
+ *   d_ac     float[v_rows][256] scratch receiving AC (by velocity row)
+ *   scratch  cgb_ihc_lambda_iir_scratch_bytes(frames, n_frames, n_iir, n_dc)
+ * IIR lengths 1..64. */
+int64_t cgb_ihc_lambda_iir_scratch_bytes(const cgb_ihc_frame* frames, int n_frames, int n_iir,
+                                         int n_dc);
+int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                           int n_frames, const float* b_taps, const float* a_taps, int n_iir,
+                           const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+                           const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
+                           float* d_lam, int64_t lam_plane_rows, float* d_ihc, float* d_ac,
+                           void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
+                           void* stream);
+
 /* IHC + lambda without any device allocation -- no counterpart in the
  * reference.  For callers that cannot allocate device memory (a host that
  * gives the library only buffers it already owns, a real-time audio thread

@@ -678,12 +678,12 @@ static inline int fir_taps_used(int k, int seg, int frdp, int total, int taps) {
   return lim < taps ? lim : taps;
 }
 
-void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int lam_rows,
-                    const double* ac_taps, int n_ac, const double* dc_taps, int n_dc,
-                    double scale, double eta_ac, double eta_dc, const double* ihc_damage,
-                    const float* aihc /*[3][256]*/, const float* spont /*[3]*/,
-                    double lambda_sat, float* ihc, float* lam, int64_t lam_stride,
-                    int mode /*0: reference mixed precision, 1: all double, 2: kernel FP32*/) {
+// ac_in: AC already computed (the IIR path), else the AC FIR runs.
+static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int total, int lam_rows,
+                            const double* ac_taps, int n_ac, const double* dc_taps, int n_dc,
+                            double scale, double eta_ac, double eta_dc, const double* ihc_damage,
+                            const float* aihc, const float* spont, double lambda_sat, float* ihc,
+                            float* lam, int64_t lam_stride, int mode, const float* ac_in) {
   if (mode == 2) {
     // The GB300 kernel's arithmetic: float taps (AC taps pre-scaled), each
     // FIR summed over taps in order with the compensated dot product Dot2
@@ -709,7 +709,7 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
     for (int k = 0; k < lam_rows; ++k) {
       int tu = fir_taps_used(k, seg, frdp, total, n_ac);
       for (int s = 0; s < NS; ++s) {
-        float acc = dot2(bt.data(), v + (size_t)k * NS + s, tu);
+        float acc = ac_in ? ac_in[(size_t)k * NS + s] : dot2(bt.data(), v + (size_t)k * NS + s, tu);
         acf[(size_t)k * NS + s] = acc;
         float ms = fmaf(v[(size_t)k * NS + s], sc, -acc);
         dsf[(size_t)k * NS + s] = ms * ms;
@@ -771,8 +771,11 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
     int tu = fir_taps_used(k, seg, frdp, total, n_ac);
     for (int s = 0; s < NS; ++s) {
       double acc = 0.0;
-      for (int i = 0; i < tu; ++i)
-        acc = acc + ac_taps[i] * scale * (double)v[(size_t)(k - i) * NS + s];
+      if (ac_in)
+        acc = (double)ac_in[(size_t)k * NS + s];
+      else
+        for (int i = 0; i < tu; ++i)
+          acc = acc + ac_taps[i] * scale * (double)v[(size_t)(k - i) * NS + s];
       if (fp64) {
         ac[(size_t)k * NS + s] = acc;
         double ms = (double)v[(size_t)k * NS + s] * scale - acc;
@@ -811,6 +814,54 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
       }
     }
   }
+}
+
+void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int lam_rows,
+                    const double* ac_taps, int n_ac, const double* dc_taps, int n_dc,
+                    double scale, double eta_ac, double eta_dc, const double* ihc_damage,
+                    const float* aihc /*[3][256]*/, const float* spont /*[3]*/,
+                    double lambda_sat, float* ihc, float* lam, int64_t lam_stride,
+                    int mode /*0: reference mixed precision, 1: all double, 2: kernel FP32*/) {
+  ihc_lambda_impl(v, rows, seg, frdp, total, lam_rows, ac_taps, n_ac, dc_taps, n_dc, scale,
+                  eta_ac, eta_dc, ihc_damage, aihc, spont, lambda_sat, ihc, lam, lam_stride, mode,
+                  nullptr);
+}
+
+// AC by the reference's IIR recursion (DeviceCudaIIRFilter, src/cochlea.cu:2745-2775):
+//   Y[k] = sum_{i<ob} b_i X[k-i] - sum_{1<=j<ob} a_j Y[k-j],  ob = the FIR look-back
+// bound, accumulated in float with each term added in double and rounded
+// (the reference's float accumulator with double taps; products and sums kept
+// as separate roundings).  b taps are multiplied by scale once, as the host
+// does; a_0 is not used (normalised).
+void orc_iir_ac(const float* v, int rows, int seg, int frdp, int total, const double* b,
+                const double* a, int n, double scale, float* ac) {
+  std::vector<double> bs(n);
+  for (int i = 0; i < n; ++i) bs[i] = b[i] * scale;
+  for (int k = 0; k < rows; ++k) {
+    const int ob = fir_taps_used(k, seg, frdp, total, n);
+    for (int s = 0; s < NS; ++s) {
+      float y = 0.0f;
+      for (int i = 0; i < ob; ++i) y = (float)((double)y + bs[i] * (double)v[(size_t)(k - i) * NS + s]);
+      for (int j = 1; j < ob; ++j) y = (float)((double)y - a[j] * (double)ac[(size_t)(k - j) * NS + s]);
+      ac[(size_t)k * NS + s] = y;
+    }
+  }
+}
+
+// IHC + lambda with the AC stage by the IIR recursion; mode as orc_ihc_lambda
+// (the AC itself is the reference arithmetic in every mode).
+void orc_ihc_lambda_iir(const float* v, int rows, int seg, int frdp, int total, int lam_rows,
+                        const double* b, const double* a, int n_iir, const double* dc_taps,
+                        int n_dc, double scale, double eta_ac, double eta_dc,
+                        const double* ihc_damage, const float* aihc, const float* spont,
+                        double lambda_sat, float* ihc, float* lam, int64_t lam_stride, int mode,
+                        float* ac_out) {
+  std::vector<float> ac((size_t)rows * NS);
+  orc_iir_ac(v, rows, seg, frdp, total, b, a, n_iir, scale, ac.data());
+  if (ac_out) std::copy(ac.begin(), ac.end(), ac_out);
+  ihc_lambda_impl(v, rows, seg, frdp, total, lam_rows, b, n_iir, dc_taps, n_dc, scale, eta_ac,
+                  eta_dc, ihc_damage, aihc, spont, lambda_sat, ihc, lam, lam_stride, mode,
+                  ac.data());
 }
 
 // ---------------------------------------------------------------------------

@@ -70,6 +70,12 @@ def load():
                                 _p, C.c_double, C.c_double, _p, _p, C.c_int]
         lib.orc_jnd_db.restype = C.c_double
         lib.orc_jnd_db.argtypes = [C.c_double, C.c_double, C.c_double]
+        lib.orc_iir_ac.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, _p, _p, C.c_int,
+                                   C.c_double, _p]
+        lib.orc_ihc_lambda_iir.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _p,
+                                           _p, C.c_int, _p, C.c_int, C.c_double, C.c_double,
+                                           C.c_double, _p, _p, _p, C.c_double, _p, _p, C.c_int64,
+                                           C.c_int, _p]
         lib.orc_ws_param_count.restype = C.c_int
         lib.orc_ws_forward_backward.argtypes = [_p, _p, _p, C.c_int, C.c_float, C.c_int, _p, _p,
                                                 _p]
@@ -201,3 +207,24 @@ def ws_forward_backward(params, feat, target, s_out, round_bf16=True, want_grad=
     load().orc_ws_forward_backward(_ptr(params), _ptr(feat), _ptr(target), n, s_out,
                                    1 if round_bf16 else 0, _ptr(out), _ptr(loss), _ptr(grad))
     return out, float(loss[0]), grad
+
+
+def ihc_lambda_iir(v, seg, frdp, total, lam_rows, b, a, dc_taps, scale, eta_ac, eta_dc,
+                   ihc_damage, aihc, spont, lambda_sat, mode=0):
+    """IHC/lambda with the AC stage by the reference's IIR recursion; returns
+    (ihc, lambda[3][lam_rows][256], ac[rows][256])."""
+    v = np.ascontiguousarray(v, np.float32)
+    rows = v.shape[0]
+    ihc = np.zeros((rows, 256), np.float32)
+    lam = np.zeros((3, lam_rows, 256), np.float32)
+    ac = np.zeros((rows, 256), np.float32)
+    b = np.ascontiguousarray(b, np.float64)
+    a = np.ascontiguousarray(a, np.float64)
+    dc = np.ascontiguousarray(dc_taps, np.float64)
+    load().orc_ihc_lambda_iir(_ptr(v), rows, seg, frdp, total, lam_rows, _ptr(b), _ptr(a), len(b),
+                              _ptr(dc), len(dc), scale, eta_ac, eta_dc,
+                              _ptr(np.ascontiguousarray(ihc_damage, np.float64)),
+                              _ptr(np.ascontiguousarray(aihc, np.float32)),
+                              _ptr(np.ascontiguousarray(spont, np.float32)), lambda_sat,
+                              _ptr(ihc), _ptr(lam), lam_rows, mode, _ptr(ac))
+    return ihc, lam, ac

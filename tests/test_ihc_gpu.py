@@ -75,3 +75,59 @@ def test_many_tiles_and_frames(stage):
 def test_empty_frame_table(stage):
     lam, _ = stage.run(np.zeros((10, 256), np.float32), np.zeros(0, ihc.FRAME_DTYPE), 4)
     assert not lam.any()
+
+
+def _oracle_iir(stage, v, fr, b, a, mode):
+    return orc.ihc_lambda_iir(v[fr["v_row0"]:fr["v_row0"] + fr["rows"]], int(fr["seg"]),
+                              int(fr["frdp"]), int(fr["total"]), int(fr["lam_rows"]),
+                              b.astype(np.float64), a.astype(np.float64),
+                              stage.dc.astype(np.float64), stage.nerve.scale,
+                              stage.nerve.eta_AC, stage.nerve.eta_DC,
+                              stage.dmg_host[fr["ihc_profile"]].astype(np.float64),
+                              stage.nerve.aihc(), np.asarray(stage.nerve.spontRate, np.float32),
+                              stage.nerve.Lambda_SAT, mode=mode)
+
+
+def _check_iir(stage, v, frames, lam_rows, b, a):
+    lam, ih, ac = stage.run_iir(v, frames, lam_rows, b, a, want_ihc=True)
+    for fr in frames:
+        r0, n, v0 = int(fr["lam_row0"]), int(fr["lam_rows"]), int(fr["v_row0"])
+        o_ihc, o_lam, o_ac = _oracle_iir(stage, v, fr, b, a, 2)
+        assert np.array_equal(ac[v0:v0 + n].view(np.uint32), o_ac[:n].view(np.uint32))
+        assert np.array_equal(ih[r0:r0 + n].view(np.uint32), o_ihc[:n].view(np.uint32))
+        assert np.array_equal(lam[:, r0:r0 + n].view(np.uint32), o_lam.view(np.uint32))
+        _, ref_lam, _ = _oracle_iir(stage, v, fr, b, a, 0)
+        for j in range(3):
+            d = np.abs(lam[j, r0:r0 + n] - ref_lam[j]).max() / np.abs(ref_lam[j]).max()
+            assert d <= REL, (j, d)
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_iir_ac_reference_run_frame(mv, stage, order):
+    """The AC stage by IIR (is_ac_iir_filter): AC, IHC and lambda bit-exact
+    against the oracle; lambda within the bar of the reference arithmetic."""
+    case = cases.decoupled_sweep(mv, n_signals=2, decouple=2, block_ms=1.5, overlap_ms=0.5)
+    cfg, sc, gamma, units, x, rows = case
+    v, _, _ = orc.bm_run(mv.section_params(), gamma, sc, units, x, rows)
+    fr = ihc.reference_frame(cfg)
+    v = v[:int(fr["rows"][0])]
+    b, a = ihc.design_ac_iir_lowpass(order=order)
+    _check_iir(stage, v, fr, int(fr["lam_rows"][0]), b, a)
+
+
+def test_iir_ac_frames_with_rule_switch(stage):
+    """Frames whose look-back rule switches to the frame total part-way (the
+    recursion must not be split there)."""
+    rng = np.random.default_rng(5)
+    t = np.arange(3600)[:, None] / 1e5
+    f = 300 + 40 * np.arange(256)[None, :]
+    v = (1e-3 * np.sin(2 * np.pi * f * t) * (1 + rng.random((1, 256)))).astype(np.float32)
+    frames = np.zeros(3, ihc.FRAME_DTYPE)
+    starts, lens = [0, 1000, 2500], [1000, 1500, 1100]
+    lam0 = 0
+    for i, (s, n) in enumerate(zip(starts, lens)):
+        frames[i] = (s, lam0, n, n - 100 if i == 2 else n, [500, 1500, 400][i],
+                     n if i < 2 else n - 100, ihc.round64(n), i % 2)
+        lam0 += frames[i]["lam_rows"]
+    b, a = ihc.design_ac_iir_lowpass(order=2)
+    _check_iir(stage, v, frames, lam0, b, a)
