@@ -686,10 +686,8 @@ extern "C" void generateInputFromProfile(
     float Max_Tol, int Relative_Error_Parameters, float M1_SP_Fix_Factor,
     float Tolerance_Fix_Factor, int Blocks_Per_Interval, int, float* fir_transfer_function,
     int fir_len, float* iir_transfer_function, int iir_len, Log&) {
-  const bool hearing_aid = fir_len > 1 || (fir_len > 0 && fir_transfer_function[0] != 1) ||
-                           iir_len > 1 || (iir_len > 0 && iir_transfer_function[0] != 1);
-  if (hearing_aid)
-    throw std::runtime_error("cochlea_gb300: hearing-aid transfer functions are not built");
+  const bool fir_on = fir_len > 1 || (fir_len > 0 && fir_transfer_function[0] != 1);
+  const bool iir_on = iir_len > 1 || (iir_len > 0 && iir_transfer_function[0] != 1);
   uploadProfiles(profiles, numOfProfiles, profilesLoaded);
   if (end_dc_expected == 0) end_dc_expected = IntervalLength;
   if (end_dc_normalized == 0) end_dc_normalized = IntervalLength;
@@ -727,6 +725,32 @@ extern "C" void generateInputFromProfile(
                               signal_mode, IntervalLength, JND_Interval_Head, Fs, H.wn_dc,
                               H.wn_norm, H.sig_dc, H.sig_norm, H.input, nullptr),
             "input generation");
+  if (fir_on || iir_on) {
+    // the reference runs the FIR stage whenever either function is active
+    // (src/cochlea.cu:4454-4503); the taps live in temporary device buffers
+    float* d_fir = nullptr;
+    float* d_iir = nullptr;
+    float* d_aux = nullptr;
+    const size_t n = (size_t)calculatedProfiles * IntervalLength;
+    gpu_check(cudaMalloc(&d_fir, std::max(fir_len, 1) * sizeof(float)), "hearing aid taps");
+    gpu_check(cudaMalloc(&d_iir, std::max(iir_len, 1) * sizeof(float)), "hearing aid taps");
+    gpu_check(cudaMalloc(&d_aux, n * sizeof(float)), "hearing aid buffer");
+    if (fir_len > 0)
+      gpu_check(cudaMemcpy(d_fir, fir_transfer_function, fir_len * sizeof(float),
+                           cudaMemcpyHostToDevice),
+                "upload hearing aid FIR");
+    if (iir_on)
+      gpu_check(cudaMemcpy(d_iir, iir_transfer_function, iir_len * sizeof(float),
+                           cudaMemcpyHostToDevice),
+                "upload hearing aid IIR");
+    const int rc = cgb_hearing_aid_dev(H.input, calculatedProfiles, IntervalLength, d_fir,
+                                       fir_len, d_iir, iir_on ? iir_len : 0, d_aux, nullptr);
+    gpu_check(cudaDeviceSynchronize(), "hearing aid");
+    cudaFree(d_fir);
+    cudaFree(d_iir);
+    cudaFree(d_aux);
+    cgb_check(rc, "hearing aid");
+  }
   gpu_check(cudaDeviceSynchronize(), "input generation");
   if (Show_Generated_Input & 1 && target_input)
     gpu_check(cudaMemcpy(target_input, H.input,

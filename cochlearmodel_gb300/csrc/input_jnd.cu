@@ -40,6 +40,37 @@ __global__ void input_gen_kernel(const cgb_profile* __restrict__ prof, int n_pro
   }
 }
 
+// Hearing-aid shaping of generated input (CudaProcessSignalTroughHearingAID
+// and ...IIR, src/cochlea.cu:4105-4150, applied at :4454-4503), per interval
+// of length L, position n, as float fma chains in tap order:
+//   aux[n] = sum_{i < min(n, Lf)} fir_i x[n-i]           (the first sample of
+//            each interval gets no term: the reference bounds by n, not n+1)
+//   out[n] = aux[n] + sum_{1 <= j < min(n+1, Li)} iir_j aux[n-j]
+// The second stage reads aux only (not its own output).  Positions past the
+// interval are not computed (the reference's grid can exceed the interval and
+// then races into the next profile).
+__global__ void hearing_aid_fir_kernel(const float* __restrict__ x, float* __restrict__ aux,
+                                       int L, const float* __restrict__ fir, int fir_len) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L) return;
+  const int64_t base = (int64_t)blockIdx.y * L;
+  const int back = min(n, fir_len);
+  float acc = 0.0f;
+  for (int i = 0; i < back; ++i) acc = __fmaf_rn(fir[i], x[base + n - i], acc);
+  aux[base + n] = acc;
+}
+
+__global__ void hearing_aid_iir_kernel(const float* __restrict__ aux, float* __restrict__ out,
+                                       int L, const float* __restrict__ iir, int iir_len) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L) return;
+  const int64_t base = (int64_t)blockIdx.y * L;
+  const int back = min(n + 1, iir_len);
+  float acc = aux[base + n];
+  for (int j = 1; j < back; ++j) acc = __fmaf_rn(iir[j], aux[base + n - j], acc);
+  out[base + n] = acc;
+}
+
 constexpr int kJndSections = 256;
 constexpr int kJndGroups = 4;   // row groups per CTA (threads = 4 x 256)
 constexpr int kJndThreads = kJndSections * kJndGroups;
@@ -210,6 +241,32 @@ extern "C" int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, in
                                            d_ref_of, d_nihc, (double)W[0], (double)W[1],
                                            (double)W[2], Fs, T, d_F_RA, d_F_AI, d_MR, n_int);
   CGB_TRY_CUDA(cudaGetLastError(), "jnd_kernel launch");
+  note_launch();
+  return CGB_OK;
+}
+
+extern "C" int cgb_hearing_aid_dev(float* d_in, int n_prof, int interval_len,
+                                   const float* d_fir, int fir_len, const float* d_iir,
+                                   int iir_len, float* d_aux, void* stream) {
+  using namespace cgb;
+  if (n_prof == 0 || interval_len == 0) return CGB_OK;
+  if (!d_in || !d_aux || n_prof < 0 || interval_len < 0 || fir_len < 0 || iir_len < 0 ||
+      (fir_len > 0 && !d_fir) || (iir_len > 0 && !d_iir))
+    return fail(CGB_ERR_ARG, "cgb_hearing_aid_dev: bad arguments");
+  if (n_prof > 65535) return fail(CGB_ERR_RANGE, "cgb_hearing_aid_dev: more than 65535 profiles");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  dim3 grid((unsigned)((interval_len + 255) / 256), (unsigned)n_prof);
+  hearing_aid_fir_kernel<<<grid, 256, 0, st>>>(d_in, d_aux, interval_len, d_fir, fir_len);
+  CGB_TRY_CUDA(cudaGetLastError(), "hearing_aid_fir_kernel launch");
+  note_launch();
+  if (iir_len > 0) {
+    hearing_aid_iir_kernel<<<grid, 256, 0, st>>>(d_aux, d_in, interval_len, d_iir, iir_len);
+    CGB_TRY_CUDA(cudaGetLastError(), "hearing_aid_iir_kernel launch");
+  } else {
+    CGB_TRY_CUDA(cudaMemcpyAsync(d_in, d_aux, (size_t)n_prof * interval_len * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, st),
+                 "hearing aid copy-back");
+  }
   note_launch();
   return CGB_OK;
 }

@@ -190,14 +190,28 @@ int main(int argc, char** argv) {
       for (int i = 0; i < L && i < (int)v.size(); ++i) noise[i] = v[i];
     }
     std::vector<float> signal(L, 0.0f);
+    // hearing-aid transfer functions (src/params.cpp:1401-1413: the IIR vector
+    // is stored negated with element 0 = 1)
+    std::vector<float> ha_fir(1, 1.0f), ha_iir(1, 1.0f);
+    {
+      const auto fv = P.vec("Hearing_AID_FIR_Transfer_Function", {});
+      if (!fv.empty()) ha_fir.assign(fv.begin(), fv.end());
+      const auto iv = P.vec("Hearing_AID_IIR_Transfer_Function", {});
+      if (!iv.empty()) {
+        ha_iir.assign(iv.size(), 0.0f);
+        for (size_t i = 0; i < iv.size(); ++i) ha_iir[i] = -1.0f * (float)iv[i];
+        ha_iir[0] = 1.0f;
+      }
+    }
     InputProfilesArrayInitialization(n_int, L, L, 0, 0);
     generateInputFromProfile(prof.data(), noise.data(), L, signal.data(), L, 0,
                              (int)P.num("Normalize_Sigma_Type", 3),
                              (int)P.num("Normalize_Sigma_Type_Signal", 3), 0.16, 0.0, 0, 0, 0, 0,
                              n_int, false, 0, n_int, overlap, L, 0, L, (float)Fs, 0, nullptr,
                              false, true, (float)P.num("MAX_M1_SP_ERROR", 1e-15),
-                             (float)P.num("MAX_TOLERANCE", 1e-10), 0, 0.0f, 0.0f, D, 0, nullptr,
-                             0, nullptr, 0, log);
+                             (float)P.num("MAX_TOLERANCE", 1e-10), 0, 0.0f, 0.0f, D, 0,
+                             ha_fir.data(), (int)ha_fir.size(), ha_iir.data(),
+                             (int)ha_iir.size(), log);
 
     // BM solver
     cudaEvent_t e0{}, e1{};

@@ -68,7 +68,8 @@ class ProfileRun:
 
     def __init__(self, device, cfg: RunConfig, sweep: ProfileSweep, noise: np.ndarray | None = None,
                  nerve: NerveConfig | None = None, jnd: JNDWindow | None = None,
-                 mv: ModelVectors | None = None, ac_taps=None, want_lambda=True):
+                 mv: ModelVectors | None = None, ac_taps=None, want_lambda=True,
+                 hearing_aid=None):
         import torch
         from .solver import BMSolver, units_to_device
         self.torch = torch
@@ -123,6 +124,21 @@ class ProfileRun:
             self.d_FRA = torch.zeros((3, self.n_int), dtype=torch.float64, device=self.device)
             self.d_FAI = torch.zeros((3, self.n_int), dtype=torch.float64, device=self.device)
         self.calc_jnd = sweep.calculate_jnd
+        # hearing-aid transfer functions (fir, iir), applied to the generated
+        # input when either is not the identity (src/cochlea.cu:4454-4503);
+        # iir holds the reference's stored form (-a with element 0 = 1)
+        self.ha = None
+        if hearing_aid is not None:
+            fir, iir = (np.atleast_1d(np.asarray(t, np.float32)) for t in hearing_aid)
+            active = len(fir) > 1 or (len(fir) > 0 and fir[0] != 1) or \
+                len(iir) > 1 or (len(iir) > 0 and iir[0] != 1)
+            if active:
+                iir_on = len(iir) > 1 or (len(iir) > 0 and iir[0] != 1)
+                self.ha = (torch.from_numpy(fir.copy()).to(self.device), len(fir),
+                           torch.from_numpy(iir.copy()).to(self.device) if iir_on else None,
+                           len(iir) if iir_on else 0,
+                           torch.zeros(self.n_int * self.L, dtype=torch.float32,
+                                       device=self.device))
 
     @property
     def audio_seconds(self) -> float:
@@ -137,6 +153,11 @@ class ProfileRun:
             native.ptr(self.d_prof), self.n_int, native.ptr(self.d_wn), None, 0, self.L, 0,
             float(self.cfg.Fs), self.wn_dc, self.wn_norm, 0.0, self.sig_norm,
             native.ptr(self.d_in), self._stream(stream)), "cgb_input_gen_dev")
+        if self.ha is not None:
+            fir, nf, iir, ni, aux = self.ha
+            native.check(self.lib.cgb_hearing_aid_dev(
+                native.ptr(self.d_in), self.n_int, self.L, native.ptr(fir), nf, native.ptr(iir),
+                ni, native.ptr(aux), self._stream(stream)), "cgb_hearing_aid_dev")
 
     def solve_bm(self, stream=None):
         self.bm.run_dev(self.sc, self.d_gamma, self.d_units, len(self.units), self.d_in,

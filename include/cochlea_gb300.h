@@ -329,6 +329,17 @@ int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, int interval_
                 const float* W, double Fs, double delta_alpha_len_factor, double* d_F_RA,
                 double* d_F_AI, double* d_MR, void* stream);
 
+/* Hearing-aid shaping of the generated input (the reference's
+ * CudaProcessSignalTroughHearingAID / ...IIR, src/cochlea.cu:4105-4150), in
+ * place on d_in float[n_prof][interval_len], per interval position n:
+ *   aux[n] = sum_{i < min(n, fir_len)} fir_i x[n-i]
+ *   out[n] = aux[n] + sum_{1 <= j < min(n+1, iir_len)} iir_j aux[n-j]
+ * (iir_len 0: out = aux).  d_fir / d_iir are device taps; d_aux is a
+ * scratch of the same size as d_in.  The reference runs this only when a
+ * transfer function is not the identity; the caller decides that. */
+int cgb_hearing_aid_dev(float* d_in, int n_prof, int interval_len, const float* d_fir,
+                        int fir_len, const float* d_iir, int iir_len, float* d_aux, void* stream);
+
 /* One interval of cgb_jnd_batch_dev (rows index each lambda plane). */
 typedef struct cgb_jnd_interval {
   int64_t row;      /* first row of the interval's window                   */

@@ -827,6 +827,34 @@ void orc_ihc_lambda(const float* v, int rows, int seg, int frdp, int total, int 
                   nullptr);
 }
 
+// Hearing-aid shaping (CudaProcessSignalTroughHearingAID and ...IIR,
+// src/cochlea.cu:4105-4150): per interval of length L,
+//   aux[n] = fma chain over i < min(n, fir_len) of fir[i] x[n-i], from 0;
+//   out[n] = fma chain over 1 <= j < min(n+1, iir_len) of iir[j] aux[n-j],
+//            from aux[n]  (iir_len 0: out = aux).
+void orc_hearing_aid(const float* x, int n_prof, int L, const float* fir, int fir_len,
+                     const float* iir, int iir_len, float* out) {
+  std::vector<float> aux((size_t)n_prof * L);
+  for (int p = 0; p < n_prof; ++p)
+    for (int n = 0; n < L; ++n) {
+      const float* xs = x + (size_t)p * L;
+      const int back = std::min(n, fir_len);
+      float acc = 0.0f;
+      for (int i = 0; i < back; ++i) acc = fmaf(fir[i], xs[n - i], acc);
+      aux[(size_t)p * L + n] = acc;
+    }
+  for (int p = 0; p < n_prof; ++p)
+    for (int n = 0; n < L; ++n) {
+      const float* as = aux.data() + (size_t)p * L;
+      float acc = as[n];
+      if (iir_len > 0) {
+        const int back = std::min(n + 1, iir_len);
+        for (int j = 1; j < back; ++j) acc = fmaf(iir[j], as[n - j], acc);
+      }
+      out[(size_t)p * L + n] = acc;
+    }
+}
+
 // AC by the reference's IIR recursion (DeviceCudaIIRFilter, src/cochlea.cu:2745-2775):
 //   Y[k] = sum_{i<ob} b_i X[k-i] - sum_{1<=j<ob} a_j Y[k-j],  ob = the FIR look-back
 // bound, accumulated in float with each term added in double and rounded

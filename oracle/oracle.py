@@ -76,6 +76,7 @@ def load():
                                            _p, C.c_int, _p, C.c_int, C.c_double, C.c_double,
                                            C.c_double, _p, _p, _p, C.c_double, _p, _p, C.c_int64,
                                            C.c_int, _p]
+        lib.orc_hearing_aid.argtypes = [_p, C.c_int, C.c_int, _p, C.c_int, _p, C.c_int, _p]
         lib.orc_ws_param_count.restype = C.c_int
         lib.orc_ws_forward_backward.argtypes = [_p, _p, _p, C.c_int, C.c_float, C.c_int, _p, _p,
                                                 _p]
@@ -228,3 +229,14 @@ def ihc_lambda_iir(v, seg, frdp, total, lam_rows, b, a, dc_taps, scale, eta_ac, 
                               _ptr(np.ascontiguousarray(spont, np.float32)), lambda_sat,
                               _ptr(ihc), _ptr(lam), lam_rows, mode, _ptr(ac))
     return ihc, lam, ac
+
+
+def hearing_aid(x, fir, iir):
+    """Hearing-aid shaping of float[n_prof][L] input (reference semantics)."""
+    x = np.ascontiguousarray(x, np.float32)
+    fir = np.ascontiguousarray(fir, np.float32)
+    iir = np.ascontiguousarray(iir, np.float32)
+    out = np.zeros_like(x)
+    load().orc_hearing_aid(_ptr(x), x.shape[0], x.shape[1], _ptr(fir), len(fir), _ptr(iir),
+                           len(iir), _ptr(out))
+    return out
