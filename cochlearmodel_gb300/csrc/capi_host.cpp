@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "cgb_internal.h"
 
@@ -171,3 +172,76 @@ int cgb_check_units(const cgb_unit* units, int n_units, int n_profiles, int64_t 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Complex-JND aggregation (ComplexJNDProfile::calculateMinValue and
+// ::calculateGradientMinMaxValue, src/ComplexJNDProfile.cpp:19-100, run by
+// AudioGramCreator::calcComplexJND, src/AudioGramCreator.cpp:548-571).  Each
+// profile lists, per tested power level, the index of its interval among the
+// calculated intervals; its JND values across the levels are reduced to one:
+//   method 0: the last strict local minimum inside the sequence; with none,
+//             the first value if it is below the second, else the last if it
+//             is below the one before (warning 1);
+//   method 1: the first value whose successor exceeds it by more than eps;
+//             with none, the first value (warning 1).
+// failed: per calculated interval, its failed-convergence count; out_failed
+// receives the count of the chosen interval.  Where the reference reads
+// outside its vectors (no minimum captured: an empty vector; one level: the
+// second element) or leaves a stale value (no boundary below its neighbour),
+// this returns the count at the chosen index, takes a single level as its
+// own value (warning 1), and returns NaN (warning 1) respectively.
+// ---------------------------------------------------------------------------
+extern "C" int cgb_complex_jnd(const double* values, int n_values, const int32_t* failed,
+                               const int32_t* intervals, int n_profiles, int n_levels,
+                               int method, float eps, float* out_value, int32_t* out_warning,
+                               int32_t* out_failed) {
+  using namespace cgb;
+  if (!values || !intervals || !out_value || !out_warning || !out_failed || n_values < 0 ||
+      n_profiles < 0 || n_levels < 1 || (method != 0 && method != 1))
+    return fail(CGB_ERR_ARG, "cgb_complex_jnd: bad arguments");
+  std::vector<double> rel(n_levels);
+  std::vector<int32_t> fl(n_levels);
+  for (int p = 0; p < n_profiles; ++p) {
+    for (int l = 0; l < n_levels; ++l) {
+      const int idx = intervals[(size_t)p * n_levels + l];
+      if (idx < 0 || idx >= n_values)
+        return fail(CGB_ERR_RANGE, "cgb_complex_jnd: interval index outside the values");
+      rel[l] = values[idx];
+      fl[l] = failed ? failed[idx] : 0;
+    }
+    float value = NAN;
+    int32_t warning = 0, fc = 0;
+    if (method == 0) {
+      int chosen = -1;
+      for (int i = 1; i + 1 < n_levels; ++i)
+        if (rel[i] < rel[i - 1] && rel[i] < rel[i + 1]) chosen = i;  // keeps the last
+      if (chosen < 0) {
+        warning = 1;
+        if (n_levels == 1) chosen = 0;
+        else if (rel[0] < rel[1]) chosen = 0;
+        else if (rel[n_levels - 1] < rel[n_levels - 2]) chosen = n_levels - 1;
+      }
+      if (chosen >= 0) {
+        value = (float)rel[chosen];
+        fc = fl[chosen];
+      }
+    } else {
+      int chosen = -1;
+      for (int i = 0; i + 1 < n_levels; ++i)
+        if (rel[i + 1] - rel[i] > (double)eps) {
+          chosen = i;
+          break;
+        }
+      if (chosen < 0) {
+        chosen = 0;
+        warning = 1;
+      }
+      value = (float)rel[chosen];
+      fc = fl[chosen];
+    }
+    out_value[p] = value;
+    out_warning[p] = warning;
+    out_failed[p] = fc;
+  }
+  return CGB_OK;
+}

@@ -26,16 +26,52 @@ class ProfileSweep:
     noises: list = field(default_factory=lambda: [1111.0])  # 1111 = no noise
     calculate_jnd: bool = False
     spl_ref: float = 2e-5
+    # complex-JND profile adjustments, indexed by profile n_freq * noise + freq
+    # (Complex_Profile_Power_Level_Divisor / _Noise_Level_Fix_Factor /
+    # _Noise_Level_Fix_Addition); missing entries count as 0
+    power_divisor: list = field(default_factory=list)
+    noise_fix_factor: list = field(default_factory=list)
+    noise_fix_addition: list = field(default_factory=list)
+
+    def signal_db(self, nlevel: int, plevel: int, flevel: int) -> float:
+        """The tested signal level (src/params.cpp:700-711), in float."""
+        cid = len(self.frequencies) * nlevel + flevel
+        get = lambda v: F32(v[cid]) if cid < len(v) else F32(0.0)
+        noise = F32(self.noises[nlevel])
+        base = F32(self.powers[plevel])
+        div = get(self.power_divisor)
+        if div != 0 and noise != F32(1111.0) and noise > 0:
+            p0 = F32(self.powers[0])
+            base = F32(p0 + F32(F32(F32(base - p0) * div) / noise))
+        if noise != F32(1111.0):
+            base = F32(base + F32(F32(get(self.noise_fix_factor) * noise) +
+                                  get(self.noise_fix_addition)))
+        return float(base)
+
+    def complex_intervals(self) -> np.ndarray:
+        """int32[n_noise * n_freq][n_power]: per complex profile (noise, freq),
+        the calculated-interval index of each tested power level
+        (ComplexJNDProfile::setInterval, src/params.cpp:723-729)."""
+        nf, npw = len(self.frequencies), len(self.powers)
+        out = np.zeros((len(self.noises) * nf, npw), np.int32)
+        idx = 0
+        for nl in range(len(self.noises)):
+            for pl in range(npw):
+                for fl in range(nf):
+                    out[nl * nf + fl, pl] = idx
+                    idx += 1
+        return out
 
     def build(self):
         """Returns (profiles PROFILE_DTYPE[n], is_reference bool[n], ref_of int32[n])."""
         prof, is_ref, ref_of = [], [], []
-        for nl in self.noises:
+        for nli, nl in enumerate(self.noises):
             wn = spl_to_amplitude(float(nl), self.spl_ref)
             first = len(prof)
-            for pl in self.powers:
-                for f in self.frequencies:
-                    prof.append((spl_to_amplitude(float(pl), self.spl_ref), wn, float(f)))
+            for pli in range(len(self.powers)):
+                for fli, f in enumerate(self.frequencies):
+                    db = self.signal_db(nli, pli, fli)
+                    prof.append((spl_to_amplitude(db, self.spl_ref), wn, float(f)))
                     is_ref.append(False)
             if self.calculate_jnd:
                 prof.append((0.0, wn, 0.0))
@@ -46,6 +82,25 @@ class ProfileSweep:
                 ref_of += list(range(first, len(prof)))
         p = np.array(prof, dtype=native.PROFILE_DTYPE)
         return p, np.array(is_ref), np.array(ref_of, np.int32)
+
+
+def complex_jnd(values, intervals, method: int = 0, eps: float = 0.0, failed=None):
+    """Complex-JND aggregation (cgb_complex_jnd): per complex profile, one
+    value from its JND values across the tested power levels.  values: per
+    calculated interval (dB); intervals: ProfileSweep.complex_intervals().
+    Returns (value float32[n], warning int32[n], failed int32[n])."""
+    lib = native.load()
+    values = np.ascontiguousarray(values, np.float64)
+    intervals = np.ascontiguousarray(intervals, np.int32)
+    n, m = intervals.shape
+    fl = None if failed is None else np.ascontiguousarray(failed, np.int32)
+    val = np.zeros(n, np.float32)
+    warn = np.zeros(n, np.int32)
+    fo = np.zeros(n, np.int32)
+    native.check(lib.cgb_complex_jnd(native.ptr(values), len(values), native.ptr(fl),
+                                     native.ptr(intervals), n, m, method, eps, native.ptr(val),
+                                     native.ptr(warn), native.ptr(fo)), "cgb_complex_jnd")
+    return val, warn, fo
 
 
 @dataclass
@@ -184,6 +239,15 @@ class ProfileRun:
             self.ihc_lambda(stream)
         if self.calc_jnd:
             self.jnd_sums(stream)
+
+    def failed_per_interval(self) -> np.ndarray:
+        """Failed-convergence count of each tested interval: the failed
+        samples of its Decouple_Filter blocks (calcJNDFinal,
+        src/AudioGramCreator.cpp:489-493), in calculated-interval order."""
+        st = self.d_stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
+        D = self.cfg.Decouple_Filter
+        per = st["failed_samples"].reshape(self.n_int, D).sum(axis=1).astype(np.int32)
+        return per[~self.is_ref]
 
     def jnd_db(self):
         F_RA = self.d_FRA.cpu().numpy()

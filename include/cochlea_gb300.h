@@ -359,6 +359,18 @@ int cgb_jnd_batch_dev(const float* d_lam, int64_t plane_rows, const cgb_jnd_inte
                       double delta_alpha_len_factor, double* d_F_RA, double* d_F_AI,
                       double* d_MR, void* stream);
 
+/* Complex-JND aggregation (ComplexJNDProfile, src/ComplexJNDProfile.cpp:19-100):
+ * per profile, the JND values of its intervals across the tested power levels
+ * (intervals int32[n_profiles][n_levels]: indexes into values/failed, the
+ * calculated intervals) reduce to one value -- method 0: the last strict
+ * interior local minimum (else a lower boundary value, warning 1); method 1:
+ * the first value whose successor exceeds it by more than eps (else the
+ * first, warning 1).  Outputs per profile: value (NaN where the reference
+ * has none), warning, failed-convergence count of the chosen interval. */
+int cgb_complex_jnd(const double* values, int n_values, const int32_t* failed,
+                    const int32_t* intervals, int n_profiles, int n_levels, int method,
+                    float eps, float* out_value, int32_t* out_warning, int32_t* out_failed);
+
 /* Final JND in dB SPL per interval from the Fisher sums (host arrays):
  * 20 log10((1/sqrt(sum_j F_j)) / spl_ref), bounded at max_db; NaN for
  * reference intervals. */
