@@ -81,6 +81,47 @@ def design_ac_lowpass(fc: float = 800.0, fs: float = 100000.0, ntaps: int = 255)
     return h.astype(np.float32)
 
 
+def design_ac_equiripple(fpass: float = 800.0, fstop: float = 1600.0, fs: float = 100000.0,
+                         num_taps: int = 255, weight_pass: float = 1.0,
+                         weight_stop: float = 10.0):
+    """Equiripple (Parks-McClellan) AC low-pass: the design the reference
+    makes with firpm for an "equiripple" AC filter (src/SubModel.cpp:147-149,
+    pass band to fpass, stop band from fstop, weights {pass, stop}), unit DC
+    gain.  Returns (taps float32, weighted ripple)."""
+    lib = native.load()
+    nyq = fs / 2.0
+    taps = np.zeros(num_taps, np.float64)
+    delta = np.zeros(1, np.float64)
+    native.check(lib.cgb_design_equiripple_lowpass(num_taps, fpass / nyq, (fstop - fpass) / nyq,
+                                                   weight_pass, weight_stop, native.ptr(taps),
+                                                   native.ptr(delta), None),
+                 "cgb_design_equiripple_lowpass")
+    return taps.astype(np.float32), float(delta[0])
+
+
+def design_ac_from_spec(fpass: float, fstop: float, fs: float = 100000.0,
+                        apass_db: float = 1.0, astop_db: float = 60.0, num_taps=None):
+    """The reference's equiripple AC design from a pass/stop specification
+    (SubModel::analyzeACFilter, src/SubModel.cpp:150-240): ripples
+    10^(-A/20), the minimum order of Oppenheim & Schafer eq. 7.104
+    (calcMinimumOrder, :143-146) when num_taps is not given, stop weight 10
+    and pass weight max(0.01, 10 deltaStop / deltaPass) (with the stop weight
+    raised when the floor applies), then the equiripple design with unit DC
+    gain.  The reference's further searches (frequency-error correction and
+    band-edge search) are not reproduced.  Returns (taps float32, ripple)."""
+    nyq = fs / 2.0
+    dp = 10.0 ** (-apass_db / 20.0)
+    ds = 10.0 ** (-astop_db / 20.0)
+    pw = (fstop - fpass) / nyq
+    if num_taps is None:
+        num_taps = int(math.ceil((-10.0 * math.log10(dp * ds) - 13.0) / (2.324 * pw * math.pi)))
+    ws = 10.0
+    wp = max(0.01, 10.0 * ds / dp)
+    if wp > 10.0 * ds / dp:
+        ws = ws * (wp / (10.0 * ds / dp))
+    return design_ac_equiripple(fpass, fstop, fs, int(num_taps), wp, ws)
+
+
 def design_ac_iir_lowpass(fc: float = 800.0, fs: float = 100000.0, order: int = 2):
     """AC low-pass IIR for the reference's is_ac_iir_filter path: a Butterworth
     low-pass of even `order`, by the bilinear transform with the cutoff

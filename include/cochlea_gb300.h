@@ -359,6 +359,17 @@ int cgb_jnd_batch_dev(const float* d_lam, int64_t plane_rows, const cgb_jnd_inte
                       double delta_alpha_len_factor, double* d_F_RA, double* d_F_AI,
                       double* d_MR, void* stream);
 
+/* Equiripple low-pass FIR for the AC filter (the design problem the
+ * reference hands to firpm in SubModel::calcFIRPM, src/SubModel.cpp:147-149):
+ * Parks-McClellan / Remez exchange over the pass band [0, omega_c] (weight
+ * weight_pass) and stop band [omega_c + transition, 1] (weight weight_stop),
+ * frequencies normalised to Nyquist = 1; num_taps odd or even (3..4096);
+ * taps double[num_taps] scaled to unit DC gain (fixDCGain).  delta_out:
+ * the weighted ripple; iterations: exchanges used (both may be null). */
+int cgb_design_equiripple_lowpass(int num_taps, double omega_c, double transition,
+                                  double weight_pass, double weight_stop, double* taps,
+                                  double* delta_out, int* iterations);
+
 /* Complex-JND aggregation (ComplexJNDProfile, src/ComplexJNDProfile.cpp:19-100):
  * per profile, the JND values of its intervals across the tested power levels
  * (intervals int32[n_profiles][n_levels]: indexes into values/failed, the
