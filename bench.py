@@ -407,15 +407,21 @@ def run_ours(args, rank, world, device):
     h_outs = [torch.empty(o.shape, dtype=o.dtype).pin_memory() for o in outs]
     e_steps = max(1, args.steps // 2)
     e_ms = 0.0
+    overlapped = hasattr(run, "step_host")
+    if overlapped:  # the JND sweep overlaps the result copies with compute
+        run.step_host(h_tables, h_outs[0], h_outs[1])  # uploads its chunk tables
     for i in range(e_steps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize(device)
         a.record(stream)
-        for d_t, h_t in zip(tables, h_tables):
-            d_t.copy_(h_t, non_blocking=True)
-        run.step()
-        for h_o, d_o in zip(h_outs, outs):
-            h_o.copy_(d_o, non_blocking=True)
+        if overlapped:
+            run.step_host(h_tables, h_outs[0], h_outs[1])
+        else:
+            for d_t, h_t in zip(tables, h_tables):
+                d_t.copy_(h_t, non_blocking=True)
+            run.step()
+            for h_o, d_o in zip(h_outs, outs):
+                h_o.copy_(d_o, non_blocking=True)
         b.record(stream)
         torch.cuda.synchronize(device)
         e_ms += a.elapsed_time(b)

@@ -72,3 +72,23 @@ def test_units_longest_first(sweep):
     b, _ = sweep
     span = b.units["end"] - b.units["start"]
     assert (np.diff(span) <= 0).all()
+
+
+def test_step_host_equals_step_and_copies(sweep):
+    """The host-buffer step with copies overlapped on a second stream returns
+    exactly what step() followed by plain copies returns."""
+    import torch
+    b, _ = sweep
+    h_tables = [pg["d_prof"].cpu().pin_memory() for pg in b.per_group]
+    b.step()
+    torch.cuda.synchronize()
+    v0, lam0, f0 = b.d_v.cpu(), b.d_lam.cpu(), b.d_FRA.clone()
+    h_v = torch.empty(b.d_v.shape, dtype=torch.float32).pin_memory()
+    h_lam = torch.empty(b.d_lam.shape, dtype=torch.float32).pin_memory()
+    for chunks in (1, 3):
+        h_v.zero_()
+        h_lam.zero_()
+        b.step_host(h_tables, h_v, h_lam, chunks=chunks)
+        torch.cuda.synchronize()
+        assert torch.equal(h_v, v0) and torch.equal(h_lam, lam0)
+        assert torch.equal(b.d_FRA, f0)
