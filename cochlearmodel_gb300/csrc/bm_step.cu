@@ -87,6 +87,27 @@ __device__ __forceinline__ void store8p(float* p, const float2 (&r)[4]) {
   reinterpret_cast<float4*>(p)[1] = make_float4(r[0].y, r[1].y, r[2].y, r[3].y);
 }
 
+// Shared-memory copies of per-section vectors are kept in pair order: within
+// each group of eight sections the order is 0,4,1,5,2,6,3,7, so a lane's two
+// 16-byte loads land as whole register pairs (no repacking moves).
+__device__ __forceinline__ int pair_pos(int s) {
+  return (s & ~7) | ((s & 3) << 1) | ((s >> 2) & 1);
+}
+
+__device__ __forceinline__ void load8q(const float* p, float2 (&r)[4]) {
+  const float4 a = reinterpret_cast<const float4*>(p)[0];
+  const float4 b = reinterpret_cast<const float4*>(p)[1];
+  r[0] = f2(a.x, a.y);
+  r[1] = f2(a.z, a.w);
+  r[2] = f2(b.x, b.y);
+  r[3] = f2(b.z, b.w);
+}
+
+__device__ __forceinline__ void store8q(float* p, const float2 (&r)[4]) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(r[0].x, r[0].y, r[1].x, r[1].y);
+  reinterpret_cast<float4*>(p)[1] = make_float4(r[2].x, r[2].y, r[3].x, r[3].y);
+}
+
 // pairs -> sections 8l..8l+7 in order
 __device__ __forceinline__ void unpair(const float2 (&r)[4], float (&o)[kSPL]) {
 #pragma unroll
@@ -118,11 +139,11 @@ struct PrevState {
       for (int k = 0; k < 4; ++k) r[j][k] = f2b(0.0f);
     if (PREV_SMEM)
 #pragma unroll
-      for (int j = 0; j < 7; ++j) store8p(sm + j * 256 + base, r[j]);
+      for (int j = 0; j < 7; ++j) store8q(sm + j * 256 + base, r[j]);
   }
   __device__ __forceinline__ void load(int j, int base, float2 (&o)[4]) const {
     if (PREV_SMEM) {
-      load8p(sm + j * 256 + base, o);
+      load8q(sm + j * 256 + base, o);
     } else {
 #pragma unroll
       for (int k = 0; k < 4; ++k) o[k] = r[j][k];
@@ -130,7 +151,7 @@ struct PrevState {
   }
   __device__ __forceinline__ void store(int j, int base, const float2 (&o)[4]) {
     if (PREV_SMEM) {
-      store8p(sm + j * 256 + base, o);
+      store8q(sm + j * 256 + base, o);
     } else {
 #pragma unroll
       for (int k = 0; k < 4; ++k) r[j][k] = o[k];
@@ -139,7 +160,8 @@ struct PrevState {
 };
 
 // One unit, executed by one full warp.  sp: shared [8][256] section
-// parameters; sg / sgs: shared gamma and gamma*S_ohc of the unit's profile.
+// parameters; sg / sgs: shared gamma and gamma*S_ohc of the unit's profile
+// (all three in pair order, as are the previous-step slice and hist).
 // The per-section arithmetic runs on section pairs (two-wide FP32), each
 // element rounding as the scalar sequence the CPU oracle evaluates.
 //
@@ -160,11 +182,33 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
                                          const unsigned char* wblob, int lane,
                                          cgb_unit_stats* st) {
   const int base = lane * kSPL;
+  const bool first = lane == 0, last = lane == 31;
   float2 rm[4];
-  load8p(sp + 1 * 256 + base, rm);
+  load8q(sp + 1 * 256 + base, rm);
   // 1/m of the halo sections 8l-1 and 8l+8 (used by the paired sweeps)
-  const float rmL = __shfl_up_sync(kFull, rm[3].y, 1);
+  float rmL = __shfl_up_sync(kFull, rm[3].y, 1);
   const float rmR = __shfl_down_sync(kFull, rm[0].x, 1);
+  // Boundary sections without per-sweep fix-ups (reference schedule and
+  // tolerance mode with the previous or extrapolated guess).  There the
+  // pressure of section 255 is +0 at every point: Y_255 = 0 and its update
+  // only sees p_256 = 0.  So (a) the left halo is shuffled with wrap-around,
+  // and lane 0 reads p_255 = +0 as p_{-1}; (b) lane 0's halo section -1 gets
+  // coefficient 0 and right-hand side +0 (from Yrm_255), so its update is +0;
+  // (c) section 255's coefficient is 0, so its update is +0 whatever its
+  // (finite) neighbours; (d) section 254's lower neighbour enters through
+  // fma(0, p_253, p_255) = +0 = p_255.  Each value equals the fixed-up
+  // sequence bit for bit.  The learned guess can leave p_255 != 0 before the
+  // first sweep, so it keeps the explicit fix-ups.
+  constexpr bool kWrap = TOL != 2;
+  const int src_l = (lane + 31) & 31;
+  float2 lo2 = f2b(1.0f);
+  if (kWrap) {
+    if (first) rmL = 0.0f;
+    if (last) {
+      rm[3].y = 0.0f;
+      lo2.y = 0.0f;
+    }
+  }
 
   PrevState<PREV_SMEM> prev;
   prev.init(prev_slice, base);
@@ -192,7 +236,6 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   int n_failed = 0, n_written = 0, status = 0, sub_in_sample = 0;
   float smp_dt = 0.0f, smp_sub = 0.0f, smp_it = 0.0f;  // per-sample sums
   float dt_prev = dt, rho = 1.0f;
-  const bool first = lane == 0, last = lane == 31;
 
   while (n < un.end) {
     if (++sub_in_sample > A.max_sub) {  // dt collapsed: stop this unit, flag it
@@ -205,7 +248,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // of this step, the other slot holds the start of the previous one
       rho = __fdiv_rn(dt, dt_prev);
       dt_prev = dt;
-      store8p(hist + (n_sub & 1) * 256 + base, p);
+      store8q(hist + (n_sub & 1) * 256 + base, p);
     }
     const float delta = (float)(tau * A.invts);
     const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
@@ -254,15 +297,15 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       const bool tm_update = out_loop < 2;
       {
         float2 Stm[4], Rtm[4], gs[4], Rs[4], Ss[4], Qs[4];
-        load8p(sp + 6 * 256 + base, Stm);
-        load8p(sp + 7 * 256 + base, Rtm);
-        load8p(sgs + base, gs);
-        load8p(sp + 2 * 256 + base, Rs);
-        load8p(sp + 3 * 256 + base, Ss);
-        load8p(sp + 4 * 256 + base, Qs);
+        load8q(sp + 6 * 256 + base, Stm);
+        load8q(sp + 7 * 256 + base, Rtm);
+        load8q(sgs + base, gs);
+        load8q(sp + 2 * 256 + base, Rs);
+        load8q(sp + 3 * 256 + base, Ss);
+        load8q(sp + 4 * 256 + base, Qs);
         if (tm_update) {
           float2 gm[4];
-          load8p(sg + base, gm);
+          load8q(sg + base, gm);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const float2 d = sub2(y[k], x[k]);
@@ -301,11 +344,12 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // second on its own sections, so one shuffle round serves two sweeps.
       // Sections 254 and 255 carry no lower coefficient; p_{-1} = p_256 = 0.
       const int J = TOL ? A.jcap : (tm_update ? A.jslow : A.jfast);
-      const float YrmL = __shfl_up_sync(kFull, Yrm[3].y, 1);
+      const float YrmL = kWrap ? __shfl_sync(kFull, Yrm[3].y, src_l)
+                               : __shfl_up_sync(kFull, Yrm[3].y, 1);
       const float YrmR = __shfl_down_sync(kFull, Yrm[0].x, 1);
       if (TOL && out_loop == 0 && n_sub >= 2) {
         float2 p2[4];
-        load8p(hist + ((n_sub + 1) & 1) * 256 + base, p2);
+        load8q(hist + ((n_sub + 1) & 1) * 256 + base, p2);
         if (A.log && n_sub % A.log_every == 0) {
           int idx = 0;
           if (lane == 0) idx = atomicAdd(A.log_count, 1);
@@ -349,34 +393,52 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       }
       int it = 0;
       for (; it + 1 < J; it += 2) {
-        const float L1 = __shfl_up_sync(kFull, p[3].y, 1);   // section 8l-1
-        const float L2 = __shfl_up_sync(kFull, p[2].y, 1);   // section 8l-2
-        const float R1 = __shfl_down_sync(kFull, p[0].x, 1); // section 8l+8
-        const float R2 = __shfl_down_sync(kFull, p[1].x, 1); // section 8l+9
-        float qL = __fmaf_rn(-__fadd_rn(L2, p[0].x), rmL, YrmL);
-        float qR = __fmaf_rn(-__fadd_rn(p[3].y, R2), rmR, YrmR);
-        if (first) qL = 0.0f;
-        if (last) qR = 0.0f;
-        // t_k = p_{k-1} + p_{k+1} on the pairs (k, k+4)
-        float2 T[4];
-        T[0] = add2(f2(first ? 0.0f : L1, p[3].x), p[1]);
-        T[1] = add2(p[0], p[2]);
-        T[2] = add2(p[1], p[3]);
-        T[3] = add2(p[2], f2(p[0].y, R1));
-        if (last) {
-          T[2].y = p[3].y;
-          T[3].y = 0.0f;
-        }
-        float2 q[4];
+        float2 T[4], q[4];
+        if (kWrap) {
+          const float L1 = __shfl_sync(kFull, p[3].y, src_l);  // section 8l-1
+          const float L2 = __shfl_sync(kFull, p[2].y, src_l);  // section 8l-2
+          const float R1 = __shfl_down_sync(kFull, p[0].x, 1); // section 8l+8
+          const float R2 = __shfl_down_sync(kFull, p[1].x, 1); // section 8l+9
+          const float qL = __fmaf_rn(-__fadd_rn(L2, p[0].x), rmL, YrmL);
+          const float qR = __fmaf_rn(-__fadd_rn(p[3].y, R2), rmR, YrmR);
+          // t_k = p_{k-1} + p_{k+1} on the pairs (k, k+4)
+          T[0] = add2(f2(L1, p[3].x), p[1]);
+          T[1] = add2(p[0], p[2]);
+          T[2] = fma2(lo2, p[1], p[3]);
+          T[3] = add2(p[2], f2(p[0].y, R1));
 #pragma unroll
-        for (int k = 0; k < 4; ++k) q[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
-        T[0] = add2(f2(qL, q[3].x), q[1]);
-        T[1] = add2(q[0], q[2]);
-        T[2] = add2(q[1], q[3]);
-        T[3] = add2(q[2], f2(q[0].y, qR));
-        if (last) {
-          T[2].y = q[3].y;
-          T[3].y = 0.0f;
+          for (int k = 0; k < 4; ++k) q[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
+          T[0] = add2(f2(qL, q[3].x), q[1]);
+          T[1] = add2(q[0], q[2]);
+          T[2] = fma2(lo2, q[1], q[3]);
+          T[3] = add2(q[2], f2(q[0].y, qR));
+        } else {
+          const float L1 = __shfl_up_sync(kFull, p[3].y, 1);   // section 8l-1
+          const float L2 = __shfl_up_sync(kFull, p[2].y, 1);   // section 8l-2
+          const float R1 = __shfl_down_sync(kFull, p[0].x, 1); // section 8l+8
+          const float R2 = __shfl_down_sync(kFull, p[1].x, 1); // section 8l+9
+          float qL = __fmaf_rn(-__fadd_rn(L2, p[0].x), rmL, YrmL);
+          float qR = __fmaf_rn(-__fadd_rn(p[3].y, R2), rmR, YrmR);
+          if (first) qL = 0.0f;
+          if (last) qR = 0.0f;
+          T[0] = add2(f2(first ? 0.0f : L1, p[3].x), p[1]);
+          T[1] = add2(p[0], p[2]);
+          T[2] = add2(p[1], p[3]);
+          T[3] = add2(p[2], f2(p[0].y, R1));
+          if (last) {
+            T[2].y = p[3].y;
+            T[3].y = 0.0f;
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) q[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
+          T[0] = add2(f2(qL, q[3].x), q[1]);
+          T[1] = add2(q[0], q[2]);
+          T[2] = add2(q[1], q[3]);
+          T[3] = add2(q[2], f2(q[0].y, qR));
+          if (last) {
+            T[2].y = q[3].y;
+            T[3].y = 0.0f;
+          }
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
@@ -420,7 +482,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       float2 da[4];
       {
         float2 invM[4];
-        load8p(sp + 0 * 256 + base, invM);
+        load8q(sp + 0 * 256 + base, invM);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const float2 an = mul2(add2(p[k], G[k]), invM[k]);
@@ -530,7 +592,8 @@ __device__ __forceinline__ void bm_body(const BMArgs& A) {
   __shared__ __align__(16) float s_gam[WARPS][2][256];
   __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 7 * 256 : 4];
   extern __shared__ __align__(16) unsigned char s_dyn[];
-  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) s_par[i] = A.secp[i];
+  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
+    s_par[(i & ~255) | pair_pos(i & 255)] = A.secp[i];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float* hist = nullptr;
   unsigned char* wblob = nullptr;
@@ -559,10 +622,10 @@ __device__ __forceinline__ void bm_body(const BMArgs& A) {
     const float* g = A.gamma + (int64_t)un.profile * 256;
 #pragma unroll
     for (int k = 0; k < kSPL; ++k) {
-      const int s = lane * kSPL + k;
+      const int s = lane * kSPL + k, q = pair_pos(s);
       const float gm = g[s];
-      s_gam[warp][0][s] = gm;
-      s_gam[warp][1][s] = __fmul_rn(gm, s_par[5 * 256 + s]);
+      s_gam[warp][0][q] = gm;
+      s_gam[warp][1][q] = __fmul_rn(gm, s_par[5 * 256 + q]);
     }
     __syncwarp();
     run_unit<PREV_SMEM, TOL>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
