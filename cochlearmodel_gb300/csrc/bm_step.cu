@@ -87,16 +87,20 @@ __device__ __forceinline__ void store8p(float* p, const float2 (&r)[4]) {
   reinterpret_cast<float4*>(p)[1] = make_float4(r[0].y, r[1].y, r[2].y, r[3].y);
 }
 
-// Shared-memory copies of per-section vectors are kept in pair order: within
-// each group of eight sections the order is 0,4,1,5,2,6,3,7, so a lane's two
-// 16-byte loads land as whole register pairs (no repacking moves).
-__device__ __forceinline__ int pair_pos(int s) {
-  return (s & ~7) | ((s & 3) << 1) | ((s >> 2) & 1);
+// Shared-memory copies of per-section vectors are laid out [half][lane][4]:
+// lane l's eight sections in pair order (0,4,1,5 | 2,6,3,7) as two 16-byte
+// halves, the first halves of all lanes contiguous, then the second halves.
+// Each of the two 16-byte loads of a warp reads one contiguous 512-byte span
+// (no bank conflicts) and lands as two whole register pairs (no repacking).
+// p points at the vector plus 4 * lane floats.
+__device__ __forceinline__ int smem_pos(int s) {
+  const int c = s & 7, pp = ((c & 3) << 1) | (c >> 2);
+  return ((pp >> 2) << 7) | ((s >> 3) << 2) | (pp & 3);
 }
 
 __device__ __forceinline__ void load8q(const float* p, float2 (&r)[4]) {
-  const float4 a = reinterpret_cast<const float4*>(p)[0];
-  const float4 b = reinterpret_cast<const float4*>(p)[1];
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  const float4 b = *reinterpret_cast<const float4*>(p + 128);
   r[0] = f2(a.x, a.y);
   r[1] = f2(a.z, a.w);
   r[2] = f2(b.x, b.y);
@@ -104,8 +108,8 @@ __device__ __forceinline__ void load8q(const float* p, float2 (&r)[4]) {
 }
 
 __device__ __forceinline__ void store8q(float* p, const float2 (&r)[4]) {
-  reinterpret_cast<float4*>(p)[0] = make_float4(r[0].x, r[0].y, r[1].x, r[1].y);
-  reinterpret_cast<float4*>(p)[1] = make_float4(r[2].x, r[2].y, r[3].x, r[3].y);
+  *reinterpret_cast<float4*>(p) = make_float4(r[0].x, r[0].y, r[1].x, r[1].y);
+  *reinterpret_cast<float4*>(p + 128) = make_float4(r[2].x, r[2].y, r[3].x, r[3].y);
 }
 
 // pairs -> sections 8l..8l+7 in order
@@ -131,7 +135,7 @@ template <bool PREV_SMEM>
 struct PrevState {
   float2 r[7][4];
   float* sm;  // [7][256] slice of this warp (PREV_SMEM only)
-  __device__ __forceinline__ void init(float* slice, int base) {
+  __device__ __forceinline__ void init(float* slice, int qb) {
     sm = slice;
 #pragma unroll
     for (int j = 0; j < 7; ++j)
@@ -139,19 +143,19 @@ struct PrevState {
       for (int k = 0; k < 4; ++k) r[j][k] = f2b(0.0f);
     if (PREV_SMEM)
 #pragma unroll
-      for (int j = 0; j < 7; ++j) store8q(sm + j * 256 + base, r[j]);
+      for (int j = 0; j < 7; ++j) store8q(sm + j * 256 + qb, r[j]);
   }
-  __device__ __forceinline__ void load(int j, int base, float2 (&o)[4]) const {
+  __device__ __forceinline__ void load(int j, int qb, float2 (&o)[4]) const {
     if (PREV_SMEM) {
-      load8q(sm + j * 256 + base, o);
+      load8q(sm + j * 256 + qb, o);
     } else {
 #pragma unroll
       for (int k = 0; k < 4; ++k) o[k] = r[j][k];
     }
   }
-  __device__ __forceinline__ void store(int j, int base, const float2 (&o)[4]) {
+  __device__ __forceinline__ void store(int j, int qb, const float2 (&o)[4]) {
     if (PREV_SMEM) {
-      store8q(sm + j * 256 + base, o);
+      store8q(sm + j * 256 + qb, o);
     } else {
 #pragma unroll
       for (int k = 0; k < 4; ++k) r[j][k] = o[k];
@@ -181,10 +185,10 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
                                          float* hist, unsigned char* ws_scratch,
                                          const unsigned char* wblob, int lane,
                                          cgb_unit_stats* st) {
-  const int base = lane * kSPL;
+  const int base = lane * kSPL, qb = lane * 4;
   const bool first = lane == 0, last = lane == 31;
   float2 rm[4];
-  load8q(sp + 1 * 256 + base, rm);
+  load8q(sp + 1 * 256 + qb, rm);
   // 1/m of the halo sections 8l-1 and 8l+8 (used by the paired sweeps)
   float rmL = __shfl_up_sync(kFull, rm[3].y, 1);
   const float rmR = __shfl_down_sync(kFull, rm[0].x, 1);
@@ -211,7 +215,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   }
 
   PrevState<PREV_SMEM> prev;
-  prev.init(prev_slice, base);
+  prev.init(prev_slice, qb);
   float2 x[4], v[4], a[4], y[4], u[4], ps[4], dp[4];
   float2 Ptm[4], p[4], G[4], Yrm[4];
 #pragma unroll
@@ -248,7 +252,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // of this step, the other slot holds the start of the previous one
       rho = __fdiv_rn(dt, dt_prev);
       dt_prev = dt;
-      store8q(hist + (n_sub & 1) * 256 + base, p);
+      store8q(hist + (n_sub & 1) * 256 + qb, p);
     }
     const float delta = (float)(tau * A.invts);
     const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
@@ -259,13 +263,13 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // holding the previous derivatives: (d0 + d0) * 0.5 == d0 exactly, so
       // one code path serves both.
       float2 x0[4], v0[4], a0[4], y0[4], u0[4], ps0[4], dp0[4];
-      prev.load(0, base, x0);
-      prev.load(1, base, v0);
-      prev.load(2, base, a0);
-      prev.load(3, base, y0);
-      prev.load(4, base, u0);
-      prev.load(5, base, ps0);
-      prev.load(6, base, dp0);
+      prev.load(0, qb, x0);
+      prev.load(1, qb, v0);
+      prev.load(2, qb, a0);
+      prev.load(3, qb, y0);
+      prev.load(4, qb, u0);
+      prev.load(5, qb, ps0);
+      prev.load(6, qb, dp0);
       if (out_loop == 0 || reset) {
         out_loop = 0;
 #pragma unroll
@@ -297,15 +301,15 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       const bool tm_update = out_loop < 2;
       {
         float2 Stm[4], Rtm[4], gs[4], Rs[4], Ss[4], Qs[4];
-        load8q(sp + 6 * 256 + base, Stm);
-        load8q(sp + 7 * 256 + base, Rtm);
-        load8q(sgs + base, gs);
-        load8q(sp + 2 * 256 + base, Rs);
-        load8q(sp + 3 * 256 + base, Ss);
-        load8q(sp + 4 * 256 + base, Qs);
+        load8q(sp + 6 * 256 + qb, Stm);
+        load8q(sp + 7 * 256 + qb, Rtm);
+        load8q(sgs + qb, gs);
+        load8q(sp + 2 * 256 + qb, Rs);
+        load8q(sp + 3 * 256 + qb, Ss);
+        load8q(sp + 4 * 256 + qb, Qs);
         if (tm_update) {
           float2 gm[4];
-          load8q(sg + base, gm);
+          load8q(sg + qb, gm);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const float2 d = sub2(y[k], x[k]);
@@ -349,7 +353,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       const float YrmR = __shfl_down_sync(kFull, Yrm[0].x, 1);
       if (TOL && out_loop == 0 && n_sub >= 2) {
         float2 p2[4];
-        load8q(hist + ((n_sub + 1) & 1) * 256 + base, p2);
+        load8q(hist + ((n_sub + 1) & 1) * 256 + qb, p2);
         if (A.log && n_sub % A.log_every == 0) {
           int idx = 0;
           if (lane == 0) idx = atomicAdd(A.log_count, 1);
@@ -482,7 +486,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       float2 da[4];
       {
         float2 invM[4];
-        load8q(sp + 0 * 256 + base, invM);
+        load8q(sp + 0 * 256 + qb, invM);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const float2 an = mul2(add2(p[k], G[k]), invM[k]);
@@ -555,13 +559,13 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       smp_dt = smp_sub = smp_it = 0.0f;
       ++n;
     }
-    prev.store(0, base, x);
-    prev.store(1, base, v);
-    prev.store(2, base, a);
-    prev.store(3, base, y);
-    prev.store(4, base, u);
-    prev.store(5, base, ps);
-    prev.store(6, base, dp);
+    prev.store(0, qb, x);
+    prev.store(1, qb, v);
+    prev.store(2, qb, a);
+    prev.store(3, qb, y);
+    prev.store(4, qb, u);
+    prev.store(5, qb, ps);
+    prev.store(6, qb, dp);
     w0 = w;
     wd0 = wd;
     wdd0 = wdd;
@@ -593,7 +597,7 @@ __device__ __forceinline__ void bm_body(const BMArgs& A) {
   __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 7 * 256 : 4];
   extern __shared__ __align__(16) unsigned char s_dyn[];
   for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
-    s_par[(i & ~255) | pair_pos(i & 255)] = A.secp[i];
+    s_par[(i & ~255) | smem_pos(i & 255)] = A.secp[i];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float* hist = nullptr;
   unsigned char* wblob = nullptr;
@@ -622,7 +626,7 @@ __device__ __forceinline__ void bm_body(const BMArgs& A) {
     const float* g = A.gamma + (int64_t)un.profile * 256;
 #pragma unroll
     for (int k = 0; k < kSPL; ++k) {
-      const int s = lane * kSPL + k, q = pair_pos(s);
+      const int s = lane * kSPL + k, q = smem_pos(s);
       const float gm = g[s];
       s_gam[warp][0][q] = gm;
       s_gam[warp][1][q] = __fmul_rn(gm, s_par[5 * 256 + q]);
