@@ -128,13 +128,13 @@ __device__ __forceinline__ float pair_sum8p(const float2 (&t)[4]) {
 }
 
 // The previous-step state (x, v, a, y, u, psi, psi') of a unit lives either
-// in registers or, with PREV_SMEM, in the warp's slice of shared memory
-// (7 x 256 floats), which frees 56 registers per thread at the cost of
+// in registers or, with PREV_SMEM, in the first 7 x 256 floats of the warp's
+// slice of shared memory, which frees 56 registers per thread at the cost of
 // reloading it on every outer iteration.
 template <bool PREV_SMEM>
 struct PrevState {
   float2 r[7][4];
-  float* sm;  // [7][256] slice of this warp (PREV_SMEM only)
+  float* sm;  // this lane in the warp's [9][256] slice (PREV_SMEM only)
   __device__ __forceinline__ void init(float* slice, int qb) {
     sm = slice;
 #pragma unroll
@@ -159,6 +159,37 @@ struct PrevState {
     } else {
 #pragma unroll
       for (int k = 0; k < 4; ++k) r[j][k] = o[k];
+    }
+  }
+};
+
+// G and P_tm between the phases of an outer iteration: registers, or (with
+// the previous-step state in shared memory) two more 256-float slots of the
+// warp's slice, which keeps the bounded-register shapes free of spills.
+template <bool IN_SMEM>
+struct SideVec {
+  float2 r[4];
+  float* sm;  // this lane's position in the slot (IN_SMEM only)
+  __device__ __forceinline__ void init(float* slot) {
+    sm = slot;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r[k] = f2b(0.0f);
+    if (IN_SMEM) store8q(sm, r);
+  }
+  __device__ __forceinline__ void put(const float2 (&o)[4]) {
+    if (IN_SMEM) {
+      store8q(sm, o);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) r[k] = o[k];
+    }
+  }
+  __device__ __forceinline__ void get(float2 (&o)[4]) const {
+    if (IN_SMEM) {
+      load8q(sm, o);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) o[k] = r[k];
     }
   }
 };
@@ -217,11 +248,14 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   PrevState<PREV_SMEM> prev;
   prev.init(prev_slice, qb);
   float2 x[4], v[4], a[4], y[4], u[4], ps[4], dp[4];
-  float2 Ptm[4], p[4], G[4], Yrm[4];
+  float2 p[4], Yrm[4];
+  SideVec<PREV_SMEM> Gs, Ps;  // G and P_tm
+  Gs.init(prev_slice + 7 * 256 + qb);
+  Ps.init(prev_slice + 8 * 256 + qb);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     x[k] = v[k] = a[k] = y[k] = u[k] = ps[k] = dp[k] = f2b(0.0f);
-    Ptm[k] = p[k] = G[k] = Yrm[k] = f2b(0.0f);
+    p[k] = Yrm[k] = f2b(0.0f);
   }
   float w0 = 0.f, wd0 = 0.f, wdd0 = 0.f, w = 0.f, wd = 0.f, wdd = 0.f;
 
@@ -300,15 +334,12 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // OHC / TM coupling, G and the right-hand side Y (scaled by 1/m).
       const bool tm_update = out_loop < 2;
       {
-        float2 Stm[4], Rtm[4], gs[4], Rs[4], Ss[4], Qs[4];
-        load8q(sp + 6 * 256 + qb, Stm);
-        load8q(sp + 7 * 256 + qb, Rtm);
-        load8q(sgs + qb, gs);
-        load8q(sp + 2 * 256 + qb, Rs);
-        load8q(sp + 3 * 256 + qb, Ss);
-        load8q(sp + 4 * 256 + qb, Qs);
+        // section tables are loaded next to their use (short live ranges)
         if (tm_update) {
-          float2 gm[4];
+          float2 Stm[4], Rtm[4], gs[4], gm[4], Ptm[4];
+          load8q(sp + 6 * 256 + qb, Stm);
+          load8q(sp + 7 * 256 + qb, Rtm);
+          load8q(sgs + qb, gs);
           load8q(sg + qb, gm);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
@@ -326,7 +357,14 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
             u[k] = f2(den.x < 0.0f ? -q.x : q.x, den.y < 0.0f ? -q.y : q.y);
             Ptm[k] = fma2(Rtm[k], u[k], mul2(Stm[k], y[k]));
           }
+          Ps.put(Ptm);
         }
+        float2 Ptm[4], G[4];
+        Ps.get(Ptm);
+        float2 Rs[4], Ss[4], Qs[4];
+        load8q(sp + 2 * 256 + qb, Rs);
+        load8q(sp + 3 * 256 + qb, Ss);
+        load8q(sp + 4 * 256 + qb, Qs);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           float2 g = mul2(Rs[k], fma2(f2b(A.ar), mul2(v[k], v[k]), f2b(1.0f)));
@@ -339,6 +377,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           if (k == 3 && last) Yk.y = 0.0f;  // section 255
           Yrm[k] = mul2(Yk, rm[k]);
         }
+        Gs.put(G);
       }
 
       // Jacobi sweeps on the pressure; p persists across iterations and steps.
@@ -487,6 +526,8 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       {
         float2 invM[4];
         load8q(sp + 0 * 256 + qb, invM);
+        float2 G[4];
+        Gs.get(G);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           const float2 an = mul2(add2(p[k], G[k]), invM[k]);
@@ -594,7 +635,7 @@ template <int WARPS, bool PREV_SMEM, int TOL>
 __device__ __forceinline__ void bm_body(const BMArgs& A) {
   __shared__ __align__(16) float s_par[8 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
-  __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 7 * 256 : 4];
+  __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 9 * 256 : 4];
   extern __shared__ __align__(16) unsigned char s_dyn[];
   for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
     s_par[(i & ~255) | smem_pos(i & 255)] = A.secp[i];

@@ -92,3 +92,20 @@ def test_per_sample_convergence_stats(mv, bm_solver):
     assert np.array_equal(conv_g.view(np.uint32), conv_o.view(np.uint32))
     e = int(units["end"][0])
     assert (conv_g[:e, 1] >= 10).all() and (conv_g[:e, 2] >= 2).all()
+
+
+def test_every_launch_shape_bit_exact(mv, bm_solver):
+    """Each built launch shape (register-only state, previous-step state and
+    G/P_tm in shared memory, bounded register counts) runs the same
+    floating-point sequence: bit-exact against the oracle on units of uneven
+    length from six signals."""
+    from cochlearmodel_gb300 import native
+    lib = native.load()
+    case = cases.framed_batch(mv, [1.0, 2.5, 0.6, 1.7, 0.9, 1.3], seed=7, block_ms=0.4,
+                              overlap_ms=0.2)
+    try:
+        for shape in range(lib.cgb_bm_launch_shape_count()):
+            native.check(lib.cgb_bm_set_launch_shape(shape), "set launch shape")
+            _compare(mv, bm_solver, case)
+    finally:
+        native.check(lib.cgb_bm_set_launch_shape(0), "set launch shape")
