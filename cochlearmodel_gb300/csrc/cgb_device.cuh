@@ -7,31 +7,6 @@ namespace cgb {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-// e^y for y >= 0 by Cody-Waite reduction y = k ln2 + r and a degree-8 Taylor
-// polynomial of e^r; 2^k is assembled in the exponent field.  The order of
-// every float operation is fixed (explicit fma, no contraction) so the CPU
-// oracle, which evaluates the same sequence, rounds identically.
-__device__ __forceinline__ float own_expf_pos(float y) {
-  const float log2e = 1.44269504088896341f;
-  const float ln2_hi = 0.693145751953125f;
-  const float ln2_lo = 1.42860682030941723e-06f;
-  float k = rintf(__fmul_rn(y, log2e));
-  float r = __fmaf_rn(-k, ln2_hi, y);
-  r = __fmaf_rn(-k, ln2_lo, r);
-  float p = 1.0f / 40320.0f;
-  p = __fmaf_rn(p, r, 1.0f / 5040.0f);
-  p = __fmaf_rn(p, r, 1.0f / 720.0f);
-  p = __fmaf_rn(p, r, 1.0f / 120.0f);
-  p = __fmaf_rn(p, r, 1.0f / 24.0f);
-  p = __fmaf_rn(p, r, 1.0f / 6.0f);
-  p = __fmaf_rn(p, r, 0.5f);
-  p = __fmaf_rn(p, r, 1.0f);
-  p = __fmaf_rn(p, r, 1.0f);
-  int ki = (int)k;
-  float scale = __int_as_float((ki + 127) << 23);
-  return __fmul_rn(p, scale);
-}
-
 // 1/d for a positive normal d without a branch: the classic bit-level seed
 // 0x7EF311C3 - bits(d) (within ~12%) refined by three Newton steps
 // r <- r + r(1 - d r); measured <= 0.5004 ulp over [1, 2) and across exponents.
@@ -43,30 +18,27 @@ __device__ __forceinline__ float own_rcpf(float d) {
   return r;
 }
 
-// tanh(x): odd Taylor series to x^21 below |x| = 0.55, 1 - 2/(e^{2|x|}+1)
-// up to |x| = 20, +-1 beyond.  Both branches are evaluated and one is
-// selected, so unrolled per-section calls keep their instruction-level
-// parallelism (no divergent branch per section).
+// tanh(x) = x P(x^2) / Q(x^2) with x clamped to [-9.5, 9.5] (where the
+// fit evaluates above 1): P and Q of degree 4 in x^2 (a minimax-relative
+// rational fit on [0, 9], derived by cochlearmodel_gb300/fit_tanh.py), Horner
+// in x^2, quotient as x P times own_rcpf(Q) (Q >= 1), result clamped to
+// [-1, 1].  One branch-free path, <= 5.5 ulp; the CPU oracle evaluates the
+// same sequence.
 __device__ __forceinline__ float own_tanhf(float x) {
-  const float ax = fabsf(x);
-  const float x2 = __fmul_rn(x, x);
-  float p = (float)(18888466084.0 / 194896477400625.0);
-  p = __fmaf_rn(p, x2, (float)(-443861162.0 / 1856156927625.0));
-  p = __fmaf_rn(p, x2, (float)(6404582.0 / 10854718875.0));
-  p = __fmaf_rn(p, x2, (float)(-929569.0 / 638512875.0));
-  p = __fmaf_rn(p, x2, (float)(21844.0 / 6081075.0));
-  p = __fmaf_rn(p, x2, (float)(-1382.0 / 155925.0));
-  p = __fmaf_rn(p, x2, (float)(62.0 / 2835.0));
-  p = __fmaf_rn(p, x2, (float)(-17.0 / 315.0));
-  p = __fmaf_rn(p, x2, (float)(2.0 / 15.0));
-  p = __fmaf_rn(p, x2, (float)(-1.0 / 3.0));
-  p = __fmul_rn(p, x2);
-  const float tp = __fmaf_rn(p, x, x);
-  const float e = own_expf_pos(__fmul_rn(2.0f, fminf(ax, 20.0f)));
-  float te = __fmaf_rn(-2.0f, own_rcpf(__fadd_rn(e, 1.0f)), 1.0f);
-  te = ax < 20.0f ? te : 1.0f;
-  te = x < 0.0f ? -te : te;
-  return ax < 0.55f ? tp : te;
+  const float xc = fminf(fmaxf(x, -9.5f), 9.5f);
+  const float z = __fmul_rn(xc, xc);
+  float p = 1.335385846346071e-08f;
+  p = __fmaf_rn(p, z, 2.0608504200936295e-05f);
+  p = __fmaf_rn(p, z, 0.0034955532755702734f);
+  p = __fmaf_rn(p, z, 0.13380996882915497f);
+  p = __fmaf_rn(p, z, 1.0f);
+  float q = 7.776229722367134e-07f;
+  q = __fmaf_rn(q, z, 0.00032855774043127894f);
+  q = __fmaf_rn(q, z, 0.02587684988975525f);
+  q = __fmaf_rn(q, z, 0.46714311838150024f);
+  q = __fmaf_rn(q, z, 1.0f);
+  const float t = __fmul_rn(__fmul_rn(xc, p), own_rcpf(q));
+  return fminf(fmaxf(t, -1.0f), 1.0f);
 }
 
 // log10(x) for a positive normal x: x = m 2^e with m in [sqrt(1/2), sqrt(2)),
@@ -114,29 +86,6 @@ __device__ __forceinline__ float2 max2(float2 a, float2 b) {
   return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y));
 }
 
-// own_expf_pos on a pair: the same operation sequence per element.
-__device__ __forceinline__ float2 own_expf_pos2(float2 y) {
-  const float log2e = 1.44269504088896341f;
-  const float ln2_hi = 0.693145751953125f;
-  const float ln2_lo = 1.42860682030941723e-06f;
-  const float2 kk = mul2(y, f2b(log2e));
-  const float2 k = f2(rintf(kk.x), rintf(kk.y));
-  float2 r = fma2(neg2(k), f2b(ln2_hi), y);
-  r = fma2(neg2(k), f2b(ln2_lo), r);
-  float2 p = f2b(1.0f / 40320.0f);
-  p = fma2(p, r, f2b(1.0f / 5040.0f));
-  p = fma2(p, r, f2b(1.0f / 720.0f));
-  p = fma2(p, r, f2b(1.0f / 120.0f));
-  p = fma2(p, r, f2b(1.0f / 24.0f));
-  p = fma2(p, r, f2b(1.0f / 6.0f));
-  p = fma2(p, r, f2b(0.5f));
-  p = fma2(p, r, f2b(1.0f));
-  p = fma2(p, r, f2b(1.0f));
-  const float2 scale = f2(__int_as_float(((int)k.x + 127) << 23),
-                          __int_as_float(((int)k.y + 127) << 23));
-  return mul2(p, scale);
-}
-
 // own_rcpf on a pair.
 __device__ __forceinline__ float2 own_rcpf2(float2 d) {
   float2 r = f2(__int_as_float(0x7EF311C3 - __float_as_int(d.x)),
@@ -148,29 +97,22 @@ __device__ __forceinline__ float2 own_rcpf2(float2 d) {
   return r;
 }
 
-// own_tanhf on a pair.
+// own_tanhf on a pair: the same operation sequence per element.
 __device__ __forceinline__ float2 own_tanhf2(float2 x) {
-  const float2 ax = abs2(x);
-  const float2 x2 = mul2(x, x);
-  float2 p = f2b((float)(18888466084.0 / 194896477400625.0));
-  p = fma2(p, x2, f2b((float)(-443861162.0 / 1856156927625.0)));
-  p = fma2(p, x2, f2b((float)(6404582.0 / 10854718875.0)));
-  p = fma2(p, x2, f2b((float)(-929569.0 / 638512875.0)));
-  p = fma2(p, x2, f2b((float)(21844.0 / 6081075.0)));
-  p = fma2(p, x2, f2b((float)(-1382.0 / 155925.0)));
-  p = fma2(p, x2, f2b((float)(62.0 / 2835.0)));
-  p = fma2(p, x2, f2b((float)(-17.0 / 315.0)));
-  p = fma2(p, x2, f2b((float)(2.0 / 15.0)));
-  p = fma2(p, x2, f2b((float)(-1.0 / 3.0)));
-  p = mul2(p, x2);
-  const float2 tp = fma2(p, x, x);
-  const float2 e = own_expf_pos2(mul2(f2b(2.0f), f2(fminf(ax.x, 20.0f), fminf(ax.y, 20.0f))));
-  float2 te = fma2(f2b(-2.0f), own_rcpf2(add2(e, f2b(1.0f))), f2b(1.0f));
-  te.x = ax.x < 20.0f ? te.x : 1.0f;
-  te.y = ax.y < 20.0f ? te.y : 1.0f;
-  te.x = x.x < 0.0f ? -te.x : te.x;
-  te.y = x.y < 0.0f ? -te.y : te.y;
-  return f2(ax.x < 0.55f ? tp.x : te.x, ax.y < 0.55f ? tp.y : te.y);
+  const float2 xc = f2(fminf(fmaxf(x.x, -9.5f), 9.5f), fminf(fmaxf(x.y, -9.5f), 9.5f));
+  const float2 z = mul2(xc, xc);
+  float2 p = f2b(1.335385846346071e-08f);
+  p = fma2(p, z, f2b(2.0608504200936295e-05f));
+  p = fma2(p, z, f2b(0.0034955532755702734f));
+  p = fma2(p, z, f2b(0.13380996882915497f));
+  p = fma2(p, z, f2b(1.0f));
+  float2 q = f2b(7.776229722367134e-07f);
+  q = fma2(q, z, f2b(0.00032855774043127894f));
+  q = fma2(q, z, f2b(0.02587684988975525f));
+  q = fma2(q, z, f2b(0.46714311838150024f));
+  q = fma2(q, z, f2b(1.0f));
+  const float2 t = mul2(mul2(xc, p), own_rcpf2(q));
+  return f2(fminf(fmaxf(t.x, -1.0f), 1.0f), fminf(fmaxf(t.y, -1.0f), 1.0f));
 }
 
 __device__ __forceinline__ float warp_sum_xor(float v) {

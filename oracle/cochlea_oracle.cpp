@@ -49,35 +49,13 @@ constexpr int NS = 256;  // cochlear sections (include/const.h:19)
 // ---------------------------------------------------------------------------
 // tanh in float.  The reference calls CUDA's tanhf; this project uses its own
 // tanh on both sides so the GPU and the oracle round identically:
-//   |x| < 0.55 : odd Taylor series of tanh to x^21 (coefficients
-//                2^{2n}(2^{2n}-1)B_{2n}/(2n)!), Horner in x^2;
-//   |x| < 20   : 1 - 2/(e^{2|x|}+1), e^y by Cody-Waite reduction
-//                y = k ln2 + r and a degree-8 Taylor polynomial of e^r;
-//   else       : +-1.
+//   x P(x^2) / Q(x^2) with x clamped to [-9.5, 9.5] (where it
+//   evaluates above 1), P and Q of degree 4 in x^2 (a minimax-relative rational fit
+//   on [0, 9], cochlearmodel_gb300/fit_tanh.py), Horner in x^2, quotient as
+//   x P times own_rcpf(Q), result clamped to [-1, 1].
+// Within 5.5 ulp of tanh; the GPU kernels evaluate the same sequence
+// (cochlearmodel_gb300/csrc/cgb_device.cuh).
 // ---------------------------------------------------------------------------
-float own_expf_pos(float y) {
-  const float log2e = 1.44269504088896341f;
-  const float ln2_hi = 0.693145751953125f;
-  const float ln2_lo = 1.42860682030941723e-06f;
-  float k = rintf(y * log2e);
-  float r = fmaf(-k, ln2_hi, y);
-  r = fmaf(-k, ln2_lo, r);
-  float p = 1.0f / 40320.0f;
-  p = fmaf(p, r, 1.0f / 5040.0f);
-  p = fmaf(p, r, 1.0f / 720.0f);
-  p = fmaf(p, r, 1.0f / 120.0f);
-  p = fmaf(p, r, 1.0f / 24.0f);
-  p = fmaf(p, r, 1.0f / 6.0f);
-  p = fmaf(p, r, 0.5f);
-  p = fmaf(p, r, 1.0f);
-  p = fmaf(p, r, 1.0f);
-  int ki = (int)k;
-  uint32_t bits = (uint32_t)(ki + 127) << 23;
-  float scale;
-  std::memcpy(&scale, &bits, 4);
-  return p * scale;
-}
-
 // 1/d for a positive normal d: bit-level seed 0x7EF311C3 - bits(d), then
 // three Newton steps r <- r + r(1 - d r).
 float own_rcpf(float d) {
@@ -93,28 +71,20 @@ float own_rcpf(float d) {
 }
 
 float own_tanhf(float x) {
-  float ax = fabsf(x);
-  if (ax < 0.55f) {
-    float x2 = x * x;
-    float p = (float)(18888466084.0 / 194896477400625.0);
-    p = fmaf(p, x2, (float)(-443861162.0 / 1856156927625.0));
-    p = fmaf(p, x2, (float)(6404582.0 / 10854718875.0));
-    p = fmaf(p, x2, (float)(-929569.0 / 638512875.0));
-    p = fmaf(p, x2, (float)(21844.0 / 6081075.0));
-    p = fmaf(p, x2, (float)(-1382.0 / 155925.0));
-    p = fmaf(p, x2, (float)(62.0 / 2835.0));
-    p = fmaf(p, x2, (float)(-17.0 / 315.0));
-    p = fmaf(p, x2, (float)(2.0 / 15.0));
-    p = fmaf(p, x2, (float)(-1.0 / 3.0));
-    p = p * x2;
-    return fmaf(p, x, x);
-  }
-  float r = 1.0f;
-  if (ax < 20.0f) {
-    float e = own_expf_pos(2.0f * ax);
-    r = fmaf(-2.0f, own_rcpf(e + 1.0f), 1.0f);
-  }
-  return x < 0.0f ? -r : r;
+  const float xc = fminf(fmaxf(x, -9.5f), 9.5f);
+  const float z = xc * xc;
+  float p = 1.335385846346071e-08f;
+  p = fmaf(p, z, 2.0608504200936295e-05f);
+  p = fmaf(p, z, 0.0034955532755702734f);
+  p = fmaf(p, z, 0.13380996882915497f);
+  p = fmaf(p, z, 1.0f);
+  float q = 7.776229722367134e-07f;
+  q = fmaf(q, z, 0.00032855774043127894f);
+  q = fmaf(q, z, 0.02587684988975525f);
+  q = fmaf(q, z, 0.46714311838150024f);
+  q = fmaf(q, z, 1.0f);
+  const float t = (xc * p) * own_rcpf(q);
+  return fminf(fmaxf(t, -1.0f), 1.0f);
 }
 
 // log10 of a positive normal float: x = m 2^e, m in [sqrt(1/2), sqrt(2)),
@@ -422,6 +392,9 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
     }
     const T delta = std::is_same<T, float>::value ? (T)(float)(tau * invTs) : (T)(tau * invTs);
     const T smp = A::fma(sx1, delta, sx0 * ((T)1 - delta));
+    // (s * 0.5) * dt == s * (dt * 0.5) exactly (power-of-two scaling), so
+    // each trapezoid update is one fma with the half step
+    const T hdt = dt * (T)0.5;
     while (another) {
       for (int s = 0; s < NS; ++s) aref[s] = a[s];
       if (out_loop == 0 || reset) {
@@ -431,22 +404,22 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
           T vn = A::fma(a0[s], dt, v0[s]);
           dv[s] = A::abs(vn - v[s]);
           v[s] = vn;
-          x[s] = A::fma((v0[s] + vn) * (T)0.5, dt, x0[s]);
+          x[s] = A::fma(v0[s] + vn, hdt, x0[s]);
           ps[s] = A::fma(dp0[s], dt, ps0[s]);
         }
         w = A::fma(wd0, dt, w0);
         wd = A::fma(wdd0, dt, wd0);
       } else {
         for (int s = 0; s < NS; ++s) {
-          T vn = A::fma((a0[s] + a[s]) * (T)0.5, dt, v0[s]);
+          T vn = A::fma(a0[s] + a[s], hdt, v0[s]);
           dv[s] = A::abs(vn - v[s]);
           v[s] = vn;
-          x[s] = A::fma((v0[s] + vn) * (T)0.5, dt, x0[s]);
-          y[s] = A::fma((u0[s] + u[s]) * (T)0.5, dt, y0[s]);
-          ps[s] = A::fma((dp0[s] + dp[s]) * (T)0.5, dt, ps0[s]);
+          x[s] = A::fma(v0[s] + vn, hdt, x0[s]);
+          y[s] = A::fma(u0[s] + u[s], hdt, y0[s]);
+          ps[s] = A::fma(dp0[s] + dp[s], hdt, ps0[s]);
         }
-        w = A::fma((wd0 + wd) * (T)0.5, dt, w0);
-        wd = A::fma((wdd0 + wdd) * (T)0.5, dt, wd0);
+        w = A::fma(wd0 + wd, hdt, w0);
+        wd = A::fma(wdd0 + wdd, hdt, wd0);
       }
       for (int s = 0; s < NS; ++s) {
         T d = y[s] - x[s];

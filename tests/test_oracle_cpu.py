@@ -8,15 +8,20 @@ from tests import cases
 
 
 def test_own_tanh_accuracy():
-    """The project's float tanh stays within 2 ulp of the exact value."""
+    """The project's float tanh (rational, one path) stays within 6 ulp of the
+    exact value, is odd, and saturates to +-1 from |x| = 9."""
     xs = np.concatenate([np.linspace(-12, 12, 20001), np.linspace(-0.6, 0.6, 20001),
-                         np.geomspace(1e-8, 1e-1, 2001), [0.55, 0.5499999, 20.0, 25.0]])
+                         np.geomspace(1e-8, 1e-1, 2001), np.linspace(8.5, 9.0, 2001),
+                         [0.55, 0.5499999, 8.999999, 9.0, 20.0, 25.0]])
     xs = xs.astype(np.float32)
     got = np.array([orc.tanhf(float(x)) for x in xs], np.float32)
     exact = np.tanh(xs.astype(np.float64))
     ulp = np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)
     err = np.abs(got.astype(np.float64) - exact) / ulp
-    assert err.max() <= 2.0, (xs[err.argmax()], err.max())
+    assert err.max() <= 6.0, (xs[err.argmax()], err.max())
+    assert np.all(np.abs(got) <= 1.0)
+    neg = np.array([orc.tanhf(float(-x)) for x in xs], np.float32)
+    assert np.array_equal(neg, -got)
     assert orc.tanhf(0.0) == 0.0 and orc.tanhf(30.0) == 1.0 and orc.tanhf(-30.0) == -1.0
 
 
