@@ -39,7 +39,7 @@ namespace {
 
 constexpr int kSecTile = 32;   // sections per CTA (one per lane)
 constexpr int kBoxRows = 64;   // rows per TMA box
-constexpr int kIhcWarps = 8;
+constexpr int kIhcWarps = 16;
 constexpr int kRB = 8;         // output rows per register block
 constexpr long long kWaitPolls = 1ll << 26;
 constexpr int kTilesPerRun = 8;  // consecutive tiles per CTA
@@ -395,6 +395,31 @@ size_t smem_bytes(int TR, int xrows, int n_ac, int n_dc) {
   return ((size_t)xrows + TR + n_dc + TR) * kSecTile * 4 + (size_t)(n_ac + n_dc) * 4 + 32;
 }
 
+// Output rows per tile: a multiple of 32 (the DC anchor grid) whose staged
+// window fits 227 KB of shared memory, at most 384.  Preferred: the largest
+// such TR that is a multiple of kIhcWarps * kRB (every warp gets the same
+// number of register blocks in phase 1) and >= n_dc (runs of tiles); else
+// the largest that fits.  TR = 0: the filters are too long for one tile.
+void pick_tile(int n_ac, int n_dc, int* TR, int* xrows) {
+  *TR = *xrows = 0;
+  int any = 0, ax = 0;
+  for (int tr = 384; tr >= 32; tr -= 32) {
+    const int xr = (tr + n_ac + n_dc - 1 + kBoxRows - 1) / kBoxRows * kBoxRows;
+    if (smem_bytes(tr, xr, n_ac, n_dc) > 227 * 1024) continue;
+    if (!any) {
+      any = tr;
+      ax = xr;
+    }
+    if (tr % (kIhcWarps * kRB) == 0 && tr >= n_dc) {
+      *TR = tr;
+      *xrows = xr;
+      return;
+    }
+  }
+  *TR = any;
+  *xrows = ax;
+}
+
 }  // namespace
 }  // namespace cgb
 
@@ -432,13 +457,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   if (v_rows > INT32_MAX)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: more than 2^31-1 velocity rows");
   std::vector<int32_t> prefix(n_frames + 1, 0);
-  int max_tr = 384;
-  // shrink the tile until the staged window fits 227 KB of shared memory
-  int TR = max_tr, xrows = 0;
-  for (; TR >= 32; TR -= 32) {  // multiples of 32: the DC anchor grid
-    xrows = (TR + n_ac + n_dc - 1 + kBoxRows - 1) / kBoxRows * kBoxRows;
-    if (smem_bytes(TR, xrows, n_ac, n_dc) <= 227 * 1024) break;
-  }
+  int TR = 0, xrows = 0;
+  pick_tile(n_ac, n_dc, &TR, &xrows);
   if (TR < 32) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
   // runs of tiles inherit the DC look-back rows from the tile before, an
   // in-place shift that needs TR >= n_dc
@@ -642,11 +662,8 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
     return fail(CGB_ERR_ARG, "cgb_ihc_lambda_noalloc_dev: d_v must be 16-byte aligned");
   if (v_rows > INT32_MAX)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: more than 2^31-1 velocity rows");
-  int TR = 384, xrows = 0;
-  for (; TR >= 32; TR -= 32) {  // multiples of 32: the DC anchor grid
-    xrows = (TR + n_ac + n_dc - 1 + kBoxRows - 1) / kBoxRows * kBoxRows;
-    if (smem_bytes(TR, xrows, n_ac, n_dc) <= 227 * 1024) break;
-  }
+  int TR = 0, xrows = 0;
+  pick_tile(n_ac, n_dc, &TR, &xrows);
   if (TR < 32)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: filters too long for one tile");
   const int run = TR >= n_dc ? kTilesPerRun : 1;
