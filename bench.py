@@ -57,6 +57,31 @@ UNIT = "audio-s/s"
 
 
 # ----------------------------------------------------------------------------
+# one process per GPU: every rank runs the whole workload (replicas, weak
+# scaling, no collective on the data path); the job's time is the slowest rank
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    """The maximum of a per-rank scalar (a time) over the ranks of the job
+    (one all-reduce on the process group's own device: the GPU under NCCL,
+    the CPU under gloo)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(audio_s_per_step: float, steps: int, world: int, t_max_s: float) -> float:
+    """Whole-job throughput: the audio-seconds all ranks processed over the
+    slowest rank's time."""
+    return audio_s_per_step * steps * world / t_max_s
+
+
+# ----------------------------------------------------------------------------
 # workloads
 # ----------------------------------------------------------------------------
 def make_workload(name, device, n_freq=64, n_seeds=4, n_signals=1024):
@@ -385,12 +410,8 @@ def run_ours(args, rank, world, device):
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    t_total = sum(a.elapsed_time(b) for a, b in ev) / 1000.0
-    if world > 1:
-        tt = torch.tensor([t_total], device=device)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(tt.item())
-    value = run.audio_seconds * args.steps * world / t_total
+    t_total = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / 1000.0, world)
+    value = job_rate(run.audio_seconds, args.steps, world, t_total)
 
     # e2e: inputs in from pinned host memory (profile tables, or the samples of
     # the mixed batch), the path, results back to pinned host memory (velocity
@@ -426,7 +447,7 @@ def run_ours(args, rank, world, device):
         torch.cuda.synchronize(device)
         e_ms += a.elapsed_time(b)
         flush.fill_(float(i))
-    e2e = run.audio_seconds * e_steps * world / (e_ms / 1000.0)
+    e2e = job_rate(run.audio_seconds, e_steps, world, max_over_ranks(e_ms / 1000.0, world))
 
     plain = plain_single_signal(run, device) \
         if rank == 0 and not args.no_plain and run.kind != "mixed_batch" else None
