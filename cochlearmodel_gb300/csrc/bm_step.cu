@@ -3,9 +3,10 @@
 // src/cochlea.cu:1436-1493).
 //
 // GB300 layout: one WARP owns one unit (one time block of one signal); lane l
-// holds sections 8l..8l+7 of every state vector in registers.  A Jacobi sweep
-// is 8 FADD + 8 FFMA per lane plus two shuffles for the halo (sections 8l-1
-// and 8l+8) -- no shared-memory round trip and no block barrier, where the
+// holds sections 8l..8l+7 of every state vector in registers, as four
+// two-wide FP32 pairs.  Two Jacobi sweeps take four two-wide adds and four
+// two-wide fmas each per lane plus one round of four shuffles for a two-section
+// halo -- no shared-memory round trip and no block barrier, where the
 // reference spends two __syncthreads per sweep across 256 threads.  The
 // Lipschitz/fault reductions are xor-butterflies, so every lane holds the
 // full result and takes the same step decision (the reference's warp-0
@@ -69,32 +70,34 @@ __device__ __forceinline__ void store8(float* p, const float (&r)[kSPL]) {
   reinterpret_cast<float4*>(p)[1] = make_float4(r[4], r[5], r[6], r[7]);
 }
 
-// Sections of a lane as four pairs: pair j holds sections 8l+j (x) and
-// 8l+j+4 (y).  With this pairing the Jacobi neighbours of a pair are whole
-// pairs (pair j-1 and j+1), so a sweep is four two-wide adds and four
-// two-wide fmas; only the two edge pairs are assembled from the halo.
+// Sections of a lane as four mirror pairs: pair j holds sections 8l+j (x)
+// and 8l+7-j (y).  The Jacobi neighbours of pair j are whole pairs j-1 and
+// j+1 (for the y half the two swap roles, and the sum p_{s-1} + p_{s+1} is
+// the same); the halo of the lane, sections 8l-1 and 8l+8 (and 8l-2, 8l+9),
+// arrives as one pair, and the lane's own edge sections 8l, 8l+1, 8l+6, 8l+7
+// sit in pairs 0 and 1 only.  Pair 3 is its own neighbour, swapped.
 __device__ __forceinline__ void load8p(const float* p, float2 (&r)[4]) {
   const float4 a = reinterpret_cast<const float4*>(p)[0];
   const float4 b = reinterpret_cast<const float4*>(p)[1];
-  r[0] = f2(a.x, b.x);
-  r[1] = f2(a.y, b.y);
-  r[2] = f2(a.z, b.z);
-  r[3] = f2(a.w, b.w);
+  r[0] = f2(a.x, b.w);
+  r[1] = f2(a.y, b.z);
+  r[2] = f2(a.z, b.y);
+  r[3] = f2(a.w, b.x);
 }
 
 __device__ __forceinline__ void store8p(float* p, const float2 (&r)[4]) {
   reinterpret_cast<float4*>(p)[0] = make_float4(r[0].x, r[1].x, r[2].x, r[3].x);
-  reinterpret_cast<float4*>(p)[1] = make_float4(r[0].y, r[1].y, r[2].y, r[3].y);
+  reinterpret_cast<float4*>(p)[1] = make_float4(r[3].y, r[2].y, r[1].y, r[0].y);
 }
 
 // Shared-memory copies of per-section vectors are laid out [half][lane][4]:
-// lane l's eight sections in pair order (0,4,1,5 | 2,6,3,7) as two 16-byte
+// lane l's eight sections in pair order (0,7,1,6 | 2,5,3,4) as two 16-byte
 // halves, the first halves of all lanes contiguous, then the second halves.
 // Each of the two 16-byte loads of a warp reads one contiguous 512-byte span
 // (no bank conflicts) and lands as two whole register pairs (no repacking).
 // p points at the vector plus 4 * lane floats.
 __device__ __forceinline__ int smem_pos(int s) {
-  const int c = s & 7, pp = ((c & 3) << 1) | (c >> 2);
+  const int c = s & 7, pp = c < 4 ? 2 * c : 2 * (7 - c) + 1;
   return ((pp >> 2) << 7) | ((s >> 3) << 2) | (pp & 3);
 }
 
@@ -117,11 +120,12 @@ __device__ __forceinline__ void unpair(const float2 (&r)[4], float (&o)[kSPL]) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     o[j] = r[j].x;
-    o[j + 4] = r[j].y;
+    o[7 - j] = r[j].y;
   }
 }
 
-// ((t0 + t1) + (t2 + t3)) + ((t4 + t5) + (t6 + t7)) on the pair layout
+// ((t0 + t1) + (t2 + t3)) + ((t4 + t5) + (t6 + t7)) on the pair layout (the
+// y halves add as (t7 + t6) + (t5 + t4): the same values, addition commutes)
 __device__ __forceinline__ float pair_sum8p(const float2 (&t)[4]) {
   const float2 s = add2(add2(t[0], t[1]), add2(t[2], t[3]));
   return __fadd_rn(s.x, s.y);
@@ -221,8 +225,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   float2 rm[4];
   load8q(sp + 1 * 256 + qb, rm);
   // 1/m of the halo sections 8l-1 and 8l+8 (used by the paired sweeps)
-  float rmL = __shfl_up_sync(kFull, rm[3].y, 1);
-  const float rmR = __shfl_down_sync(kFull, rm[0].x, 1);
+  float2 rmh = f2(__shfl_up_sync(kFull, rm[0].y, 1), __shfl_down_sync(kFull, rm[0].x, 1));
   // Boundary sections without per-sweep fix-ups (reference schedule and
   // tolerance mode with the previous or extrapolated guess).  There the
   // pressure of section 255 is +0 at every point: Y_255 = 0 and its update
@@ -236,12 +239,12 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   // first sweep, so it keeps the explicit fix-ups.
   constexpr bool kWrap = TOL != 2;
   const int src_l = (lane + 31) & 31;
-  float2 lo2 = f2b(1.0f);
+  float2 lo1 = f2b(1.0f);  // lower-neighbour factor of pair 1 (section 254)
   if (kWrap) {
-    if (first) rmL = 0.0f;
+    if (first) rmh.x = 0.0f;
     if (last) {
-      rm[3].y = 0.0f;
-      lo2.y = 0.0f;
+      rm[0].y = 0.0f;
+      lo1.y = 0.0f;
     }
   }
 
@@ -377,7 +380,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           if (k == 0 && first)  // section 0
             Yk.x = __fmul_rn(A.dxa0,
                              __fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmul_rn(A.gme, smp))));
-          if (k == 3 && last) Yk.y = 0.0f;  // section 255
+          if (k == 0 && last) Yk.y = 0.0f;  // section 255
           Yrm[k] = mul2(Yk, rm[k]);
         }
         Gs.put(G);
@@ -390,9 +393,9 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       // second on its own sections, so one shuffle round serves two sweeps.
       // Sections 254 and 255 carry no lower coefficient; p_{-1} = p_256 = 0.
       const int J = TOL ? A.jcap : (tm_update ? A.jslow : A.jfast);
-      const float YrmL = kWrap ? __shfl_sync(kFull, Yrm[3].y, src_l)
-                               : __shfl_up_sync(kFull, Yrm[3].y, 1);
-      const float YrmR = __shfl_down_sync(kFull, Yrm[0].x, 1);
+      const float2 Yrmh = f2(kWrap ? __shfl_sync(kFull, Yrm[0].y, src_l)
+                                   : __shfl_up_sync(kFull, Yrm[0].y, 1),
+                             __shfl_down_sync(kFull, Yrm[0].x, 1));
       if (TOL && out_loop == 0 && n_sub >= 2) {
         float2 p2[4];
         load8q(hist + ((n_sub + 1) & 1) * 256 + qb, p2);
@@ -429,7 +432,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           const float sc = __fmul_rn(nr, wb[200]);
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            p[k] = fma2(f2b(sc), o[k], f2(pe[k], pe[k + 4]));
+            p[k] = fma2(f2b(sc), o[k], f2(pe[k], pe[7 - k]));
           n_sw += 1;  // the residual sweep of the features
           __syncwarp();
         } else if (A.guess >= 1) {
@@ -440,51 +443,40 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       int it = 0;
       for (; it + 1 < J; it += 2) {
         float2 T[4], q[4];
+        // halo pairs: (8l-1, 8l+8) and (8l-2, 8l+9)
+        float2 H, H2;
         if (kWrap) {
-          const float L1 = __shfl_sync(kFull, p[3].y, src_l);  // section 8l-1
-          const float L2 = __shfl_sync(kFull, p[2].y, src_l);  // section 8l-2
-          const float R1 = __shfl_down_sync(kFull, p[0].x, 1); // section 8l+8
-          const float R2 = __shfl_down_sync(kFull, p[1].x, 1); // section 8l+9
-          const float qL = __fmaf_rn(-__fadd_rn(L2, p[0].x), rmL, YrmL);
-          const float qR = __fmaf_rn(-__fadd_rn(p[3].y, R2), rmR, YrmR);
-          // t_k = p_{k-1} + p_{k+1} on the pairs (k, k+4)
-          T[0] = add2(f2(L1, p[3].x), p[1]);
-          T[1] = add2(p[0], p[2]);
-          T[2] = fma2(lo2, p[1], p[3]);
-          T[3] = add2(p[2], f2(p[0].y, R1));
-#pragma unroll
-          for (int k = 0; k < 4; ++k) q[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
-          T[0] = add2(f2(qL, q[3].x), q[1]);
-          T[1] = add2(q[0], q[2]);
-          T[2] = fma2(lo2, q[1], q[3]);
-          T[3] = add2(q[2], f2(q[0].y, qR));
+          H = f2(__shfl_sync(kFull, p[0].y, src_l), __shfl_down_sync(kFull, p[0].x, 1));
+          H2 = f2(__shfl_sync(kFull, p[1].y, src_l), __shfl_down_sync(kFull, p[1].x, 1));
         } else {
-          const float L1 = __shfl_up_sync(kFull, p[3].y, 1);   // section 8l-1
-          const float L2 = __shfl_up_sync(kFull, p[2].y, 1);   // section 8l-2
-          const float R1 = __shfl_down_sync(kFull, p[0].x, 1); // section 8l+8
-          const float R2 = __shfl_down_sync(kFull, p[1].x, 1); // section 8l+9
-          float qL = __fmaf_rn(-__fadd_rn(L2, p[0].x), rmL, YrmL);
-          float qR = __fmaf_rn(-__fadd_rn(p[3].y, R2), rmR, YrmR);
-          if (first) qL = 0.0f;
-          if (last) qR = 0.0f;
-          T[0] = add2(f2(first ? 0.0f : L1, p[3].x), p[1]);
-          T[1] = add2(p[0], p[2]);
-          T[2] = add2(p[1], p[3]);
-          T[3] = add2(p[2], f2(p[0].y, R1));
-          if (last) {
-            T[2].y = p[3].y;
-            T[3].y = 0.0f;
-          }
+          H = f2(__shfl_up_sync(kFull, p[0].y, 1), __shfl_down_sync(kFull, p[0].x, 1));
+          H2 = f2(__shfl_up_sync(kFull, p[1].y, 1), __shfl_down_sync(kFull, p[1].x, 1));
+          if (first) H.x = 0.0f;
+        }
+        // the first sweep on the halo sections 8l-1 and 8l+8
+        float2 qh = fma2(neg2(add2(H2, p[0])), rmh, Yrmh);
+        if (!kWrap) {
+          if (first) qh.x = 0.0f;
+          if (last) qh.y = 0.0f;
+        }
+        // t_s = p_{s-1} + p_{s+1} on the mirror pairs
+        T[0] = add2(H, p[1]);
+        T[1] = kWrap ? fma2(lo1, p[2], p[0]) : add2(p[2], p[0]);
+        T[2] = add2(p[1], p[3]);
+        T[3] = f2(__fadd_rn(p[2].x, p[3].y), __fadd_rn(p[2].y, p[3].x));
+        if (!kWrap && last) {
+          T[0].y = 0.0f;
+          T[1].y = p[0].y;
+        }
 #pragma unroll
-          for (int k = 0; k < 4; ++k) q[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
-          T[0] = add2(f2(qL, q[3].x), q[1]);
-          T[1] = add2(q[0], q[2]);
-          T[2] = add2(q[1], q[3]);
-          T[3] = add2(q[2], f2(q[0].y, qR));
-          if (last) {
-            T[2].y = q[3].y;
-            T[3].y = 0.0f;
-          }
+        for (int k = 0; k < 4; ++k) q[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
+        T[0] = add2(qh, q[1]);
+        T[1] = kWrap ? fma2(lo1, q[2], q[0]) : add2(q[2], q[0]);
+        T[2] = add2(q[1], q[3]);
+        T[3] = f2(__fadd_rn(q[2].x, q[3].y), __fadd_rn(q[2].y, q[3].x));
+        if (!kWrap && last) {
+          T[0].y = 0.0f;
+          T[1].y = q[0].y;
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
@@ -506,18 +498,17 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         }
       }
       if (!TOL && it < J) {
-        float left = __shfl_up_sync(kFull, p[3].y, 1);
-        float right = __shfl_down_sync(kFull, p[0].x, 1);
-        if (first) left = 0.0f;
-        if (last) right = 0.0f;
+        float2 H = f2(__shfl_up_sync(kFull, p[0].y, 1), __shfl_down_sync(kFull, p[0].x, 1));
+        if (first) H.x = 0.0f;
+        if (last) H.y = 0.0f;
         float2 T[4];
-        T[0] = add2(f2(left, p[3].x), p[1]);
-        T[1] = add2(p[0], p[2]);
+        T[0] = add2(H, p[1]);
+        T[1] = add2(p[2], p[0]);
         T[2] = add2(p[1], p[3]);
-        T[3] = add2(p[2], f2(p[0].y, right));
+        T[3] = f2(__fadd_rn(p[2].x, p[3].y), __fadd_rn(p[2].y, p[3].x));
         if (last) {
-          T[2].y = p[3].y;
-          T[3].y = right;
+          T[0].y = H.y;
+          T[1].y = p[0].y;
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
