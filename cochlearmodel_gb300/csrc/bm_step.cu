@@ -441,6 +441,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         }
       }
       int it = 0;
+#pragma unroll 2
       for (; it + 1 < J; it += 2) {
         float2 T[4], q[4];
         // halo pairs: (8l-1, 8l+8) and (8l-2, 8l+9)

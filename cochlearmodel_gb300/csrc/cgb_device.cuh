@@ -18,15 +18,15 @@ __device__ __forceinline__ float own_rcpf(float d) {
   return r;
 }
 
-// tanh(x) = x P(x^2) / Q(x^2) with x clamped to [-9.5, 9.5] (where the
-// fit evaluates above 1): P and Q of degree 4 in x^2 (a minimax-relative
-// rational fit on [0, 9], derived by cochlearmodel_gb300/fit_tanh.py), Horner
-// in x^2, quotient as x P times own_rcpf(Q) (Q >= 1), result clamped to
-// [-1, 1].  One branch-free path, <= 5.5 ulp; the CPU oracle evaluates the
-// same sequence.
+// tanh(x) = x P(z) / Q(z), z = min(x^2, 9.5^2): P and Q of degree 4 in z (a
+// minimax-relative rational fit on [0, 9], derived by
+// cochlearmodel_gb300/fit_tanh.py), Horner in z, quotient as x P times
+// own_rcpf(Q) (Q >= 1), result clamped to [-1, 1].  From |x| = 9.5 on,
+// |x| P / Q exceeds 1, so the result saturates to +-1 exactly (also for
+// infinite x; NaN gives -1).  One branch-free path, <= 5.5 ulp; the CPU
+// oracle evaluates the same sequence.
 __device__ __forceinline__ float own_tanhf(float x) {
-  const float xc = fminf(fmaxf(x, -9.5f), 9.5f);
-  const float z = __fmul_rn(xc, xc);
+  const float z = fminf(__fmul_rn(x, x), 90.25f);
   float p = 1.335385846346071e-08f;
   p = __fmaf_rn(p, z, 2.0608504200936295e-05f);
   p = __fmaf_rn(p, z, 0.0034955532755702734f);
@@ -37,7 +37,7 @@ __device__ __forceinline__ float own_tanhf(float x) {
   q = __fmaf_rn(q, z, 0.02587684988975525f);
   q = __fmaf_rn(q, z, 0.46714311838150024f);
   q = __fmaf_rn(q, z, 1.0f);
-  const float t = __fmul_rn(__fmul_rn(xc, p), own_rcpf(q));
+  const float t = __fmul_rn(__fmul_rn(x, p), own_rcpf(q));
   return fminf(fmaxf(t, -1.0f), 1.0f);
 }
 
@@ -99,8 +99,8 @@ __device__ __forceinline__ float2 own_rcpf2(float2 d) {
 
 // own_tanhf on a pair: the same operation sequence per element.
 __device__ __forceinline__ float2 own_tanhf2(float2 x) {
-  const float2 xc = f2(fminf(fmaxf(x.x, -9.5f), 9.5f), fminf(fmaxf(x.y, -9.5f), 9.5f));
-  const float2 z = mul2(xc, xc);
+  const float2 z0 = mul2(x, x);
+  const float2 z = f2(fminf(z0.x, 90.25f), fminf(z0.y, 90.25f));
   float2 p = f2b(1.335385846346071e-08f);
   p = fma2(p, z, f2b(2.0608504200936295e-05f));
   p = fma2(p, z, f2b(0.0034955532755702734f));
@@ -111,7 +111,7 @@ __device__ __forceinline__ float2 own_tanhf2(float2 x) {
   q = fma2(q, z, f2b(0.02587684988975525f));
   q = fma2(q, z, f2b(0.46714311838150024f));
   q = fma2(q, z, f2b(1.0f));
-  const float2 t = mul2(mul2(xc, p), own_rcpf2(q));
+  const float2 t = mul2(mul2(x, p), own_rcpf2(q));
   return f2(fminf(fmaxf(t.x, -1.0f), 1.0f), fminf(fmaxf(t.y, -1.0f), 1.0f));
 }
 

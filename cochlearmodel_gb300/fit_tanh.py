@@ -4,8 +4,8 @@ own_tanhf / own_tanhf2 and the oracle's copy).
     python -m cochlearmodel_gb300.fit_tanh
 
 tanh(x) = x P(z) / Q(z), z = x^2, P and Q of degree 4 in z with Q(0) = 1;
-the evaluation clamps x to [-9.5, 9.5] (where x P / Q exceeds 1) and the
-result to [-1, 1], so it saturates to +-1 exactly.  The fit minimises the maximum relative error of P/Q
+the evaluation clamps z to 9.5^2 (from there on |x| P / Q exceeds 1) and
+the result to [-1, 1], so it saturates to +-1 exactly.  The fit minimises the maximum relative error of P/Q
 against tanh(x)/x on [0, 9] by linearised least squares (Sanathanan-Koerner
 iteration: P - f Q weighted by 1/Q_prev) with Lawson's multiplicative
 reweighting towards the minimax solution; the best iterate is kept.  The

@@ -23,6 +23,8 @@ def test_own_tanh_accuracy():
     neg = np.array([orc.tanhf(float(-x)) for x in xs], np.float32)
     assert np.array_equal(neg, -got)
     assert orc.tanhf(0.0) == 0.0 and orc.tanhf(30.0) == 1.0 and orc.tanhf(-30.0) == -1.0
+    for big in (9.5, 9.500001, 1e30, float("inf")):
+        assert orc.tanhf(big) == 1.0 and orc.tanhf(-big) == -1.0, big
 
 
 def test_thomas_matches_dense_solve():
