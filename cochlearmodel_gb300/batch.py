@@ -204,7 +204,6 @@ class BatchSweep:
         about equal lambda rows, each with its own uploaded tables."""
         if getattr(self, "_chunks", None) is not None and self._n_chunks == chunks:
             return self._chunks
-        torch = self.torch
         rows = self.frames["lam_rows"].astype(np.int64)
         cum = np.cumsum(rows)
         bounds = [0]
@@ -213,22 +212,10 @@ class BatchSweep:
             if bounds[-1] < b < len(rows):
                 bounds.append(b)
         bounds.append(len(rows))
-        out = []
-        for a, b in zip(bounds[:-1], bounds[1:]):
-            fr = np.ascontiguousarray(self.frames[a:b])
-            need = self.lib.cgb_ihc_lambda_scratch_bytes(len(fr), len(self.ihc.ac),
-                                                         len(self.ihc.dc))
-            sc = torch.empty(int(need), dtype=torch.uint8, device=self.device)
-            native.check(self.lib.cgb_ihc_lambda_upload_dev(
-                native.ptr(fr), len(fr), native.ptr(self.ihc.ac), len(self.ihc.ac),
-                native.ptr(self.ihc.dc), len(self.ihc.dc), C.byref(self.ihc.prm), self.v_rows,
-                self.lam_rows, 1, native.ptr(sc), int(sc.numel()), self._stream(None)),
-                "cgb_ihc_lambda_upload_dev")
-            r0 = int(fr["lam_row0"][0])
-            r1 = int(fr["lam_row0"][-1] + fr["lam_rows"][-1])
-            out.append((fr, sc, r0, r1))
-        self._chunks, self._n_chunks = out, chunks
-        return out
+        groups = [self.frames[a:b] for a, b in zip(bounds[:-1], bounds[1:])]
+        self._chunks = self.ihc.upload_chunks(groups, self.v_rows, self.lam_rows)
+        self._n_chunks = chunks
+        return self._chunks
 
     def step_host(self, h_tables, h_v, h_lam, chunks: int = 4):
         """One step through host buffers (pinned): the profile tables in, the
@@ -238,36 +225,16 @@ class BatchSweep:
         computes; only the last chunk's rows are copied after the compute.
         Results equal step() followed by the copies."""
         torch = self.torch
-        s0 = torch.cuda.current_stream(self.device)
         if getattr(self, "_copy_stream", None) is None:
             self._copy_stream = torch.cuda.Stream(self.device)
-        s1 = self._copy_stream
         parts = self._chunk_tables(chunks)
         for pg, h in zip(self.per_group, h_tables):
             pg["d_prof"].copy_(h, non_blocking=True)
         self.generate_input()
         self.solve_bm()
-        e = torch.cuda.Event()
-        e.record(s0)
-        s1.wait_event(e)
-        with torch.cuda.stream(s1):
-            h_v.copy_(self.d_v, non_blocking=True)
-        for fr, sc, r0, r1 in parts:
-            native.check(self.lib.cgb_ihc_lambda_launch_dev(
-                native.ptr(self.d_v), self.v_rows, native.ptr(fr), len(fr),
-                native.ptr(self.ihc.ac), len(self.ihc.ac), native.ptr(self.ihc.dc),
-                len(self.ihc.dc), C.byref(self.ihc.prm), native.ptr(self.ihc.dmg), 1,
-                native.ptr(self.ihc.aihc), native.ptr(self.d_lam), self.lam_rows, None,
-                native.ptr(sc), int(sc.numel()), native.ptr(self.ihc.status),
-                self._stream(s0)), "cgb_ihc_lambda_launch_dev")
-            ec = torch.cuda.Event()
-            ec.record(s0)
-            s1.wait_event(ec)
-            with torch.cuda.stream(s1):
-                for j in range(3):  # one contiguous copy per lambda plane
-                    h_lam[j, r0:r1].copy_(self.d_lam[j, r0:r1], non_blocking=True)
+        self.ihc.run_overlapped(self.d_v, parts, self.d_lam, h_v, h_lam, self._copy_stream)
         self.jnd_sums()
-        s0.wait_stream(s1)
+        torch.cuda.current_stream(self.device).wait_stream(self._copy_stream)
 
     def step(self, stream=None):
         self.generate_input(stream)

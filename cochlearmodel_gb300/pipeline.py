@@ -13,7 +13,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import native
-from .ihc import FRAME_DTYPE, IHCStage, NerveConfig, reference_frame
+from .ihc import FRAME_DTYPE, IHCStage, NerveConfig, reference_frame, split_frame
 from .model import ModelVectors, RunConfig, bm_scalars, reference_units, spl_to_amplitude
 
 F32 = np.float32
@@ -230,6 +230,34 @@ class ProfileRun:
             self.jnd_win.delta_alpha_time_factor * self.cfg.Fs,
             native.ptr(self.d_FRA), native.ptr(self.d_FAI), None, self._stream(stream)),
             "cgb_jnd_dev")
+
+    def step_host(self, h_tables, h_v, h_lam, chunks: int = 4):
+        """One step through host buffers (pinned): the profile table in, the
+        whole path, velocity and the three lambda planes out.  The copies run
+        on a second stream, overlapped with compute: velocity while the IHC
+        stage runs, and each IHC chunk's lambda rows while the next chunk
+        computes.  The chunks are the run's frame cut at interval boundaries
+        (ihc.split_frame), so the results equal step() followed by the
+        copies."""
+        torch = self.torch
+        if not self.want_lambda:
+            raise ValueError("step_host needs the lambda stage")
+        if getattr(self, "_copy_stream", None) is None:
+            self._copy_stream = torch.cuda.Stream(self.device)
+        if getattr(self, "_chunks", None) is None or self._n_chunks != chunks:
+            parts = split_frame(self.frames, chunks)
+            self._chunks = self.ihc.upload_chunks([parts[i:i + 1] for i in range(len(parts))],
+                                                  self.rows, self.lam_rows)
+            self._n_chunks = chunks
+        for d_t, h_t in zip([self.d_prof], h_tables):
+            d_t.copy_(h_t, non_blocking=True)
+        self.generate_input()
+        self.solve_bm()
+        self.ihc.run_overlapped(self.d_v, self._chunks, self.d_lam, h_v, h_lam,
+                                self._copy_stream)
+        if self.calc_jnd:
+            self.jnd_sums()
+        torch.cuda.current_stream(self.device).wait_stream(self._copy_stream)
 
     def step(self, stream=None):
         """One pass of the path over the whole sweep (device buffers only)."""
