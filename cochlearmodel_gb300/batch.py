@@ -217,7 +217,7 @@ class BatchSweep:
         self._n_chunks = chunks
         return self._chunks
 
-    def step_host(self, h_tables, h_v, h_lam, chunks: int = 4):
+    def step_host(self, h_tables, h_v, h_lam, chunks: int = 8):
         """One step through host buffers (pinned): the profile tables in, the
         whole path, velocity and the three lambda planes out.  The copies run
         on a second stream, overlapped with compute: velocity while the IHC

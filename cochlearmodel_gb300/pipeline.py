@@ -231,7 +231,7 @@ class ProfileRun:
             native.ptr(self.d_FRA), native.ptr(self.d_FAI), None, self._stream(stream)),
             "cgb_jnd_dev")
 
-    def step_host(self, h_tables, h_v, h_lam, chunks: int = 4):
+    def step_host(self, h_tables, h_v, h_lam, chunks: int = 8):
         """One step through host buffers (pinned): the profile table in, the
         whole path, velocity and the three lambda planes out.  The copies run
         on a second stream, overlapped with compute: velocity while the IHC
