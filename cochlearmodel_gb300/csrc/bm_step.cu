@@ -310,7 +310,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       prev.load(4, qb, u0);
       prev.load(5, qb, ps0);
       prev.load(6, qb, dp0);
-      if (out_loop == 0 || reset) {
+      if (__all_sync(kFull, out_loop == 0 || reset)) {
         out_loop = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -492,7 +492,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           }
           dm = warp_max_xor(dm);
           pm = warp_max_xor(pm);
-          if (dm <= __fmul_rn(A.jtol, pm)) {
+          if (__all_sync(kFull, dm <= __fmul_rn(A.jtol, pm))) {
             it += 2;
             break;
           }
@@ -541,15 +541,19 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         const float ev = warp_sum_xor(evp);
         const float F = warp_sum_xor(fp);
         const float L = ev > mmspt ? __fdiv_rn(__fmul_rn(ea, dt), ev) : 0.0f;
-        if (L > 6.0f) {
+        // Step decisions are the same in every lane (they come from warp
+        // reductions and uniform counters); taking them through a vote makes
+        // that visible to the compiler, which then branches without
+        // reconvergence barriers.
+        if (__all_sync(kFull, L > 6.0f)) {
           dt = __fmul_rn(dt, 0.5f);
           if (dt < A.dtmin) dt = A.dtmin;
           another = 0;
           reset = 1;
-        } else if (F > 0.0f) {
+        } else if (__all_sync(kFull, F > 0.0f)) {
           another = 1;
           reset = 0;
-        } else if (L < 0.5f) {
+        } else if (__all_sync(kFull, L < 0.5f)) {
           dt = __fmul_rn(dt, 2.0f);
           if (dt > A.dtmax) dt = A.dtmax;
           another = 0;
@@ -568,18 +572,18 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         reset = 1;
         fail_flag = 1;
       }
-    } while (another);
+    } while (__all_sync(kFull, another));
     ++n_sub;
     n_it += out_loop;
     smp_sub = __fadd_rn(smp_sub, 1.0f);
     smp_dt = __fadd_rn(smp_dt, dt);
     smp_it = __fadd_rn(smp_it, (float)out_loop);
 
-    if (tau > A.tout) {
+    if (__all_sync(kFull, tau > A.tout)) {
       tau -= A.tout;
       sx0 = sx1;
       sx1 = inb[n + 2];
-      if (n >= un.out_first) {
+      if (__all_sync(kFull, n >= un.out_first)) {
         store8p(outb + (int64_t)n * 256 + base, v);
         if (fb && lane == 0) fb[n] = fail_flag;
         if (cb && lane == 0) {
