@@ -440,10 +440,10 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           for (int k = 0; k < 4; ++k) p[k] = fma2(f2b(rho), sub2(p[k], p2[k]), p[k]);
         }
       }
-      int it = 0;
-#pragma unroll 2
-      for (; it + 1 < J; it += 2) {
-        float2 T[4], q[4];
+      // two sweeps with one shuffle round; q holds the first sweep's result
+      float2 q[4];
+      auto sweep_pair = [&]() {
+        float2 T[4];
         // halo pairs: (8l-1, 8l+8) and (8l-2, 8l+9)
         float2 H, H2;
         if (kWrap) {
@@ -481,20 +481,32 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
-        if (TOL) {
-          float dm = 0.0f, pm = 0.0f;
+      };
+      int it = 0;
+      if (!TOL && J == 20) {
+        // the reference schedule's slow count, fully unrolled
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const float2 e = abs2(sub2(p[k], q[k]));
-            const float2 ap = abs2(p[k]);
-            dm = fmaxf(dm, fmaxf(e.x, e.y));
-            pm = fmaxf(pm, fmaxf(ap.x, ap.y));
-          }
-          dm = warp_max_xor(dm);
-          pm = warp_max_xor(pm);
-          if (__all_sync(kFull, dm <= __fmul_rn(A.jtol, pm))) {
-            it += 2;
-            break;
+        for (int r = 0; r < 10; ++r) sweep_pair();
+        it = 20;
+      } else {
+#pragma unroll 2
+        for (; it + 1 < J; it += 2) {
+          sweep_pair();
+          if (TOL) {
+            float dm = 0.0f, pm = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const float2 e = abs2(sub2(p[k], q[k]));
+              const float2 ap = abs2(p[k]);
+              dm = fmaxf(dm, fmaxf(e.x, e.y));
+              pm = fmaxf(pm, fmaxf(ap.x, ap.y));
+            }
+            dm = warp_max_xor(dm);
+            pm = warp_max_xor(pm);
+            if (__all_sync(kFull, dm <= __fmul_rn(A.jtol, pm))) {
+              it += 2;
+              break;
+            }
           }
         }
       }
