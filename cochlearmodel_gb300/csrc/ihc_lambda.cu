@@ -42,7 +42,7 @@ constexpr int kBoxRows = 64;   // rows per TMA box
 constexpr int kIhcWarps = 16;
 constexpr int kRB = 8;         // output rows per register block
 constexpr long long kWaitPolls = 1ll << 26;
-constexpr int kTilesPerRun = 8;  // consecutive tiles per CTA
+constexpr int kTilesPerRun = 8;  // consecutive tiles per CTA (short runs)
 
 struct IHCArgs {
   const cgb_ihc_frame* frames;
@@ -420,6 +420,30 @@ void pick_tile(int n_ac, int n_dc, int* TR, int* xrows) {
   *xrows = ax;
 }
 
+// Tiles per CTA run.  A run's first tile recomputes the DC filter's n_dc - 1
+// look-back rows, so longer runs cost less; the longest of 32 and 16 tiles
+// that still leaves at least two CTAs per SM (eight section blocks per run),
+// else 8.  Runs need TR >= n_dc (the look-back is inherited in place).  The
+// choice depends only on the frame table and the device, so the upload and
+// the launch of one table agree.
+int pick_run(const cgb_ihc_frame* frames, int n_frames, int TR, int n_dc) {
+  if (TR < n_dc) return 1;
+  int dev = 0, n_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      n_sm < 1)
+    n_sm = 1 << 20;  // unknown: keep the short runs
+  for (int r : {32, 16}) {
+    long long runs = 0;
+    for (int i = 0; i < n_frames; ++i) {
+      const long long tiles = ((long long)frames[i].lam_rows + TR - 1) / TR;
+      runs += (tiles + r - 1) / r;
+    }
+    if (runs * (256 / kSecTile) >= 2LL * n_sm) return r;
+  }
+  return kTilesPerRun;
+}
+
 }  // namespace
 }  // namespace cgb
 
@@ -460,9 +484,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   int TR = 0, xrows = 0;
   pick_tile(n_ac, n_dc, &TR, &xrows);
   if (TR < 32) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
-  // runs of tiles inherit the DC look-back rows from the tile before, an
-  // in-place shift that needs TR >= n_dc
-  const int run = TR >= n_dc ? kTilesPerRun : 1;
+  const int run = pick_run(frames, n_frames, TR, n_dc);
   for (int i = 0; i < n_frames; ++i) {
     const cgb_ihc_frame& fr = frames[i];
     const bool ok = fr.v_row0 >= 0 && fr.lam_rows >= 0 && fr.lam_rows <= fr.rows &&
@@ -666,7 +688,7 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   pick_tile(n_ac, n_dc, &TR, &xrows);
   if (TR < 32)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: filters too long for one tile");
-  const int run = TR >= n_dc ? kTilesPerRun : 1;
+  const int run = pick_run(frames, n_frames, TR, n_dc);
   int32_t prefix[kNoAllocMaxFrames + 1];
   prefix[0] = 0;
   for (int i = 0; i < n_frames; ++i) {
