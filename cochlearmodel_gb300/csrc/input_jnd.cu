@@ -97,6 +97,8 @@ __device__ __forceinline__ void jnd_interval(const float* __restrict__ lam, int6
   const float* rf = lam + ((int64_t)j * plane_rows + ref_row) * 256 + s;
   double sum_c = 0.0, sum_r = 0.0, sum_ai = 0.0;
   const int nb = len / kJndRows;
+  // two blocks per pass keep twice the loads in flight (same order of sums)
+#pragma unroll 2
   for (int b = g; b < nb; b += kJndGroups) {
     const int t = b * kJndRows;
     float pc = 0.0f, pr = 0.0f, pa = 0.0f;
