@@ -60,6 +60,7 @@ struct IHCArgs {
   int TR, xrows;               // output rows per tile, staged rows (multiple of 64)
   int32_t* status;
   int dc_uniform;              // all DC taps equal: running window sum
+  int ac_sym;                  // AC taps symmetric: FIR over tap pairs
   int run;                     // tiles per CTA (consecutive, one frame)
   const float* ac_ext;         // AC by velocity row (the IIR path), or null: the FIR
 };
@@ -91,6 +92,15 @@ struct Dot2 {
     s = t;
     c = __fadd_rn(c, __fadd_rn(e, q));
   }
+  // b (x1 + x2) for a symmetric tap pair: the pair sum by TwoSum, Dot2 on
+  // its rounded value, b times its rounding error into c by one fma
+  __device__ __forceinline__ void add_pair(float b, float x1, float x2) {
+    const float sg = __fadd_rn(x1, x2);
+    const float zz = __fsub_rn(sg, x1);
+    const float ep = __fadd_rn(__fsub_rn(x1, __fsub_rn(sg, zz)), __fsub_rn(x2, zz));
+    add(b, sg);
+    c = __fmaf_rn(b, ep, c);
+  }
   __device__ __forceinline__ float result() const { return __fadd_rn(s, c); }
 };
 
@@ -107,6 +117,13 @@ struct Dot2x2 {
     const float2 e = add2(sub2(s, sub2(t, z)), sub2(p, z));
     s = t;
     c = add2(c, add2(e, q));
+  }
+  __device__ __forceinline__ void add_pair(float2 b, float2 x1, float2 x2) {
+    const float2 sg = add2(x1, x2);
+    const float2 zz = sub2(sg, x1);
+    const float2 ep = add2(sub2(x1, sub2(sg, zz)), sub2(x2, zz));
+    add(b, sg);
+    c = fma2(b, ep, c);
   }
   __device__ __forceinline__ float2 result() const { return add2(s, c); }
 };
@@ -144,6 +161,64 @@ __device__ __forceinline__ void fir_block8(const float* __restrict__ src,
     out[j] = r.x;
     out[j + 4] = r.y;
   }
+}
+
+// fir_block8 for a symmetric (linear-phase) filter of n taps, b_k = b_{n-1-k}:
+// for each tap pair k the rows t-k and t-(n-1)+k are added exactly first
+// (Dot2::add_pair), then the centre tap of an odd filter.  Two windows move
+// in opposite directions: W1 (rows t-k, as in fir_block8) and W2 (rows
+// t-(n-1)+k), one shared-memory load each per tap pair.  The rows read lie
+// in [kb - n + 1, kb + 7], inside the staged window.
+__device__ __forceinline__ void fir_block8_sym(const float* __restrict__ src,
+                                               const float* __restrict__ b, int n,
+                                               float (&out)[kRB]) {
+  float2 W1[4], W2[4];
+  Dot2x2 acc[4];
+  const int o2 = -(n - 1) * kSecTile;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    acc[j].init();
+    W1[j] = f2(src[j * kSecTile], src[(j + 4) * kSecTile]);
+    W2[j] = f2(src[o2 + j * kSecTile], src[o2 + (j + 4) * kSecTile]);
+  }
+  const int half = n / 2;
+#pragma unroll 2
+  for (int k = 0; k < half; ++k) {
+    const float2 bk = f2b(b[k]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[j].add_pair(bk, W1[j], W2[j]);
+    const float w13 = W1[3].x;
+    W1[3] = W1[2];
+    W1[2] = W1[1];
+    W1[1] = W1[0];
+    W1[0] = f2(src[-(k + 1) * kSecTile], w13);
+    const float w20 = W2[0].y;
+    W2[0] = W2[1];
+    W2[1] = W2[2];
+    W2[2] = W2[3];
+    W2[3] = f2(w20, src[o2 + (k + 8) * kSecTile]);
+  }
+  if (n & 1) {
+    const float2 bc = f2b(b[half]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[j].add(bc, W1[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float2 r = acc[j].result();
+    out[j] = r.x;
+    out[j + 4] = r.y;
+  }
+}
+
+// One row of a symmetric filter with all n taps (the order of fir_block8_sym).
+__device__ __forceinline__ float fir_row_sym(const float* __restrict__ src,
+                                             const float* __restrict__ b, int n) {
+  Dot2 acc;
+  acc.init();
+  for (int k = 0; k < n / 2; ++k) acc.add_pair(b[k], src[-k * kSecTile], src[-(n - 1 - k) * kSecTile]);
+  if (n & 1) acc.add(b[n / 2], src[-(n / 2) * kSecTile]);
+  return acc.result();
 }
 
 // s + c += x exactly (Knuth's TwoSum; the rounding error goes to c).
@@ -290,11 +365,18 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
         for (int r = 0; r < kRB; ++r)
           acc[r] = r < nr ? A.ac_ext[((int64_t)f.v_row0 + kb + r) * 256 + s] : 0.0f;
       } else if (fast) {
-        fir_block8(src, bac, A.n_ac, acc);
+        if (A.ac_sym)
+          fir_block8_sym(src, bac, A.n_ac, acc);
+        else
+          fir_block8(src, bac, A.n_ac, acc);
       } else {
 #pragma unroll
-        for (int r = 0; r < kRB; ++r)
-          acc[r] = r < nr ? fir_row(src + r * kSecTile, bac, taps_used(kb + r, f, A.n_ac)) : 0.0f;
+        for (int r = 0; r < kRB; ++r) {
+          const int tu = taps_used(kb + r, f, A.n_ac);
+          acc[r] = r >= nr ? 0.0f
+                   : (A.ac_sym && tu == A.n_ac ? fir_row_sym(src + r * kSecTile, bac, tu)
+                                               : fir_row(src + r * kSecTile, bac, tu));
+        }
       }
 #pragma unroll
       for (int r = 0; r < kRB; ++r) {
@@ -418,6 +500,15 @@ void pick_tile(int n_ac, int n_dc, int* TR, int* xrows) {
   }
   *TR = any;
   *xrows = ax;
+}
+
+// The AC taps as the kernel uses them (scaled in float) are symmetric,
+// b_k == b_{n-1-k}: the FIR then runs over tap pairs (fir_block8_sym).
+int ac_symmetric(const float* ac_taps, int n_ac, float scale) {
+  if (n_ac < 2) return 0;
+  for (int i = 0; i < n_ac / 2; ++i)
+    if (ac_taps[i] * scale != ac_taps[n_ac - 1 - i] * scale) return 0;
+  return 1;
 }
 
 // Tiles per CTA run.  A run's first tile recomputes the DC filter's n_dc - 1
@@ -560,6 +651,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
+  A.ac_sym = ac_symmetric(ac_taps, n_ac, prm->scale);
   const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
   CGB_TRY_CUDA(cudaFuncSetAttribute(ihc_lambda_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -760,6 +852,7 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
   A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
+  A.ac_sym = ac_symmetric(ac_taps, n_ac, prm->scale);
   const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
   CGB_TRY_CUDA(cudaFuncSetAttribute(ihc_lambda_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),

@@ -659,7 +659,8 @@ static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int tot
   if (mode == 2) {
     // The GB300 kernel's arithmetic: float taps (AC taps pre-scaled), each
     // FIR summed over taps in order with the compensated dot product Dot2
-    // (Ogita, Rump, Oishi 2005), own log10, float lambda.
+    // (Ogita, Rump, Oishi 2005) -- for symmetric AC taps and rows with the
+    // whole filter, over tap pairs (dot2s) -- own log10, float lambda.
     auto dot2 = [](const float* b, const float* x, int tu) {
       float s = 0.0f, c = 0.0f;
       for (int i = 0; i < tu; ++i) {
@@ -673,15 +674,45 @@ static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int tot
       }
       return s + c;
     };
+    // Linear-phase (symmetric) taps, rows with the whole filter: the pair
+    // x_{t-k} + x_{t-n+1+k} is formed exactly by TwoSum, Dot2 takes b_k
+    // times its rounded sum, and b_k times the sum's rounding error goes into
+    // the compensation with one fma; the centre tap of an odd filter last.
+    auto dot2s = [](const float* b, const float* x, int n) {
+      float s = 0.0f, c = 0.0f;
+      auto step = [&](float bb, float xx) {
+        float p = bb * xx;
+        float q = fmaf(bb, xx, -p);
+        float t = s + p;
+        float z = t - s;
+        float e = (s - (t - z)) + (p - z);
+        s = t;
+        c = c + (e + q);
+      };
+      for (int k = 0; k < n / 2; ++k) {
+        const float x1 = x[-(int64_t)k * NS], x2 = x[-(int64_t)(n - 1 - k) * NS];
+        const float sg = x1 + x2;
+        const float zz = sg - x1;
+        const float ep = (x1 - (sg - zz)) + (x2 - zz);
+        step(b[k], sg);
+        c = fmaf(b[k], ep, c);
+      }
+      if (n & 1) step(b[n / 2], x[-(int64_t)(n / 2) * NS]);
+      return s + c;
+    };
     std::vector<float> acf((size_t)rows * NS), dsf((size_t)rows * NS);
     std::vector<float> bt(n_ac), dt(n_dc);
     for (int i = 0; i < n_ac; ++i) bt[i] = (float)(ac_taps[i] * scale);
     for (int i = 0; i < n_dc; ++i) dt[i] = (float)dc_taps[i];
+    bool ac_sym = n_ac > 1;
+    for (int i = 0; i < n_ac / 2; ++i) ac_sym = ac_sym && bt[i] == bt[n_ac - 1 - i];
     const float sc = (float)scale, ea = (float)eta_ac, ed = (float)eta_dc;
     for (int k = 0; k < lam_rows; ++k) {
       int tu = fir_taps_used(k, seg, frdp, total, n_ac);
       for (int s = 0; s < NS; ++s) {
-        float acc = ac_in ? ac_in[(size_t)k * NS + s] : dot2(bt.data(), v + (size_t)k * NS + s, tu);
+        float acc = ac_in ? ac_in[(size_t)k * NS + s]
+                          : (ac_sym && tu == n_ac ? dot2s(bt.data(), v + (size_t)k * NS + s, tu)
+                                                  : dot2(bt.data(), v + (size_t)k * NS + s, tu));
         acf[(size_t)k * NS + s] = acc;
         float ms = fmaf(v[(size_t)k * NS + s], sc, -acc);
         dsf[(size_t)k * NS + s] = ms * ms;

@@ -72,6 +72,32 @@ def test_many_tiles_and_frames(stage):
     _check(stage, v, frames, lam0)
 
 
+@pytest.mark.parametrize("kind", ["asymmetric", "even_symmetric"])
+def test_other_ac_filters(kind):
+    """The FIR paths besides the default odd symmetric filter (tap pairs plus a
+    centre tap): an asymmetric filter takes the plain Dot2 over taps, an even
+    symmetric one the tap pairs alone.  Bit-exact against the oracle and
+    within the lambda bar, on frames with look-back restarts."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    base = ihc.design_ac_lowpass().astype(np.float64)
+    if kind == "asymmetric":
+        taps = base * (1.0 + 0.3 * np.arange(len(base)) / (len(base) - 1))
+    else:
+        taps = 0.5 * (base[:-1] + base[1:])
+    taps = (taps / taps.sum()).astype(np.float32)
+    st = ihc.IHCStage("cuda:0", ac_taps=taps)
+    rng = np.random.default_rng(11)
+    t = np.arange(2600)[:, None] / 1e5
+    f = 250 + 45 * np.arange(256)[None, :]
+    v = (1e-3 * np.sin(2 * np.pi * f * t) * (1 + rng.random((1, 256)))).astype(np.float32)
+    frames = np.zeros(2, ihc.FRAME_DTYPE)
+    frames[0] = (0, 0, 1300, 1300, 650, 1300, ihc.round64(1300), 0)
+    frames[1] = (1300, 1300, 1300, 1200, 1300, 1200, ihc.round64(1300), 0)
+    _check(st, v, frames, 2500)
+
+
 def test_empty_frame_table(stage):
     lam, _ = stage.run(np.zeros((10, 256), np.float32), np.zeros(0, ihc.FRAME_DTYPE), 4)
     assert not lam.any()
