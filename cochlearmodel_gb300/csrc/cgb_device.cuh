@@ -23,8 +23,9 @@ __device__ __forceinline__ float own_rcpf(float d) {
 // cochlearmodel_gb300/fit_tanh.py), Horner in z, quotient as x P times
 // own_rcpf(Q) (Q >= 1), result clamped to [-1, 1].  From |x| = 9.5 on,
 // |x| P / Q exceeds 1, so the result saturates to +-1 exactly (also for
-// infinite x; NaN gives -1).  One branch-free path, <= 5.5 ulp; the CPU
-// oracle evaluates the same sequence.
+// infinite x; NaN gives -1).  One branch-free path, <= 6.1 ulp (every float
+// in [0, 9.5] checked against double tanh); the CPU oracle evaluates the same
+// sequence.
 __device__ __forceinline__ float own_tanhf(float x) {
   const float z = fminf(__fmul_rn(x, x), 90.25f);
   float p = 1.335385846346071e-08f;

@@ -10,7 +10,8 @@ against tanh(x)/x on [0, 9] by linearised least squares (Sanathanan-Koerner
 iteration: P - f Q weighted by 1/Q_prev) with Lawson's multiplicative
 reweighting towards the minimax solution; the best iterate is kept.  The
 printed float32 values are the ones the kernel and the oracle use; the float
-evaluation (Horner in z, x P times own_rcpf(Q)) stays within 5.5 ulp of tanh.
+evaluation (Horner in z, x P times own_rcpf(Q)) stays within 6.1 ulp of tanh
+(every float in [0, 9.5] checked against double tanh: at most 6.03 ulp).
 """
 from __future__ import annotations
 
