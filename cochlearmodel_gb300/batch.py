@@ -178,18 +178,30 @@ class BatchSweep:
                 native.ptr(self.d_in) + 4 * g.in_base, self._stream(stream)),
                 "cgb_input_gen_dev")
 
-    def solve_bm(self, stream=None):
+    def solve_bm(self, stream=None, h_v=None):
+        """The BM stage; with h_v (pinned, shaped like d_v) every velocity row
+        is stored there too as the kernel writes it."""
         self.bm.run_dev(self.sc, self.d_gamma, self.d_units, len(self.units), self.d_in,
-                        self.d_v, self.d_failed, self.d_stats, stream, extras=self.extras)
+                        self.d_v, self.d_failed, self.d_stats, stream, extras=self.extras,
+                        h_out=h_v)
 
-    def ihc_lambda(self, stream=None):
+    def ihc_lambda(self, stream=None, h_lam=None):
+        """The IHC/lambda stage; with h_lam (pinned, shaped like d_lam) every
+        lambda value is stored there too."""
         sc = self.ihc.scratch(len(self.frames))
-        native.check(self.lib.cgb_ihc_lambda_launch_dev(
-            native.ptr(self.d_v), self.v_rows, native.ptr(self.frames), len(self.frames),
-            native.ptr(self.ihc.ac), len(self.ihc.ac), native.ptr(self.ihc.dc), len(self.ihc.dc),
-            C.byref(self.ihc.prm), native.ptr(self.ihc.dmg), 1, native.ptr(self.ihc.aihc),
-            native.ptr(self.d_lam), self.lam_rows, None, native.ptr(sc), int(sc.numel()),
-            native.ptr(self.ihc.status), self._stream(stream)), "cgb_ihc_lambda_launch_dev")
+        args = [native.ptr(self.d_v), self.v_rows, native.ptr(self.frames), len(self.frames),
+                native.ptr(self.ihc.ac), len(self.ihc.ac), native.ptr(self.ihc.dc),
+                len(self.ihc.dc), C.byref(self.ihc.prm), native.ptr(self.ihc.dmg), 1,
+                native.ptr(self.ihc.aihc), native.ptr(self.d_lam), self.lam_rows, None,
+                native.ptr(sc), int(sc.numel()), native.ptr(self.ihc.status)]
+        if h_lam is None:
+            native.check(self.lib.cgb_ihc_lambda_launch_dev(*args, self._stream(stream)),
+                         "cgb_ihc_lambda_launch_dev")
+        else:
+            native.check_host_mirror(h_lam, self.d_lam, "h_lam")
+            native.check(self.lib.cgb_ihc_lambda_launch_mirror_dev(
+                *args, native.ptr(h_lam), self._stream(stream)),
+                "cgb_ihc_lambda_launch_mirror_dev")
 
     def jnd_sums(self, stream=None):
         """Fisher sums of every interval of every group in one launch."""
@@ -199,42 +211,24 @@ class BatchSweep:
             self.jnd_win.delta_alpha_time_factor * self.Fs, native.ptr(self.d_FRA),
             native.ptr(self.d_FAI), None, self._stream(stream)), "cgb_jnd_batch_dev")
 
-    def _chunk_tables(self, chunks: int):
-        """Frame chunks of the IHC stage for step_host: contiguous groups with
-        about equal lambda rows, each with its own uploaded tables."""
-        if getattr(self, "_chunks", None) is not None and self._n_chunks == chunks:
-            return self._chunks
-        rows = self.frames["lam_rows"].astype(np.int64)
-        cum = np.cumsum(rows)
-        bounds = [0]
-        for c in range(1, chunks):
-            b = int(np.searchsorted(cum, c * cum[-1] / chunks)) + 1
-            if bounds[-1] < b < len(rows):
-                bounds.append(b)
-        bounds.append(len(rows))
-        groups = [self.frames[a:b] for a, b in zip(bounds[:-1], bounds[1:])]
-        self._chunks = self.ihc.upload_chunks(groups, self.v_rows, self.lam_rows)
-        self._n_chunks = chunks
-        return self._chunks
-
-    def step_host(self, h_tables, h_v, h_lam, chunks: int = 8):
+    def step_host(self, h_tables, h_v, h_lam):
         """One step through host buffers (pinned): the profile tables in, the
-        whole path, velocity and the three lambda planes out.  The copies run
-        on a second stream, overlapped with compute: velocity while the IHC
-        stage runs, and each IHC chunk's lambda rows while the next chunk
-        computes; only the last chunk's rows are copied after the compute.
-        Results equal step() followed by the copies."""
-        torch = self.torch
-        if getattr(self, "_copy_stream", None) is None:
-            self._copy_stream = torch.cuda.Stream(self.device)
-        parts = self._chunk_tables(chunks)
+        whole path, velocity and the three lambda planes out.  The kernels
+        store their results into h_v and h_lam as they write them, over the
+        CPU-GPU link while they run: BM each velocity row, the IHC stage each
+        lambda value.  No copy follows the compute.  Rows that no kernel
+        writes are zeroed here, as they are on the device, so the results
+        equal step() followed by copies of d_v and d_lam."""
+        from .solver import host_gaps, zero_host_gaps
+        if getattr(self, "_gaps", None) is None:
+            self._gaps = host_gaps(self.units, self.v_rows, self.frames, self.lam_rows)
+        zero_host_gaps(h_v, h_lam, self._gaps)
         for pg, h in zip(self.per_group, h_tables):
             pg["d_prof"].copy_(h, non_blocking=True)
         self.generate_input()
-        self.solve_bm()
-        self.ihc.run_overlapped(self.d_v, parts, self.d_lam, h_v, h_lam, self._copy_stream)
+        self.solve_bm(h_v=h_v)
+        self.ihc_lambda(h_lam=h_lam)
         self.jnd_sums()
-        torch.cuda.current_stream(self.device).wait_stream(self._copy_stream)
 
     def step(self, stream=None):
         self.generate_input(stream)

@@ -40,6 +40,9 @@ struct BMArgs {
   int n_units;
   const float* in;
   float* out;
+  // host mirror of out (pinned, mapped): its byte offset from out, or 0 for
+  // none; a row's host address is its device address plus the offset
+  long long host_delta;
   int32_t* failed;
   float* conv;  // [rows][3] mean dt, substeps, mean outer iterations per sample
   cgb_unit_stats* stats;
@@ -597,6 +600,10 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       sx1 = inb[n + 2];
       if (__all_sync(kFull, n >= un.out_first)) {
         store8p(outb + (int64_t)n * 256 + base, v);
+        if (A.host_delta)
+          store8p(reinterpret_cast<float*>(reinterpret_cast<char*>(outb + (int64_t)n * 256 + base) +
+                                           A.host_delta),
+                  v);
         if (fb && lane == 0) fb[n] = fail_flag;
         if (cb && lane == 0) {
           cb[(int64_t)n * 3 + 0] = __fdiv_rn(smp_dt, smp_sub);
@@ -786,14 +793,21 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: the weight blob must be 16-byte aligned");
   if ((reinterpret_cast<uintptr_t>(d_out) & 15) || (reinterpret_cast<uintptr_t>(d_secp) & 15))
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: d_out and d_secp must be 16-byte aligned");
+  if (ex && ex->h_out) {
+    const int rc = check_host_mirror(ex->h_out, "cgb_bm_run_dev: h_out");
+    if (rc) return rc;
+  }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  BMArgs A;
+  BMArgs A{};
   A.secp = d_secp;
   A.gamma = d_gamma;
   A.units = d_units;
   A.n_units = n_units;
   A.in = d_in;
   A.out = d_out;
+  A.host_delta = ex && ex->h_out ? (long long)(reinterpret_cast<uintptr_t>(ex->h_out) -
+                                               reinterpret_cast<uintptr_t>(d_out))
+                                  : 0;
   A.failed = d_failed;
   A.conv = d_conv;
   A.stats = d_stats;

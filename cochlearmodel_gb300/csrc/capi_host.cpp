@@ -31,6 +31,22 @@ int cuda_check(int cuda_status, const char* what) {
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+int check_host_mirror(const void* p, const char* what) {
+  if (reinterpret_cast<uintptr_t>(p) & 15)
+    return fail(CGB_ERR_ARG, std::string(what) + ": the host mirror must be 16-byte aligned");
+  cudaPointerAttributes at{};
+  const cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(CGB_ERR_ARG, std::string(what) + ": the host mirror is not a known pointer");
+  }
+  if (at.type != cudaMemoryTypeHost || at.hostPointer != p || at.devicePointer != p)
+    return fail(CGB_ERR_ARG, std::string(what) +
+                                 ": the host mirror must be pinned host memory mapped at the "
+                                 "same address on the device");
+  return 0;
+}
+
 // Physical constants of the model as the reference's #defines produce them
 // (include/const.h:216-297): each macro is a float expression evaluated left
 // to right; CModel stores the result in a double (src/model.cpp:18-55).
@@ -57,7 +73,7 @@ extern "C" {
 
 const char* cgb_last_error(void) { return cgb::g_last_error.c_str(); }
 
-int cgb_abi_version(void) { return 1; }
+int cgb_abi_version(void) { return 2; }
 
 int64_t cgb_kernel_launch_count(void) { return cgb::g_launches.load(); }
 

@@ -13,6 +13,11 @@ int fail(int code, const std::string& msg);
 // Checks a CUDA runtime status; on failure records "<what>: <cuda message>".
 int cuda_check(int cuda_status, const char* what);
 void note_launch();
+// A host mirror receives a kernel's results by device stores over the
+// CPU-GPU link: it must be pinned host memory mapped into the device address
+// space at the same address (cudaHostAlloc, or cudaHostRegister with the
+// mapped flag, under unified addressing) and 16-byte aligned.
+int check_host_mirror(const void* p, const char* what);
 
 }  // namespace cgb
 

@@ -55,6 +55,7 @@ struct IHCArgs {
   const float* dmg;            // [P][256] 10^ihc
   const float* aihc;           // [3][256]
   float* lam;                  // [3][lam_plane_rows][256]
+  float* lam_host;             // host mirror of lam (pinned, mapped), or null
   int64_t lam_plane_rows;
   float* ihc;                  // [lam rows][256] or null
   int TR, xrows;               // output rows per tile, staged rows (multiple of 64)
@@ -407,6 +408,11 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
       A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
       A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
       A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
+      if (A.lam_host) {
+        A.lam_host[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
+        A.lam_host[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
+        A.lam_host[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
+      }
     };
     if (A.dc_uniform) {
       // tiles start on multiples of 32 rows, so every 32-row block opens on
@@ -558,7 +564,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
                     const float* d_aihc, float* d_lam, int64_t lam_plane_rows, float* d_ihc,
                     void* d_scratch, int64_t scratch_bytes, int32_t* d_status, void* stream,
                     int mode,
-                    const float* ac_ext = nullptr) {
+                    const float* ac_ext = nullptr, float* lam_host = nullptr) {
   if (n_frames == 0) return CGB_OK;
   if (!frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_scratch ||
       ((mode & kLaunch) && (!d_v || !d_dmg || !d_aihc || !d_lam || !d_status)))
@@ -569,6 +575,10 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: scratch buffer too small");
   if ((mode & kLaunch) && (reinterpret_cast<uintptr_t>(d_v) & 15))
     return fail(CGB_ERR_ARG, "cgb_ihc_lambda_dev: d_v must be 16-byte aligned");
+  if (lam_host) {
+    const int rc = check_host_mirror(lam_host, "cgb_ihc_lambda_dev: h_lam");
+    if (rc) return rc;
+  }
   if (v_rows > INT32_MAX)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: more than 2^31-1 velocity rows");
   std::vector<int32_t> prefix(n_frames + 1, 0);
@@ -625,7 +635,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   if (cr != CUDA_SUCCESS)
     return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
 
-  IHCArgs A;
+  IHCArgs A{};
   A.frames = reinterpret_cast<const cgb_ihc_frame*>(sc);
   A.tile_prefix = reinterpret_cast<const int32_t*>(sc + fbytes);
   A.n_frames = n_frames;
@@ -642,6 +652,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   A.dmg = d_dmg;
   A.aihc = d_aihc;
   A.lam = d_lam;
+  A.lam_host = lam_host;
   A.lam_plane_rows = lam_plane_rows;
   A.ihc = d_ihc;
   A.TR = TR;
@@ -700,6 +711,19 @@ extern "C" int cgb_ihc_lambda_launch_dev(const float* d_v, int64_t v_rows,
   return cgb::ihc_lambda_impl(d_v, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc, prm,
                               d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc,
                               d_scratch, scratch_bytes, d_status, stream, cgb::kLaunch);
+}
+
+extern "C" int cgb_ihc_lambda_launch_mirror_dev(
+    const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames, int n_frames,
+    const float* ac_taps, int n_ac, const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+    const float* d_dmg, int n_dmg_profiles, const float* d_aihc, float* d_lam,
+    int64_t lam_plane_rows, float* d_ihc, void* d_scratch, int64_t scratch_bytes,
+    int32_t* d_status, float* h_lam, void* stream) {
+  if (!h_lam) return cgb::fail(CGB_ERR_ARG, "cgb_ihc_lambda_launch_mirror_dev: null h_lam");
+  return cgb::ihc_lambda_impl(d_v, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc, prm,
+                              d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc,
+                              d_scratch, scratch_bytes, d_status, stream, cgb::kLaunch, nullptr,
+                              h_lam);
 }
 
 // ---------------------------------------------------------------------------
@@ -826,7 +850,7 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (cr != CUDA_SUCCESS)
     return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
-  IHCArgs A;
+  IHCArgs A{};
   A.frames = reinterpret_cast<const cgb_ihc_frame*>(sc);
   A.tile_prefix = reinterpret_cast<const int32_t*>(sc + kNoAllocPrefixOff);
   A.n_frames = n_frames;

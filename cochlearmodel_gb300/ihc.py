@@ -164,44 +164,6 @@ def reference_frame(cfg: RunConfig, v_row0: int = 0, lam_row0: int = 0,
     return f
 
 
-def split_frame(frame: np.ndarray, parts: int, min_tail: int = 1024) -> np.ndarray:
-    """One frame cut into up to `parts` consecutive frames of about equal
-    lambda rows, with the same result row for row.
-
-    Cuts fall on offsets o that are multiples of both the frame's interval
-    length `seg` and 32, and that leave at least `min_tail` rows (the longest
-    filter) to the last frame.
-    - o % seg == 0 keeps each row's look-back rule, (k + 1) % seg.
-    - o % 32 == 0 keeps the DC window's anchor rows.
-    - The last row (frdp - 1) keeps the full filter when frdp and total move
-      down by o with the rows.
-    Without such an offset the frame comes back whole."""
-    f = np.ascontiguousarray(frame).view(FRAME_DTYPE).reshape(-1)
-    if len(f) != 1:
-        raise ValueError("split_frame takes one frame")
-    f = f[0]
-    seg, frdp, L = int(f["seg"]), int(f["frdp"]), int(f["lam_rows"])
-    unit = seg * 32 // math.gcd(seg, 32)
-    cuts = []
-    for c in range(1, max(1, parts)):
-        o = int(round(c * L / parts / unit)) * unit
-        if 0 < o < L and frdp - o >= min_tail and (not cuts or o > cuts[-1]):
-            cuts.append(o)
-    starts = [0] + cuts
-    out = np.zeros(len(starts), FRAME_DTYPE)
-    for i, o in enumerate(starts):
-        end = starts[i + 1] if i + 1 < len(starts) else L
-        g = out[i:i + 1]
-        g[:] = f
-        g["v_row0"] += o
-        g["lam_row0"] += o
-        g["rows"] -= o
-        g["lam_rows"] = end - o
-        g["frdp"] -= o
-        g["total"] -= o
-    return out
-
-
 class IHCStage:
     """Device-side IHC/lambda stage: damage/A tables, scratch and status."""
 
@@ -264,37 +226,24 @@ class IHCStage:
             out.append((fr, sc, r0, r1))
         return out
 
-    def launch_chunk(self, v, chunk, lam, stream) -> None:
-        """The IHC/lambda launch of one uploaded group (upload_chunks)."""
+    def launch_chunk(self, v, chunk, lam, stream, h_lam=None) -> None:
+        """The IHC/lambda launch of one uploaded group (upload_chunks).  With
+        h_lam (a pinned host tensor shaped like lam) the kernel also stores
+        every lambda value there."""
         fr, sc, _, _ = chunk
-        native.check(self.lib.cgb_ihc_lambda_launch_dev(
-            native.ptr(v), int(v.shape[0]), native.ptr(fr), len(fr), native.ptr(self.ac),
-            len(self.ac), native.ptr(self.dc), len(self.dc), C.byref(self.prm),
-            native.ptr(self.dmg), int(self.dmg.shape[0]), native.ptr(self.aihc), native.ptr(lam),
-            int(lam.shape[1]), None, native.ptr(sc), int(sc.numel()), native.ptr(self.status),
-            C.c_void_p(stream.cuda_stream)), "cgb_ihc_lambda_launch_dev")
-
-    def run_overlapped(self, v, chunks, lam, h_v, h_lam, copy_stream) -> None:
-        """After the BM stage on the current stream: copies the velocity to h_v
-        on copy_stream while the IHC stage runs, one launch per chunk, and each
-        chunk's lambda rows (one contiguous copy per plane) while the next chunk
-        computes.  The caller joins copy_stream before reading the host buffers."""
-        torch = self.torch
-        s0 = torch.cuda.current_stream(self.device)
-        e = torch.cuda.Event()
-        e.record(s0)
-        copy_stream.wait_event(e)
-        with torch.cuda.stream(copy_stream):
-            h_v.copy_(v, non_blocking=True)
-        for ch in chunks:
-            self.launch_chunk(v, ch, lam, s0)
-            ec = torch.cuda.Event()
-            ec.record(s0)
-            copy_stream.wait_event(ec)
-            r0, r1 = ch[2], ch[3]
-            with torch.cuda.stream(copy_stream):
-                for j in range(lam.shape[0]):
-                    h_lam[j, r0:r1].copy_(lam[j, r0:r1], non_blocking=True)
+        args = [native.ptr(v), int(v.shape[0]), native.ptr(fr), len(fr), native.ptr(self.ac),
+                len(self.ac), native.ptr(self.dc), len(self.dc), C.byref(self.prm),
+                native.ptr(self.dmg), int(self.dmg.shape[0]), native.ptr(self.aihc),
+                native.ptr(lam), int(lam.shape[1]), None, native.ptr(sc), int(sc.numel()),
+                native.ptr(self.status)]
+        if h_lam is None:
+            native.check(self.lib.cgb_ihc_lambda_launch_dev(
+                *args, C.c_void_p(stream.cuda_stream)), "cgb_ihc_lambda_launch_dev")
+        else:
+            native.check_host_mirror(h_lam, lam, "h_lam")
+            native.check(self.lib.cgb_ihc_lambda_launch_mirror_dev(
+                *args, native.ptr(h_lam), C.c_void_p(stream.cuda_stream)),
+                "cgb_ihc_lambda_launch_mirror_dev")
 
     def run_iir(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, b, a,
                 want_ihc: bool = False):

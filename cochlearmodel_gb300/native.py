@@ -65,6 +65,8 @@ _SIGS = {
                                        _p]),
     "cgb_ihc_lambda_launch_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64,
                                        _p, _p, _i64, _p, _p]),
+    "cgb_ihc_lambda_launch_mirror_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p,
+                                              _p, _i64, _p, _p, _i64, _p, _p, _p]),
     "cgb_ihc_lambda_noalloc_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p,
                                         _i64, _p, _p, _p]),
     "cgb_input_gen_dev": (_i, [_p, _i, _p, _p, _i, _i, _i, C.c_float, _d, _d, _d, _d, _p, _p]),
@@ -106,9 +108,11 @@ assert JND_INTERVAL_DTYPE.itemsize == 32
 
 
 class BMExtras(C.Structure):
-    """cgb_bm_extras: network weights and training-record logging."""
+    """cgb_bm_extras: network weights, training-record logging and the host
+    mirror of the velocity output (fields left at zero are unused)."""
     _fields_ = [("d_ws_blob", C.c_void_p), ("d_log", C.c_void_p), ("log_cap", C.c_int64),
-                ("log_every", C.c_int32), ("pad_", C.c_int32), ("d_log_count", C.c_void_p)]
+                ("log_every", C.c_int32), ("pad_", C.c_int32), ("d_log_count", C.c_void_p),
+                ("h_out", C.c_void_p)]
 
 
 def lib_path() -> Path:
@@ -142,6 +146,19 @@ def check(status: int, what: str = "") -> None:
     if status != 0:
         msg = load().cgb_last_error().decode(errors="replace")
         raise CGBError(f"{what or 'cochlea_gb300'} failed ({status}): {msg}")
+
+
+def check_host_mirror(t, like, name: str):
+    """A host mirror receives a kernel's stores directly, so its size must be
+    exactly that of the device buffer it mirrors: a pinned, contiguous CPU
+    tensor of the same shape and dtype (torch's pin_memory() maps it into the
+    device address space at the same address)."""
+    ok = (t is not None and t.device.type == "cpu" and t.is_pinned() and t.is_contiguous()
+          and t.dtype == like.dtype and tuple(t.shape) == tuple(like.shape))
+    if not ok:
+        raise ValueError(f"{name} must be a pinned contiguous CPU tensor of shape "
+                         f"{tuple(like.shape)} and dtype {like.dtype}")
+    return t
 
 
 def ptr(a) -> int:

@@ -13,7 +13,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import native
-from .ihc import FRAME_DTYPE, IHCStage, NerveConfig, reference_frame, split_frame
+from .ihc import FRAME_DTYPE, IHCStage, NerveConfig, reference_frame
 from .model import ModelVectors, RunConfig, bm_scalars, reference_units, spl_to_amplitude
 
 F32 = np.float32
@@ -214,9 +214,11 @@ class ProfileRun:
                 native.ptr(self.d_in), self.n_int, self.L, native.ptr(fir), nf, native.ptr(iir),
                 ni, native.ptr(aux), self._stream(stream)), "cgb_hearing_aid_dev")
 
-    def solve_bm(self, stream=None):
+    def solve_bm(self, stream=None, h_v=None):
+        """The BM stage; with h_v (pinned, shaped like d_v) every velocity row
+        is stored there too as the kernel writes it."""
         self.bm.run_dev(self.sc, self.d_gamma, self.d_units, len(self.units), self.d_in,
-                        self.d_v, self.d_failed, self.d_stats, stream)
+                        self.d_v, self.d_failed, self.d_stats, stream, h_out=h_v)
 
     def ihc_lambda(self, stream=None):
         self.ihc.run_dev(self.d_v, self.frames, self.d_lam, None, stream)
@@ -231,33 +233,29 @@ class ProfileRun:
             native.ptr(self.d_FRA), native.ptr(self.d_FAI), None, self._stream(stream)),
             "cgb_jnd_dev")
 
-    def step_host(self, h_tables, h_v, h_lam, chunks: int = 8):
+    def step_host(self, h_tables, h_v, h_lam):
         """One step through host buffers (pinned): the profile table in, the
-        whole path, velocity and the three lambda planes out.  The copies run
-        on a second stream, overlapped with compute: velocity while the IHC
-        stage runs, and each IHC chunk's lambda rows while the next chunk
-        computes.  The chunks are the run's frame cut at interval boundaries
-        (ihc.split_frame), so the results equal step() followed by the
-        copies."""
+        whole path, velocity and the three lambda planes out.  The kernels
+        store their results into h_v and h_lam as they write them, over the
+        CPU-GPU link while they run: BM each velocity row, the IHC stage each
+        lambda value.  Rows that no kernel writes are zeroed here, as they
+        are on the device, so the results equal step() followed by copies of
+        d_v and d_lam."""
+        from .solver import host_gaps, zero_host_gaps
         torch = self.torch
         if not self.want_lambda:
             raise ValueError("step_host needs the lambda stage")
-        if getattr(self, "_copy_stream", None) is None:
-            self._copy_stream = torch.cuda.Stream(self.device)
-        if getattr(self, "_chunks", None) is None or self._n_chunks != chunks:
-            parts = split_frame(self.frames, chunks)
-            self._chunks = self.ihc.upload_chunks([parts[i:i + 1] for i in range(len(parts))],
-                                                  self.rows, self.lam_rows)
-            self._n_chunks = chunks
-        for d_t, h_t in zip([self.d_prof], h_tables):
-            d_t.copy_(h_t, non_blocking=True)
+        if getattr(self, "_whole", None) is None:
+            self._whole = self.ihc.upload_chunks([self.frames], self.rows, self.lam_rows)[0]
+            self._gaps = host_gaps(self.units, self.rows, self.frames, self.lam_rows)
+        zero_host_gaps(h_v, h_lam, self._gaps)
+        self.d_prof.copy_(h_tables[0], non_blocking=True)
         self.generate_input()
-        self.solve_bm()
-        self.ihc.run_overlapped(self.d_v, self._chunks, self.d_lam, h_v, h_lam,
-                                self._copy_stream)
+        self.solve_bm(h_v=h_v)
+        self.ihc.launch_chunk(self.d_v, self._whole, self.d_lam,
+                              torch.cuda.current_stream(self.device), h_lam=h_lam)
         if self.calc_jnd:
             self.jnd_sums()
-        torch.cuda.current_stream(self.device).wait_stream(self._copy_stream)
 
     def step(self, stream=None):
         """One pass of the path over the whole sweep (device buffers only)."""

@@ -25,6 +25,41 @@ def units_to_device(units: np.ndarray, device) -> torch.Tensor:
     return torch.from_numpy(u.view(np.uint8).copy()).to(device)
 
 
+def unwritten_ranges(starts, ends, rows: int) -> list[tuple[int, int]]:
+    """Row ranges of [0, rows) outside every written span [starts[i], ends[i])."""
+    cover = np.zeros(rows + 1, np.int64)
+    np.add.at(cover, np.asarray(starts, np.int64), 1)
+    np.add.at(cover, np.asarray(ends, np.int64), -1)
+    written = (np.cumsum(cover[:-1]) > 0).astype(np.int8)
+    edges = np.flatnonzero(np.diff(np.concatenate([[1], written, [1]])))
+    return [(int(a), int(b)) for a, b in zip(edges[0::2], edges[1::2])]
+
+
+def unit_rows(units: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """First and one-past-last output row each unit writes (when it completes)."""
+    u = np.ascontiguousarray(units).view(native.UNIT_DTYPE)
+    first = u["out_base"] + np.maximum(u["start"], u["out_first"])
+    return first, u["out_base"] + u["end"]
+
+
+def host_gaps(units: np.ndarray, v_rows: int, frames: np.ndarray, lam_rows: int):
+    """Velocity and lambda row ranges that no kernel writes (they stay zero
+    on the device): the padding rows between runs, and rows before a unit's
+    first output."""
+    return (unwritten_ranges(*unit_rows(units), v_rows),
+            unwritten_ranges(frames["lam_row0"], frames["lam_row0"] + frames["lam_rows"],
+                             lam_rows))
+
+
+def zero_host_gaps(h_v, h_lam, gaps) -> None:
+    """Zeroes the host mirrors' rows that no kernel writes."""
+    hv, hl = h_v.numpy(), h_lam.numpy()
+    for a, b in gaps[0]:
+        hv[a:b] = 0
+    for a, b in gaps[1]:
+        hl[:, a:b] = 0
+
+
 class BMSolver:
     """Holds the section parameters and the work-queue scratch on one device."""
 
@@ -45,13 +80,22 @@ class BMSolver:
                 n_units: int, inp: torch.Tensor, out: torch.Tensor,
                 failed: torch.Tensor | None = None, stats: torch.Tensor | None = None,
                 stream: torch.cuda.Stream | None = None, conv: torch.Tensor | None = None,
-                extras: native.BMExtras | None = None) -> None:
+                extras: native.BMExtras | None = None,
+                h_out: torch.Tensor | None = None) -> None:
         """Enqueues the solver on `stream` (default: torch's current stream).
         All tensors live on this solver's device; `units` holds cgb_unit
         records (see units_to_device) already validated by check_units.
         extras: network weights / training-record logging of the tolerance
-        mode (jacobi_mode 2)."""
+        mode (jacobi_mode 2).  h_out: a pinned host tensor shaped like `out`
+        that receives every velocity row as the kernel writes it."""
         st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if h_out is not None:
+            native.check_host_mirror(h_out, out, "h_out")
+            ex = native.BMExtras()
+            if extras is not None:
+                C.memmove(C.addressof(ex), C.addressof(extras), C.sizeof(ex))
+            ex.h_out = h_out.data_ptr()
+            extras = ex
         native.check(self.lib.cgb_bm_run_ex_dev(
             native.ptr(self.secp), native.ptr(gamma), int(gamma.shape[0]), C.byref(sc),
             native.ptr(units), int(n_units), native.ptr(inp), int(inp.numel()),

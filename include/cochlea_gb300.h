@@ -102,6 +102,12 @@ typedef struct cgb_bm_extras {
   int32_t log_every;      /* record every n-th step start of each unit       */
   int32_t pad_;
   int32_t* d_log_count;   /* records claimed (may exceed log_cap)            */
+  float* h_out;           /* host mirror of d_out, or NULL: pinned host memory
+                             mapped at the same address on the device, 16-byte
+                             aligned, out_rows x 256 floats.  The kernel stores
+                             every velocity row there too, as it writes it, so
+                             the rows reach the host while the solve runs;
+                             rows no unit writes are left as they are. */
 } cgb_bm_extras;
 
 /* One frame of the IHC/lambda stage: a run of consecutive velocity rows that
@@ -257,6 +263,18 @@ int cgb_ihc_lambda_launch_dev(const float* d_v, int64_t v_rows, const cgb_ihc_fr
                               int n_dmg_profiles, const float* d_aihc, float* d_lam,
                               int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
                               int64_t scratch_bytes, int32_t* d_status, void* stream);
+/* cgb_ihc_lambda_launch_dev with a host mirror of d_lam: h_lam is pinned host
+ * memory mapped at the same address on the device (16-byte aligned, the
+ * layout of d_lam).  The kernel stores every lambda value there too, so the
+ * three planes reach the host while the stage runs, with no copy after it. */
+int cgb_ihc_lambda_launch_mirror_dev(const float* d_v, int64_t v_rows,
+                                     const cgb_ihc_frame* frames, int n_frames,
+                                     const float* ac_taps, int n_ac, const float* dc_taps,
+                                     int n_dc, const cgb_ihc_params* prm, const float* d_dmg,
+                                     int n_dmg_profiles, const float* d_aihc, float* d_lam,
+                                     int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
+                                     int64_t scratch_bytes, int32_t* d_status, float* h_lam,
+                                     void* stream);
 
 /* IHC + lambda with the AC stage by IIR (the reference's is_ac_iir_filter
  * path, DeviceCudaIIRFilter src/cochlea.cu:2745-2775):

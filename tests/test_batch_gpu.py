@@ -75,8 +75,11 @@ def test_units_longest_first(sweep):
 
 
 def test_step_host_equals_step_and_copies(sweep):
-    """The host-buffer step with copies overlapped on a second stream returns
-    exactly what step() followed by plain copies returns."""
+    """The host-buffer step, whose kernels store their results into the
+    pinned host buffers as they write them, returns exactly what step()
+    followed by plain copies returns.  The buffers start as NaN, so the rows
+    no kernel writes must be zeroed; a second step into the same buffers
+    gives the same values."""
     import torch
     b, _ = sweep
     h_tables = [pg["d_prof"].cpu().pin_memory() for pg in b.per_group]
@@ -85,10 +88,38 @@ def test_step_host_equals_step_and_copies(sweep):
     v0, lam0, f0 = b.d_v.cpu(), b.d_lam.cpu(), b.d_FRA.clone()
     h_v = torch.empty(b.d_v.shape, dtype=torch.float32).pin_memory()
     h_lam = torch.empty(b.d_lam.shape, dtype=torch.float32).pin_memory()
-    for chunks in (1, 3):
-        h_v.zero_()
-        h_lam.zero_()
-        b.step_host(h_tables, h_v, h_lam, chunks=chunks)
+    h_v.fill_(float("nan"))
+    h_lam.fill_(float("nan"))
+    for _ in range(2):
+        b.step_host(h_tables, h_v, h_lam)
         torch.cuda.synchronize()
         assert torch.equal(h_v, v0) and torch.equal(h_lam, lam0)
         assert torch.equal(b.d_FRA, f0)
+    assert len(b._gaps[0]) > 0  # the groups' padding rows were zeroed
+
+
+def test_host_mirror_rejects_bad_buffers(sweep):
+    """A host mirror must match its device buffer and be pinned: the Python
+    layer rejects a short or pageable tensor, and the library rejects a
+    pageable host pointer and a device pointer, before anything launches."""
+    import ctypes as C
+    import torch
+    from cochlearmodel_gb300 import native
+    b, _ = sweep
+    short = torch.empty((b.d_v.shape[0] - 1, 256), dtype=torch.float32).pin_memory()
+    with pytest.raises(ValueError):
+        b.solve_bm(h_v=short)
+    with pytest.raises(ValueError):
+        b.ihc_lambda(h_lam=torch.empty(b.d_lam.shape, dtype=torch.float32))
+    lib = native.load()
+    pageable = np.zeros((b.d_v.shape[0], 256), np.float32)
+    for bad in (pageable.ctypes.data, b.d_v.data_ptr()):
+        ex = native.BMExtras()
+        ex.h_out = bad
+        rc = lib.cgb_bm_run_ex_dev(
+            native.ptr(b.bm.secp), native.ptr(b.d_gamma), 1, C.byref(b.sc), native.ptr(b.d_units),
+            len(b.units), native.ptr(b.d_in), int(b.d_in.numel()), native.ptr(b.d_v),
+            int(b.d_v.shape[0]), None, None, None, native.ptr(b.bm.work),
+            C.cast(C.byref(ex), C.c_void_p), None)
+        assert rc == 1 and b"host mirror" in lib.cgb_last_error()
+    torch.cuda.synchronize()

@@ -76,12 +76,10 @@ def test_jnd_sums_and_db(run):
 
 
 def test_profile_step_host_equals_step_and_copies(mv):
-    """The host-buffer step of a profile run (velocity copied during the IHC
-    stage, the lambda rows of each frame chunk during the next chunk) returns
-    exactly what step() followed by plain copies returns, for the frame whole
-    and cut at interval boundaries (256-row intervals, 22 of them)."""
+    """The host-buffer step of a profile run, whose kernels store their
+    results into the pinned host buffers as they write them, returns exactly
+    what step() followed by plain copies returns (buffers starting as NaN)."""
     import torch
-    from cochlearmodel_gb300 import ihc
     cfg = model.RunConfig(Time_Block_Length=0.00128, Decouple_Filter=2, Overlap_Time=0.0005,
                           OHC_Vector=np.linspace(0.5, 0.05, 256, dtype=np.float32))
     sweep = ProfileSweep(frequencies=[500.0, 1000.0, 2000.0, 3000.0, 4000.0],
@@ -89,18 +87,15 @@ def test_profile_step_host_equals_step_and_copies(mv):
     noise = np.random.default_rng(3).standard_normal(300).astype(np.float32)
     r = ProfileRun("cuda:0", cfg, sweep, noise=noise, mv=mv,
                    jnd=JNDWindow(head=0.0003, tail=0.0002))
-    assert int(r.frames["seg"][0]) == 256 and len(ihc.split_frame(r.frames, 4)) == 4
     h_tables = [r.d_prof.cpu().pin_memory()]
     r.step()
     torch.cuda.synchronize()
     v0, lam0, f0 = r.d_v.cpu(), r.d_lam.cpu(), r.d_FRA.clone()
     h_v = torch.empty(r.d_v.shape, dtype=torch.float32).pin_memory()
     h_lam = torch.empty(r.d_lam.shape, dtype=torch.float32).pin_memory()
-    for chunks in (1, 4):
-        h_v.zero_()
-        h_lam.zero_()
-        r.step_host(h_tables, h_v, h_lam, chunks=chunks)
-        torch.cuda.synchronize()
-        assert len(r._chunks) == chunks
-        assert torch.equal(h_v, v0) and torch.equal(h_lam, lam0)
-        assert torch.equal(r.d_FRA, f0)
+    h_v.fill_(float("nan"))
+    h_lam.fill_(float("nan"))
+    r.step_host(h_tables, h_v, h_lam)
+    torch.cuda.synchronize()
+    assert torch.equal(h_v, v0) and torch.equal(h_lam, lam0)
+    assert torch.equal(r.d_FRA, f0)
