@@ -20,8 +20,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import native
-from .ihc import FRAME_DTYPE, IHCStage, NerveConfig, reference_frame
-from .model import ModelVectors, RunConfig, bm_scalars, reference_units, spl_to_amplitude
+from .ihc import IHCStage, NerveConfig, reference_frame
+from .model import ModelVectors, RunConfig, bm_scalars, reference_units
 from .pipeline import JNDWindow, ProfileSweep
 
 F32 = np.float32

@@ -13,7 +13,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import native
-from .ihc import FRAME_DTYPE, IHCStage, NerveConfig, reference_frame
+from .ihc import IHCStage, NerveConfig, reference_frame
 from .model import ModelVectors, RunConfig, bm_scalars, reference_units, spl_to_amplitude
 
 F32 = np.float32

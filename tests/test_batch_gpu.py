@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from cochlearmodel_gb300 import batch
-from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun, ProfileSweep
+from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun
 
 pytestmark = pytest.mark.gpu
 

@@ -3,7 +3,7 @@
 import numpy as np
 import pytest
 
-from cochlearmodel_gb300 import model, native
+from cochlearmodel_gb300 import model
 from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun, ProfileSweep
 from oracle import oracle as orc
 
