@@ -145,3 +145,33 @@ def test_trained_network_gain(mv, bm_solver):
           (r0["sweeps_per_step"], r1["sweeps_per_step"], r2["sweeps_per_step"]))
     assert r0["status"] == r1["status"] == r2["status"] == 0
     assert r2["sweeps_per_step"] < 0.85 * r0["sweeps_per_step"]
+
+
+def test_host_mirror_keeps_the_extras(bm_solver, ws_data):
+    """A host mirror merged into extras that carry the network weights (the
+    learned guess): the kernel still finds the weights, the device velocity
+    equals the run without the mirror, and the pinned host buffer holds
+    exactly the rows the kernel wrote."""
+    import torch
+    from cochlearmodel_gb300.solver import unit_rows, units_to_device
+    W, net = ws_data[0], ws_data[1]
+    batch = W.signal_batch(2, ms=2.0, seed=9)
+    d = bm_solver.device
+    sc = model.tolerance_mode(model.bm_scalars(batch.cfg, bm_solver.mv), guess=2,
+                              learned_every=4)
+    gamma = torch.from_numpy(np.ascontiguousarray(batch.cfg.gamma()[None], np.float32)).to(d)
+    u = units_to_device(batch.units, d)
+    x = torch.from_numpy(batch.inp).to(d)
+    runs = []
+    for mirror in (False, True):
+        out = torch.zeros((batch.out_rows, 256), dtype=torch.float32, device=d)
+        h = torch.full((batch.out_rows, 256), float("nan")).pin_memory() if mirror else None
+        bm_solver.run_dev(sc, gamma, u, len(batch.units), x, out, extras=net.extras(), h_out=h)
+        torch.cuda.synchronize(d)
+        runs.append((out.cpu(), h))
+    (v0, _), (v1, h) = runs
+    assert torch.equal(v0, v1)
+    first, end = unit_rows(batch.units)
+    assert (end > first).all()
+    for a, b in zip(first, end):
+        assert torch.equal(h[a:b], v1[a:b])
