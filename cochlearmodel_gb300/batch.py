@@ -222,13 +222,15 @@ class BatchSweep:
         from .solver import host_gaps, zero_host_gaps
         if getattr(self, "_gaps", None) is None:
             self._gaps = host_gaps(self.units, self.v_rows, self.frames, self.lam_rows)
-        zero_host_gaps(h_v, h_lam, self._gaps)
         for pg, h in zip(self.per_group, h_tables):
             pg["d_prof"].copy_(h, non_blocking=True)
         self.generate_input()
         self.solve_bm(h_v=h_v)
         self.ihc_lambda(h_lam=h_lam)
         self.jnd_sums()
+        # no kernel writes these rows, so the host zeroes them while the
+        # kernels run
+        zero_host_gaps(h_v, h_lam, self._gaps)
 
     def step(self, stream=None):
         self.generate_input(stream)

@@ -248,7 +248,6 @@ class ProfileRun:
         if getattr(self, "_whole", None) is None:
             self._whole = self.ihc.upload_chunks([self.frames], self.rows, self.lam_rows)[0]
             self._gaps = host_gaps(self.units, self.rows, self.frames, self.lam_rows)
-        zero_host_gaps(h_v, h_lam, self._gaps)
         self.d_prof.copy_(h_tables[0], non_blocking=True)
         self.generate_input()
         self.solve_bm(h_v=h_v)
@@ -256,6 +255,9 @@ class ProfileRun:
                               torch.cuda.current_stream(self.device), h_lam=h_lam)
         if self.calc_jnd:
             self.jnd_sums()
+        # no kernel writes these rows, so the host zeroes them while the
+        # kernels run
+        zero_host_gaps(h_v, h_lam, self._gaps)
 
     def step(self, stream=None):
         """One pass of the path over the whole sweep (device buffers only)."""
