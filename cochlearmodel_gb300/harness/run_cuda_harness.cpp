@@ -8,10 +8,15 @@
 // and the final JND in dB.  Parameters come from a key = value file in the
 // grammar of the reference's .par files (src/ConfigFileHandler.cpp:31-59).
 //
-// Output (little-endian): int64 header {rows, lam_rows, n_intervals, n_ac},
-// float velocity[rows][256], float lambda[3][lam_rows][256],
-// float F_RA[3][n], float FisherAI[3][n], double jnd_rate_db[n],
-// double jnd_ai_db[n].
+// Outputs:
+// - Output_File (this harness's container, little-endian): int64 header
+//   {rows, lam_rows, n_intervals, n_ac}, float velocity[rows][256], float
+//   lambda[3][lam_rows][256], float F_RA[3][n], float FisherAI[3][n], double
+//   jnd_rate_db[n], double jnd_ai_db[n].
+// - Output_Result and JND_File_Name (the reference's own keys): the raw
+//   float32 files Run_Cuda writes through OutputBuffer<float>, in its
+//   write_vector order, selected by Allowed_Outputs / Discard_* and
+//   Calculate_JND_Types as the reference selects them.
 //
 // usage: run_cuda_harness <params.par>
 
@@ -23,6 +28,7 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <memory>
 #include <regex>
 #include <sstream>
 #include <stdexcept>
@@ -62,6 +68,7 @@ std::vector<double> numbers(const std::string& v) {
 
 struct Par {
   std::map<std::string, std::string> m;
+  bool has(const std::string& k) const { return m.count(k) > 0; }
   double num(const std::string& k, double def) const {
     auto it = m.find(k);
     return it == m.end() ? def : std::stod(it->second);
@@ -97,6 +104,35 @@ std::vector<float> read_f32(const std::string& path) {
 }
 
 double spl2pa(double db, double ref) { return db == 1111.0 ? 0.0 : 10.0 * std::pow(10.0, db / 20.0) * ref; }
+
+// The reference's binary output target: OutputBuffer<float> opened for
+// writing (include/OutputBuffer.h:47-110) behind ConfigFileHandler::write_vector
+// (src/ConfigFileHandler.cpp:124-131).  It holds raw float32 values with no
+// header, appended in the order of the write_vector calls; values of other
+// types are cast to float first (castVector).
+class RawTarget {
+ public:
+  explicit RawTarget(const std::string& path) : f_(path, std::ios::binary | std::ios::trunc) {
+    if (!f_) throw std::runtime_error("cannot open Target file " + path);
+  }
+  template <class T>
+  void append(const T* src, size_t length) {
+    std::vector<float> buf(length);
+    for (size_t i = 0; i < length; ++i) buf[i] = (float)src[i];
+    f_.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)(length * 4));
+  }
+
+ private:
+  std::ofstream f_;
+};
+
+// transposeVector(v, column_size) (include/cvector.cpp:520-530)
+std::vector<float> transpose(const std::vector<float>& v, size_t column_size) {
+  std::vector<float> out(v.size());
+  const size_t row_size = v.size() / column_size;
+  for (size_t i = 0; i < v.size(); ++i) out[(i % row_size) * column_size + i / row_size] = v[i];
+  return out;
+}
 
 }  // namespace
 
@@ -268,11 +304,11 @@ int main(int argc, char** argv) {
     // JND (AudioGramCreator::calcJND / calcJNDFinal)
     std::vector<float> FRA(3 * n_int, 0.0f), FAI(3 * n_int, 0.0f);
     std::vector<double> jr(n_int, NAN), ja(n_int, NAN);
+    std::vector<int> serial(n_int), calc_pos, to_ref;
     if (calc_jnd) {
       const int head = (int)std::round((float)Fs * (float)P.num("JND_Interval_Head", 0.014));
       const int tail = (int)std::round((float)Fs * (float)P.num("JND_Interval_Tail", 0.002));
       const int len = L - head - tail;
-      std::vector<int> serial(n_int), calc_pos, to_ref;
       int ci = 0;
       for (int i = 0; i < n_int; ++i) {
         const int rr = i * (int)ref_pos.size() / n_int;
@@ -308,6 +344,77 @@ int main(int argc, char** argv) {
         };
         jr[i] = db(ra);
         ja[i] = db(ai);
+      }
+    }
+
+    // The reference's own output files, written when the .par names them.
+    // One Run_Cuda pass in profile mode (src/solver.cpp:704-830,
+    // AudioGramCreator::saveLambdas src/AudioGramCreator.cpp:202-212): the
+    // transient is shown (Decouple_Filter > 0 requires it) and its tail removed
+    // (Remove_Transient_Tail = 1 for generated profiles), so every stream
+    // starts at node 0 and holds writeTime - overlap = N * Time_Blocks nodes.
+    // write_vector calls whose name has no registered target go to the
+    // Output_Result file (VirtualHandler::write_vector, include/VirtualHandler.h:
+    // 156-173); jnd_ai and jnd_rms are registered to the raw JND file
+    // (src/params.cpp:1636-1646).
+    const std::string out_result = P.str("Output_Result", "");
+    const std::string jnd_file = P.str("JND_File_Name", "");
+    if (!out_result.empty() || (calc_jnd && !jnd_file.empty())) {
+      // Allowed_Outputs (src/params.cpp:820-832): bit 0 velocity, bits 1-3 the
+      // lambdas; the Discard_* keys set them unless Allowed_Outputs is given
+      unsigned allowed = 0;
+      if (P.has("Discard_BM_Velocity_Output") && P.num("Discard_BM_Velocity_Output", 0) != 1)
+        allowed |= 1u;
+      if (P.has("Discard_Lambdas_Output") && P.num("Discard_Lambdas_Output", 0) != 1)
+        allowed |= 14u;
+      if (P.has("Allowed_Outputs")) allowed = (unsigned)P.num("Allowed_Outputs", 0);
+      const unsigned jnd_types = P.has("Calculate_JND_Types")
+                                     ? (unsigned)P.num("Calculate_JND_Types", 0)
+                                     : (1u << 16) - 1;
+      const bool jnd_rms = (jnd_types & 1u) != 0, jnd_ai = (jnd_types & 2u) != 0;
+      const size_t nodes = (size_t)N * TB;  // writeTime - overlap
+      std::vector<int> failed_nodes((size_t)total_nodes), failed_blocks(TB);
+      GeneralKernel_Copy_Results_Template<int>(failed_nodes.data(), getCudaFailedTimeNodes(),
+                                               (size_t)total_nodes);
+      GeneralKernel_Copy_Results_Template<int>(failed_blocks.data(), getCudaFailedBlocks(),
+                                               (size_t)TB);
+      std::unique_ptr<RawTarget> main_out;
+      if (!out_result.empty()) main_out.reset(new RawTarget(out_result));
+      if (main_out) {
+        main_out->append(failed_nodes.data(), nodes);
+        main_out->append(failed_blocks.data(), (size_t)TB);
+        if (allowed & 1u) main_out->append(v.data(), nodes * 256);
+        for (int j = 0; j < LAMBDA_COUNT; ++j)
+          if (allowed & (2u << j))
+            main_out->append(lam.data() + (size_t)j * calc_time * 256, nodes * 256);
+      }
+      if (calc_jnd) {
+        // calcJNDFinal (src/AudioGramCreator.cpp:454-508): per tested
+        // interval, its blocks' failed samples and the bounded JND in dB
+        const size_t n_calc = calc_pos.size();
+        std::vector<float> failed_signals(n_calc, 0.0f), ai(n_calc), rate(n_calc);
+        for (size_t k = 0; k < n_calc; ++k) {
+          const int i = calc_pos[k];
+          for (int b = 0; b < D; ++b) failed_signals[k] += (float)failed_blocks[(size_t)i * D + b];
+          ai[k] = (float)ja[i];
+          rate[k] = (float)jr[i];
+        }
+        // column layout of the raw JND vectors (src/solver.cpp:763-767), for
+        // generated tones (JND_Signal_Source 0)
+        const size_t n_pow = powers.size(), n_freq = freqs.size();
+        const size_t rms_m = n_calc / (n_pow * n_freq);
+        const size_t mcols = rms_m * n_pow;
+        std::unique_ptr<RawTarget> raw;
+        if (!jnd_file.empty()) raw.reset(new RawTarget(jnd_file));
+        if (main_out) main_out->append(failed_signals.data(), n_calc);
+        if (jnd_ai) {
+          if (main_out) main_out->append(ai.data(), n_calc);  // jnd_ai_power
+          if (raw) raw->append(transpose(ai, mcols).data(), n_calc);
+        }
+        if (jnd_rms) {
+          if (main_out) main_out->append(rate.data(), n_calc);  // jnd_rms_power
+          if (raw) raw->append(transpose(rate, mcols).data(), n_calc);
+        }
       }
     }
 

@@ -6,7 +6,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from cochlearmodel_gb300 import build, ihc, model
+from cochlearmodel_gb300 import build, ihc, model, native
 from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun, ProfileSweep
 
 pytestmark = pytest.mark.gpu
@@ -122,3 +122,74 @@ def test_harness_iir_ac_filter(tmp_path, mv):
     lam2, _, _ = stage.run_iir(np.ascontiguousarray(v[:rows]), fr, n_lam, b, a)
     assert np.array_equal(lam[:, :n_lam].view(np.uint32), lam2.view(np.uint32))
     assert np.isfinite(jr[np.isfinite(jr)]).all()
+
+
+def _transpose(v, column_size):
+    """transposeVector(v, column_size) of the reference (include/cvector.cpp:520-530)."""
+    out = np.empty_like(v)
+    row = len(v) // column_size
+    for i in range(len(v)):
+        out[(i % row) * column_size + i // row] = v[i]
+    return out
+
+
+def test_harness_writes_the_reference_output_files(tmp_path, mv):
+    """With the reference's own keys (Output_Result, JND_File_Name,
+    Allowed_Outputs) the harness writes the files Run_Cuda writes: raw
+    float32 in write_vector order.  The Output_Result file holds the failed
+    nodes, the failed blocks, velocity, the three lambda planes (the transient
+    tail removed), then the failed signals and the AI and rate JNDs of the
+    tested intervals; the JND file holds the two JND vectors transposed to
+    frequency-major order."""
+    import torch
+    noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
+    ac = ihc.design_ac_lowpass()
+    (tmp_path / "ac.f32").write_bytes(ac.tobytes())
+    (tmp_path / "noise.f32").write_bytes(noise.tobytes())
+    out, res_bin, jnd_bin = tmp_path / "out.bin", tmp_path / "result.bin", tmp_path / "jnd.bin"
+    par = tmp_path / "run.par"
+    par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32", out=out) +
+                   f'Output_Result = "{res_bin}"\nJND_File_Name = "{jnd_bin}"\n'
+                   "Allowed_Outputs = 15\n")
+    build.build()
+    res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stderr
+    v, lam, fra, fai, jr, ja = read_out(out)
+
+    cfg = model.RunConfig(Time_Block_Length=0.002, Decouple_Filter=2, Overlap_Time=0.001,
+                          OHC_Vector=np.array([0.5, 0.3, 0.1], np.float32),
+                          IHC_Vector=np.array([8.0, 6.0], np.float32))
+    sweep = ProfileSweep(frequencies=[1000.0, 3000.0], powers=[40.0, 80.0],
+                         noises=[1111.0, 30.0], calculate_jnd=True)
+    run = ProfileRun("cuda:0", cfg, sweep, noise=noise, mv=mv, ac_taps=ac,
+                     jnd=JNDWindow(head=0.001, tail=0.0005))
+    run.step()
+    torch.cuda.synchronize()
+    nodes = run.N * cfg.Time_Blocks
+    tested = run.ref_of != np.arange(run.n_int)
+    n_calc = int(tested.sum())
+    failed = run.d_failed.cpu().numpy()
+    st = run.d_stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
+
+    raw = np.fromfile(res_bin, np.float32)
+    sizes = [nodes, cfg.Time_Blocks, nodes * 256, nodes * 256, nodes * 256, nodes * 256,
+             n_calc, n_calc, n_calc]
+    assert raw.size == sum(sizes)
+    parts = np.split(raw, np.cumsum(sizes)[:-1])
+    assert np.array_equal(parts[0], failed[:nodes].astype(np.float32))
+    assert np.array_equal(parts[1], st["failed_samples"].astype(np.float32))
+    assert np.array_equal(parts[2].reshape(nodes, 256).view(np.uint32),
+                          run.d_v.cpu().numpy()[:nodes].view(np.uint32))
+    for j in range(3):
+        assert np.array_equal(parts[3 + j].reshape(nodes, 256).view(np.uint32),
+                              lam[j, :nodes].view(np.uint32))
+    assert np.array_equal(parts[6], run.failed_per_interval().astype(np.float32))
+    ai, rate = ja[tested].astype(np.float32), jr[tested].astype(np.float32)
+    assert np.array_equal(parts[7], ai) and np.array_equal(parts[8], rate)
+    rate_db, ai_db, _, _ = run.jnd_db()
+    assert np.abs(parts[7] - ai_db[tested]).max() < 1e-3
+
+    cols = n_calc // (2 * 2) * 2  # tested intervals / (powers x frequencies) x powers
+    jnd = np.fromfile(jnd_bin, np.float32)
+    assert np.array_equal(jnd, np.concatenate([_transpose(ai, cols), _transpose(rate, cols)]))
