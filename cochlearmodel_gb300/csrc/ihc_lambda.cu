@@ -232,6 +232,7 @@ __device__ __forceinline__ void two_sum_add(float& s, float& c, float x) {
 }
 
 constexpr int kDcAnchor = 32;  // DC window re-summed at frame rows k % 32 == 0
+constexpr int kEmitRows = 4;   // rows per warp in one IHC / lambda batch
 
 __device__ __forceinline__ float fir_row(const float* __restrict__ src,
                                          const float* __restrict__ b, int tu) {
@@ -394,25 +395,15 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
     if (threadIdx.x == 0 && t + 1 < t1)
       stage_rows(&vmap, X, mbar, boxes_next, (int)f.v_row0 + (t + 1) * A.TR - A.n_ac, s0);
 
-    // phase 2: DC, IHC and lambda on rows [row0, row0 + TRt)
-    auto emit = [&](int k, float dc) {
-      const float ac = ACb[(size_t)(k - row0) * kSecTile + lane];
-      const float pre = __fmaf_rn(ac, A.eta_ac, __fmul_rn(dc, A.eta_dc));
-      const float y = __fmul_rn(dmg, pre);
-      const float lg = own_log10f(__fadd_rn(fmaxf(y, 0.0f), 1e-20f));
-      const int64_t row = f.lam_row0 + k;
-      if (A.ihc) A.ihc[row * 256 + s] = lg;
-      const float l0 = sec0 ? A.spont0 : fminf(A.sat, fmaxf(__fmul_rn(a0, lg), A.spont0));
-      const float l1 = sec0 ? A.spont1 : fminf(A.sat, fmaxf(__fmul_rn(a1, lg), A.spont1));
-      const float l2 = sec0 ? A.spont2 : fminf(A.sat, fmaxf(__fmul_rn(a2, lg), A.spont2));
-      A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
-      A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
-      A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
-      if (A.lam_host) {
-        A.lam_host[(0 * A.lam_plane_rows + row) * 256 + s] = l0;
-        A.lam_host[(1 * A.lam_plane_rows + row) * 256 + s] = l1;
-        A.lam_host[(2 * A.lam_plane_rows + row) * 256 + s] = l2;
-      }
+    // phase 2: DC, IHC and lambda on rows [row0, row0 + TRt).  Pass 1
+    // computes each row's pre-synaptic value eta_AC * AC + eta_DC * DC and
+    // leaves it in the row's ACb slot.  Pass 2 turns pre-synaptic values into
+    // IHC and lambda, kEmitRows rows per warp at a time: their arithmetic is
+    // branch-free and independent, so the rows' dependent chains (log10)
+    // interleave; the stores follow, behind the uniform output branches.
+    auto set_pre = [&](int k, float dc) {
+      float& slot = ACb[(size_t)(k - row0) * kSecTile + lane];
+      slot = __fmaf_rn(slot, A.eta_ac, __fmul_rn(dc, A.eta_dc));
     };
     if (A.dc_uniform) {
       // tiles start on multiples of 32 rows, so every 32-row block opens on
@@ -437,7 +428,7 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
           // d * (ws + wc), rounded once
           const float p = __fmul_rn(d, ws);
           const float q = __fmaf_rn(d, ws, -p);
-          emit(k, __fadd_rn(p, __fmaf_rn(d, wc, q)));
+          set_pre(k, __fadd_rn(p, __fmaf_rn(d, wc, q)));
         }
       }
     } else {
@@ -459,7 +450,37 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
         }
 #pragma unroll
         for (int r = 0; r < kRB; ++r)
-          if (r < nr) emit(kb + r, acc[r]);
+          if (r < nr) set_pre(kb + r, acc[r]);
+      }
+    }
+    __syncthreads();
+    for (int kb = row0 + warp * kEmitRows; kb < k_hi; kb += kIhcWarps * kEmitRows) {
+      float lg[kEmitRows], l0[kEmitRows], l1[kEmitRows], l2[kEmitRows];
+#pragma unroll
+      for (int r = 0; r < kEmitRows; ++r) {
+        // rows past the tile repeat its last row; they are not stored
+        const int k = min(kb + r, k_hi - 1);
+        const float pre = ACb[(size_t)(k - row0) * kSecTile + lane];
+        const float y = __fmul_rn(dmg, pre);
+        lg[r] = own_log10f(__fadd_rn(fmaxf(y, 0.0f), 1e-20f));
+        l0[r] = sec0 ? A.spont0 : fminf(A.sat, fmaxf(__fmul_rn(a0, lg[r]), A.spont0));
+        l1[r] = sec0 ? A.spont1 : fminf(A.sat, fmaxf(__fmul_rn(a1, lg[r]), A.spont1));
+        l2[r] = sec0 ? A.spont2 : fminf(A.sat, fmaxf(__fmul_rn(a2, lg[r]), A.spont2));
+      }
+#pragma unroll
+      for (int r = 0; r < kEmitRows; ++r) {
+        if (kb + r < k_hi) {
+          const int64_t row = f.lam_row0 + kb + r;
+          A.lam[(0 * A.lam_plane_rows + row) * 256 + s] = l0[r];
+          A.lam[(1 * A.lam_plane_rows + row) * 256 + s] = l1[r];
+          A.lam[(2 * A.lam_plane_rows + row) * 256 + s] = l2[r];
+          if (A.ihc) A.ihc[row * 256 + s] = lg[r];
+          if (A.lam_host) {
+            A.lam_host[(0 * A.lam_plane_rows + row) * 256 + s] = l0[r];
+            A.lam_host[(1 * A.lam_plane_rows + row) * 256 + s] = l1[r];
+            A.lam_host[(2 * A.lam_plane_rows + row) * 256 + s] = l2[r];
+          }
+        }
       }
     }
     __syncthreads();
