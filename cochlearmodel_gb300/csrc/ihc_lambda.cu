@@ -414,17 +414,31 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
         const int ke = min(kb + kDcAnchor, k_hi);
         float ws = 0.0f, wc = 0.0f;
         int tu_prev = -1;
+        // taps_used(k) stepped from row to row: lim = (k + 1) mod sg(k)
+        int sg = kb < f.frdp - 1 ? f.seg : f.total;
+        int lim = (kb + 1) % sg;
+#pragma unroll 4
         for (int k = kb; k < ke; ++k) {
-          const int tu = taps_used(k, f, A.n_dc);
+          const int tu = lim < A.n_dc ? lim : A.n_dc;
+          // both window ends lie inside DS for every tu <= n_dc, so they are
+          // loaded ahead of the dependent sums
+          const float x_new = col[(size_t)(k - dsbase) * kSecTile];
+          const float x_old = col[(size_t)(k - tu - dsbase) * kSecTile];
           if (k == kb || (tu != tu_prev && tu != tu_prev + 1)) {
             ws = wc = 0.0f;
             for (int j = 0; j < tu; ++j)
               two_sum_add(ws, wc, col[(size_t)(k - j - dsbase) * kSecTile]);
           } else {
-            two_sum_add(ws, wc, col[(size_t)(k - dsbase) * kSecTile]);
-            if (tu == tu_prev) two_sum_add(ws, wc, -col[(size_t)(k - tu - dsbase) * kSecTile]);
+            two_sum_add(ws, wc, x_new);
+            if (tu == tu_prev) two_sum_add(ws, wc, -x_old);
           }
           tu_prev = tu;
+          if (k + 1 == f.frdp - 1) {
+            sg = f.total;
+            lim = (k + 2) % sg;
+          } else if (++lim == sg) {
+            lim = 0;
+          }
           // d * (ws + wc), rounded once
           const float p = __fmul_rn(d, ws);
           const float q = __fmaf_rn(d, ws, -p);
