@@ -16,12 +16,13 @@
 //   lambda_j = s ? min(SAT, max(A_js IHC, spont_j)) : spont_j,  j = 0..2
 // in FP32, each FIR accumulated with a compensated dot product (Dot2).
 //
-// GB300 layout: one CTA = 32 sections x TR output rows.  The velocity window
-// it needs (TR rows plus both filters' look-back) is staged into shared
-// memory by TMA (cp.async.bulk.tensor.2d, 128-row boxes, completion on an
-// mbarrier with a bounded wait); AC / dS / DC are computed from shared
-// memory with 8-row register blocking (one LDS feeds 8 rows), and the three
-// lambda planes are written with coalesced 128-byte rows.
+// GB300 layout: one CTA = 32 sections x a run of consecutive TR-row tiles.
+// Each tile's velocity window (TR rows plus the look-back) is staged into
+// shared memory by TMA (cp.async.bulk.tensor.2d, 64-row boxes, completion on
+// an mbarrier with a bounded wait), the next tile's while the current one
+// finishes; AC and dS are computed from shared memory with 8-row register
+// blocking, then DC, IHC and lambda, and the three lambda planes are written
+// with coalesced 128-byte rows.
 
 #include <cuda.h>
 #include <cuda_runtime.h>
