@@ -61,3 +61,19 @@ def test_zero_host_gaps_touches_only_the_gaps():
     zero_host_gaps(h_v, h_lam, ([(0, 2), (8, 10)], [(5, 6)]))
     assert (h_v[:2] == 0).all() and (h_v[8:] == 0).all() and (h_v[2:8] == 7).all()
     assert (h_lam[:, 5] == 0).all() and (h_lam[:, :5] == 7).all()
+
+
+def test_host_mirror_check_rejects_mismatched_buffers():
+    """The kernels store straight into a host mirror, so the Python layer
+    accepts only a pinned, contiguous tensor of the device buffer's exact
+    shape and dtype; everything else raises before any launch."""
+    import pytest
+    like = torch.zeros((8, 256), dtype=torch.float32)
+    bad = [None,
+           torch.zeros((7, 256), dtype=torch.float32),            # short
+           torch.zeros((8, 256), dtype=torch.float64),            # dtype
+           torch.zeros((256, 8), dtype=torch.float32).t(),        # not contiguous
+           torch.zeros((8, 256), dtype=torch.float32)]            # pageable
+    for t in bad:
+        with pytest.raises(ValueError):
+            native.check_host_mirror(t, like, "h_v")
