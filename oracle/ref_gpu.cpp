@@ -1,0 +1,289 @@
+// Test infrastructure: a launcher for the REFERENCE's own CUDA kernels.
+//
+// oracle/build_ref_gpu.sh compiles the reference's device code
+// (src/cochlea.cu with include/cochlea.cuh, unmodified) into
+// oracle/_ref/cochlea_ref.cubin for sm_103a.  This file is our own host side:
+// it loads that cubin through the CUDA driver API, fills the reference's
+// __constant__ symbols and launch arguments the way the reference's host
+// functions do (each step cites the lines it restates), launches the
+// reference's kernels and copies their results back.  It is the parity judge
+// for the product's reference-arithmetic BM mode and reports the reference's
+// FP32 results for the error tables; nothing in the product links or loads it.
+//
+// Everything is synchronous and uses the device's primary context (the one the
+// CUDA runtime, and therefore torch, uses).
+
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+std::string g_err;
+CUmodule g_mod = nullptr;
+CUcontext g_ctx = nullptr;
+
+int fail(const std::string& m) {
+  g_err = m;
+  return 1;
+}
+
+#define RG_TRY(call, what)                                                      \
+  do {                                                                          \
+    CUresult rc_ = (call);                                                      \
+    if (rc_ != CUDA_SUCCESS) {                                                  \
+      const char* s_ = nullptr;                                                 \
+      cuGetErrorString(rc_, &s_);                                               \
+      return fail(std::string(what) + ": " + (s_ ? s_ : "CUDA driver error"));  \
+    }                                                                           \
+  } while (0)
+
+// Finds a kernel of the module by the start of its mangled name.
+CUfunction find_fn(const std::string& prefix) {
+  unsigned n = 0;
+  if (cuModuleGetFunctionCount(&n, g_mod) != CUDA_SUCCESS) return nullptr;
+  std::vector<CUfunction> fns(n);
+  if (cuModuleEnumerateFunctions(fns.data(), n, g_mod) != CUDA_SUCCESS) return nullptr;
+  for (CUfunction f : fns) {
+    const char* name = nullptr;
+    if (cuFuncGetName(&name, f) == CUDA_SUCCESS && name &&
+        std::strncmp(name, prefix.c_str(), prefix.size()) == 0)
+      return f;
+  }
+  return nullptr;
+}
+
+std::string mangled(const char* name) {
+  return "_Z" + std::to_string(std::strlen(name)) + name;
+}
+
+// A zero-filled device buffer freed on scope exit.
+struct DBuf {
+  CUdeviceptr p = 0;
+  size_t bytes = 0;
+  ~DBuf() {
+    if (p) cuMemFree(p);
+  }
+  int alloc(size_t n) {
+    bytes = n ? n : 16;
+    if (cuMemAlloc(&p, bytes) != CUDA_SUCCESS) return fail("cuMemAlloc");
+    if (cuMemsetD8(p, 0, bytes) != CUDA_SUCCESS) return fail("cuMemsetD8");
+    return 0;
+  }
+  int up(const void* h, size_t n) {
+    if (n > bytes) return fail("upload larger than buffer");
+    return cuMemcpyHtoD(p, h, n) == CUDA_SUCCESS ? 0 : fail("cuMemcpyHtoD");
+  }
+  int down(void* h, size_t n) const {
+    if (n > bytes) return fail("download larger than buffer");
+    return cuMemcpyDtoH(h, p, n) == CUDA_SUCCESS ? 0 : fail("cuMemcpyDtoH");
+  }
+};
+
+int set_symbol(const char* name, const void* h, size_t n) {
+  CUdeviceptr d = 0;
+  size_t bytes = 0;
+  RG_TRY(cuModuleGetGlobal(&d, &bytes, g_mod, name), std::string("symbol ") + name);
+  if (n > bytes) return fail(std::string("symbol ") + name + " is smaller than its data");
+  RG_TRY(cuMemcpyHtoD(d, h, n), std::string("upload ") + name);
+  return 0;
+}
+
+constexpr int kSections = 256;
+constexpr int kMaxBlocks = 65536;  // MAX_NUMBER_OF_BLOCKS, include/const.h:363
+
+}  // namespace
+
+extern "C" {
+
+// The BMOHCNewKernel arguments that reach the kernels (src/cochlea.cu:990-1042),
+// as CSolver::Run_Cuda passes them (src/solver.cpp:629-659).
+typedef struct {
+  float w_ohc, time_step, time_step_out, delta_x, alpha_r;
+  int enable_psi, enable_OW;
+  float Ts, alpha_l, alpha_s, Gme, a0, a1, a2, sigma_ow, eta_1, eta_2;
+  int Time_Blocks, samplesBufferLengthP1, overlap_nodes_for_block;
+  long long overlapTimeMicroSec;
+  int show_transient;
+  float cuda_max_time_step, cuda_min_time_step;
+  int Decouple_Filter;
+  float Max_M1_SP_Error_Parameter, Max_Tolerance_Parameter;
+  int Relative_Error_Parameters;
+  float M1_SP_Fix_Factor, Tolerance_Fix_Factor, SPLREfVal;
+  int JACOBBY_Loops_Fast, JACOBBY_Loops_Slow, Cuda_Outern_Loops;
+} refgpu_bm_params;
+
+const char* refgpu_last_error(void) { return g_err.c_str(); }
+
+// Loads the reference cubin into the primary context of device 0.
+int refgpu_load(const char* cubin_path) {
+  if (g_mod) return 0;
+  RG_TRY(cuInit(0), "cuInit");
+  CUdevice dev;
+  RG_TRY(cuDeviceGet(&dev, 0), "cuDeviceGet");
+  RG_TRY(cuDevicePrimaryCtxRetain(&g_ctx, dev), "cuDevicePrimaryCtxRetain");
+  RG_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+  RG_TRY(cuModuleLoad(&g_mod, cubin_path), std::string("cuModuleLoad ") + cubin_path);
+  return 0;
+}
+
+// Runs the reference's BM kernel `variant` over one Run_Cuda parameter set:
+//   variant 0  : BMOHC_NEW_kernel (Run_Fast_BM_Calculation = 0, the default;
+//                include/cochlea.cuh:3486-4324, dispatched at src/cochlea.cu:2298-2330)
+//   variant 17 : BMOHC_FAST_Pre_fmaf_No_Constants_kernel_4B_Optimized_triple_aggregations
+//                (include/cochlea.cuh:13573-14245, dispatched at src/cochlea.cu:1436-1493)
+// sections: gamma, mass, rsM (= 1/m), U, L, R, S, Q, S_ohc, S_tm, R_tm, each
+// float[256] as Run_Cuda casts them (src/solver.cpp:357-376).  mtt / mmspt:
+// the per-block throw and m1-sp tolerances (setupToleranceProfile,
+// src/cochlea.cu:4256-4287), Time_Blocks entries each.  input: the sample
+// buffer (input_len >= samplesBufferLengthP1).  Outputs: saved_speeds
+// float[out_rows][256], failed_nodes int[out_rows] and failed_blocks
+// int[Time_Blocks] (the last two may be null).
+int refgpu_bm_run(int variant, const refgpu_bm_params* p, const float* const* sections,
+                  const float* mtt, const float* mmspt, const float* input, long long input_len,
+                  float* saved_speeds, long long out_rows, int* failed_nodes,
+                  int* failed_blocks) {
+  if (!g_mod) return fail("refgpu_bm_run: refgpu_load first");
+  if (!p || !sections || !mtt || !mmspt || !input || !saved_speeds)
+    return fail("refgpu_bm_run: null argument");
+  const int TB = p->Time_Blocks;
+  if (TB < 1 || TB > kMaxBlocks) return fail("refgpu_bm_run: Time_Blocks out of range");
+  if (input_len < p->samplesBufferLengthP1 || out_rows < p->samplesBufferLengthP1)
+    return fail("refgpu_bm_run: buffers shorter than samplesBufferLengthP1");
+  CUfunction fn = nullptr;
+  if (variant == 0)
+    fn = find_fn(mangled("BMOHC_NEW_kernel"));
+  else if (variant == 17)
+    fn = find_fn(mangled("BMOHC_FAST_Pre_fmaf_No_Constants_kernel_4B_Optimized_triple_aggregations"));
+  else
+    return fail("refgpu_bm_run: variant must be 0 or 17");
+  if (!fn) return fail("refgpu_bm_run: kernel not found in the cubin");
+  RG_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+
+  // Constant packing, src/cochlea.cu:1098-1147.
+  float c[64] = {};
+  int ci[16] = {};
+  long long cl[8] = {};
+  c[0] = p->Ts;
+  c[1] = static_cast<float>(1.0 / static_cast<double>(p->Ts));
+  c[2] = p->alpha_l;
+  c[3] = p->alpha_s;
+  c[4] = -1.0f * p->alpha_l;
+  c[5] = -1.0f * p->alpha_s;
+  c[6] = static_cast<float>(static_cast<double>(p->alpha_l) / static_cast<double>(p->alpha_s));
+  c[7] = static_cast<float>(1.0 / static_cast<double>(p->sigma_ow));
+  c[8] = p->delta_x;
+  c[9] = p->delta_x * p->delta_x;
+  c[10] = p->a0;
+  c[11] = p->a1;
+  c[12] = p->a2;
+  c[13] = p->eta_1;
+  c[14] = p->eta_2;
+  c[15] = p->Gme;
+  c[16] = p->enable_OW * p->Gme;
+  c[17] = (1 - p->enable_OW) * p->Gme;
+  c[18] = -p->w_ohc;
+  c[19] = p->time_step;
+  c[20] = p->time_step_out;
+  c[21] = p->cuda_min_time_step;
+  c[22] = p->cuda_max_time_step;
+  c[23] = p->Max_M1_SP_Error_Parameter;
+  c[24] = p->Max_Tolerance_Parameter;
+  c[25] = p->alpha_r;
+  c[26] = c[8] * c[10];
+  c[31] = -p->a1;
+  c[32] = -p->a2;
+  c[33] = p->SPLREfVal;
+  c[34] = 1.0f / p->SPLREfVal;
+  c[35] = p->M1_SP_Fix_Factor;
+  c[36] = p->Tolerance_Fix_Factor;
+  ci[0] = p->Decouple_Filter;
+  ci[1] = p->enable_OW;
+  ci[2] = p->enable_psi;
+  ci[3] = TB;
+  ci[4] = p->samplesBufferLengthP1;
+  ci[5] = p->overlap_nodes_for_block;
+  ci[6] = p->show_transient;
+  ci[7] = p->Relative_Error_Parameters;
+  ci[8] = (p->samplesBufferLengthP1 - p->overlap_nodes_for_block) / (TB + 1);
+  ci[9] = p->JACOBBY_Loops_Fast;
+  ci[10] = p->JACOBBY_Loops_Slow;
+  ci[11] = p->Cuda_Outern_Loops;
+  cl[0] = p->overlapTimeMicroSec;
+
+  // Block partition, src/cochlea.cu:1152-1176.
+  std::vector<int> out_idx(kMaxBlocks, 0), end_idx(kMaxBlocks, 0);
+  const int D = ci[0], N = ci[8], ov = ci[5];
+  for (int b = 0; b < TB; ++b) {
+    const int transient_offset = (b > 0 && (D == 0 || (D != 1 && b % D != 0)));
+    const int preDecoupled = D > 0 && (D == 1 || ((b + 1) % D == 0)) && b != TB - 1;
+    const int postDecoupled = D > 0 && (b % D == 0);
+    const int input_sample = b * N;
+    out_idx[b] = input_sample + std::max(1 - transient_offset - postDecoupled, 0) * ov;
+    const int block_length = N + (1 - preDecoupled) * ov;
+    end_idx[b] = input_sample + block_length;
+    if (b > 0) out_idx[b] = std::max(out_idx[b], end_idx[b - 1]);
+  }
+  if (set_symbol("model_constants", c, sizeof(c))) return 1;
+  if (set_symbol("model_constants_integers", ci, sizeof(ci))) return 1;
+  if (set_symbol("model_constants_longs", cl, sizeof(cl))) return 1;
+
+  // Buffers.  The kernels read input_samples[input_sample + 2] at most up to
+  // the block end and write saved_speeds / failure rows below it; both are
+  // padded.
+  const long long rows = out_rows + 4;
+  DBuf d_in, d_out, d_fn, d_fb, d_sec[11], d_mtt, d_mmspt, d_oi, d_ei, d_conv[6];
+  if (d_in.alloc((size_t)(input_len + 16) * 4) || d_in.up(input, (size_t)input_len * 4)) return 1;
+  if (d_out.alloc((size_t)rows * kSections * 4) || d_fn.alloc((size_t)rows * 4) ||
+      d_fb.alloc((size_t)kMaxBlocks * 4))
+    return 1;
+  for (int i = 0; i < 11; ++i) {
+    if (!sections[i]) return fail("refgpu_bm_run: null section vector");
+    if (d_sec[i].alloc(kSections * 4) || d_sec[i].up(sections[i], kSections * 4)) return 1;
+  }
+  if (d_mtt.alloc(kMaxBlocks * 4) || d_mtt.up(mtt, (size_t)TB * 4)) return 1;
+  if (d_mmspt.alloc(kMaxBlocks * 4) || d_mmspt.up(mmspt, (size_t)TB * 4)) return 1;
+  if (d_oi.alloc(kMaxBlocks * 4) || d_oi.up(out_idx.data(), kMaxBlocks * 4)) return 1;
+  if (d_ei.alloc(kMaxBlocks * 4) || d_ei.up(end_idx.data(), kMaxBlocks * 4)) return 1;
+  // convergence statistics: per node (0, 2, 4) and per block (1, 3, 5)
+  for (int i = 0; i < 6; ++i)
+    if (d_conv[i].alloc((size_t)((i & 1) ? kMaxBlocks : rows) * 4)) return 1;
+
+  // Argument order of the dispatch, src/cochlea.cu:2303-2327 / 1442-1490;
+  // the kernels take mass, rsM, U, L, R, S, Q, gamma, S_ohc, S_tm, R_tm.
+  CUdeviceptr ptrs[25] = {d_in.p,      d_out.p,     d_fn.p,      d_fb.p,      d_sec[1].p,
+                          d_sec[2].p,  d_sec[3].p,  d_sec[4].p,  d_sec[5].p,  d_sec[6].p,
+                          d_sec[7].p,  d_sec[0].p,  d_sec[8].p,  d_sec[9].p,  d_sec[10].p,
+                          d_mtt.p,     d_mmspt.p,   d_oi.p,      d_ei.p,      d_conv[0].p,
+                          d_conv[1].p, d_conv[2].p, d_conv[3].p, d_conv[4].p, d_conv[5].p};
+  std::vector<void*> args;
+  for (auto& q : ptrs) args.push_back(&q);
+  float base_time = 0.0f;
+  float s_w = p->w_ohc, s_ts = p->time_step, s_tso = p->time_step_out, s_dx = p->delta_x,
+        s_ar = p->alpha_r, s_Ts = p->Ts, s_al = p->alpha_l, s_as = p->alpha_s, s_g = p->Gme,
+        s_a0 = p->a0, s_a1 = p->a1, s_a2 = p->a2, s_sow = p->sigma_ow, s_e1 = p->eta_1,
+        s_e2 = p->eta_2, s_dtmin = p->cuda_min_time_step, s_dtmax = p->cuda_max_time_step;
+  int s_psi = p->enable_psi, s_ow = p->enable_OW, s_len = p->samplesBufferLengthP1,
+      s_ov = p->overlap_nodes_for_block;
+  if (variant == 17) {
+    void* extra[] = {&s_w,  &s_ts, &s_tso, &s_dx, &s_ar, &s_psi, &s_ow,    &base_time,
+                     &s_Ts, &s_al, &s_as,  &s_g,  &s_a0, &s_a1,  &s_a2,    &s_sow,
+                     &s_e1, &s_e2, &s_len, &s_ov, &s_dtmin, &s_dtmax};
+    for (void* e : extra) args.push_back(e);
+  }
+  RG_TRY(cuLaunchKernel(fn, (unsigned)TB, 1, 1, kSections, 1, 1, 0, nullptr, args.data(),
+                        nullptr),
+         "cuLaunchKernel (reference BM)");
+  RG_TRY(cuCtxSynchronize(), "reference BM kernel");
+  if (d_out.down(saved_speeds, (size_t)out_rows * kSections * 4)) return 1;
+  if (failed_nodes && d_fn.down(failed_nodes, (size_t)out_rows * 4)) return 1;
+  if (failed_blocks && d_fb.down(failed_blocks, (size_t)TB * 4)) return 1;
+  return 0;
+}
+
+}  // extern "C"
