@@ -1,6 +1,7 @@
-// BM/OHC adaptive-step solver (reference kernel 17,
-// include/cochlea.cuh:13573-14245, launched by BMOHCNewKernel,
-// src/cochlea.cu:1436-1493).
+// BM/OHC adaptive-step solver: reference kernel 17
+// (include/cochlea.cuh:13573-14245) and the default BMOHC_NEW_kernel
+// (include/cochlea.cuh:3486-4324), launched by BMOHCNewKernel
+// (src/cochlea.cu:1436-1493, 2298-2330).
 //
 // GB300 layout: one WARP owns one unit (one time block of one signal); lane l
 // holds sections 8l..8l+7 of every state vector in registers, as four
@@ -9,16 +10,29 @@
 // halo -- no shared-memory round trip and no block barrier, where the
 // reference spends two __syncthreads per sweep across 256 threads.  The
 // Lipschitz/fault reductions are xor-butterflies, so every lane holds the
-// full result and takes the same step decision (the reference's warp-0
-// reduction leaves the full value only in lane 0; its other lanes race on
-// the shared decision slots -- this kernel takes the lane-0 semantics).
-// Units come from a device work queue, so a persistent grid of warps drains
-// batches of uneven-length signals.
+// full result and takes the same step decision.  Units come from a device
+// work queue, so a persistent grid of warps drains batches of uneven-length
+// signals.
 //
-// Floating-point order is fixed (compiled with --fmad=false; explicit
-// __fmaf_rn where an FMA is intended) and matches the CPU oracle, which
-// evaluates the same sequence, bit for bit.  The simulated-time accumulator
-// is double.
+// Step controller (CTL):
+//   0  kernel 17: a step needs another iteration while the SUM over sections
+//      of |v - v_ref| - max(mtt, v dt) is positive.  Kernel 17's warp-0
+//      reduction leaves the full sum only in lane 0 and its other lanes race
+//      on the shared decision slots; this kernel takes the lane-0 value.
+//   1  BMOHC_NEW_kernel: another iteration while ANY section has
+//      |v - v_ref| > max(mtt, v dt) (its fault count, cochlea.cuh:4080-4100).
+// Arithmetic (ARITH):
+//   0  own fixed order (explicit __fmaf_rn, own tanh and reciprocal, double
+//      simulated-time accumulator), reproduced bit for bit by the CPU oracle.
+//   1  BMOHC_NEW_kernel's own operation order: its fmaf placement, CUDA's
+//      tanhf, __fdividef where it divides, its shared-memory tree order for
+//      the velocity-error sum, one Jacobi sweep at a time and a float time
+//      accumulator; checked bit for bit against the reference's compiled
+//      kernel.  (CUDA's tanhf gives the same bits under --fmad=false as under
+//      the reference's default --fmad=true, checked on every float input.)
+//
+// Floating-point order is fixed: the file is compiled with --fmad=false and
+// every fused multiply-add is an explicit __fmaf_rn.
 
 #include <cuda_runtime.h>
 
@@ -49,6 +63,9 @@ struct BMArgs {
   int32_t* work;
   float ratio, nas, al, e1, e2, nw, ar, dx2, dxa0, na1, na2, gme, sow;
   float dt0, dtmin, dtmax;
+  // ARITH 1: the reference's float constants 1/Ts, 1/sigma_ow (each formed in
+  // double and rounded, src/cochlea.cu:1099,1105) and time_step_out
+  float fs_f, rsow, tout_f;
   int jfast, jslow, max_outer, max_sub;
   double tout, invts;
   // tolerance mode (jacobi_mode 2)
@@ -201,11 +218,43 @@ struct SideVec {
   }
 };
 
+// CUDA's tanhf and __fdividef on a pair (ARITH 1).
+__device__ __forceinline__ float2 tanhf2(float2 x) { return f2(tanhf(x.x), tanhf(x.y)); }
+__device__ __forceinline__ float2 fdividef2(float2 a, float2 b) {
+  return f2(__fdividef(a.x, b.x), __fdividef(a.y, b.y));
+}
+
+// Sum over the 256 sections in BMOHC_NEW_kernel's order (ARITH 1): its
+// shared-memory tree adds element i + t into element i for t = 128, 64, ...,
+// 1 (include/cochlea.cuh:4057-4066).  Section s = 8l + j sits in lane l, so
+// the strides 128..8 pair lanes l and l + 16..1 element by element (an xor
+// butterfly leaves the same value in both lanes, addition commutes), and
+// strides 4, 2, 1 finish inside the lane.  Every lane returns the sum.
+__device__ __forceinline__ float ref_tree_sum(const float2 (&t)[4]) {
+  float e[kSPL];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    e[j] = t[j].x;
+    e[7 - j] = t[j].y;
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+    for (int j = 0; j < kSPL; ++j) e[j] = __fadd_rn(e[j], __shfl_xor_sync(kFull, e[j], o));
+#pragma unroll
+  for (int j = 0; j < 4; ++j) e[j] = __fadd_rn(e[j], e[j + 4]);
+  e[0] = __fadd_rn(e[0], e[2]);
+  e[1] = __fadd_rn(e[1], e[3]);
+  return __fadd_rn(e[0], e[1]);
+}
+
 // One unit, executed by one full warp.  sp: shared [8][256] section
 // parameters; sg / sgs: shared gamma and gamma*S_ohc of the unit's profile
 // (all three in pair order, as are the previous-step slice and hist).
 // The per-section arithmetic runs on section pairs (two-wide FP32), each
-// element rounding as the scalar sequence the CPU oracle evaluates.
+// element rounding as the scalar sequence the CPU oracle (ARITH 0) or the
+// reference's BMOHC_NEW_kernel (ARITH 1) evaluates.  CTL and ARITH: see the
+// head of this file.
 //
 // TOL 0: fixed sweep counts (the reference schedule).  TOL 1: tolerance
 // mode; each solve sweeps in pairs until max|p2 - p1| <= jtol * max|p2|
@@ -215,7 +264,7 @@ struct SideVec {
 // network's correction of the extrapolation every learn_every-th step.
 // hist: two 256-float slots per warp holding the pressure at the start of
 // the last two steps; ws_scratch / wblob: inference scratch and weights.
-template <bool PREV_SMEM, int TOL>
+template <bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
                                          const float* __restrict__ sp,
                                          const float* __restrict__ sg,
@@ -272,7 +321,8 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   float* cb = A.conv ? A.conv + un.out_base * 3 : nullptr;
 
   float dt = A.dt0;
-  double tau = 0.0;
+  double tau = 0.0;   // ARITH 0: simulated time since the current sample
+  float tau_f = 0.0f; // ARITH 1: the reference's float accumulator (curr_time_f)
   int n = un.start;
   float sx0 = inb[n], sx1 = inb[n + 1];
   int fail_flag = 0;
@@ -294,7 +344,9 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       dt_prev = dt;
       store8q(hist + (n_sub & 1) * 256 + qb, p);
     }
-    const float delta = (float)(tau * A.invts);
+    // ARITH 1: sx[9] = curr_time_f * Fs, sx[10] = 1 - sx[9]
+    // (include/cochlea.cuh:3925-3927)
+    const float delta = ARITH ? __fmul_rn(tau_f, A.fs_f) : (float)(tau * A.invts);
     const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
     // (s * 0.5) * dt == s * (dt * 0.5) exactly, so each trapezoid update is
     // one fma with the half step
@@ -326,11 +378,14 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       }
       float2 dv[4], fl[4];
       const float2 mtt2 = f2b(mtt);
+      bool fault = false;  // CTL 1: some section of this lane fails the speed test
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const float2 vn = fma2(add2(a0[k], a[k]), hdt2, v0[k]);
         dv[k] = abs2(sub2(vn, v[k]));
-        fl[k] = sub2(dv[k], max2(mtt2, mul2(vn, dt2)));
+        const float2 thr = max2(mtt2, mul2(vn, dt2));
+        if (CTL == 0) fl[k] = sub2(dv[k], thr);
+        else fault = fault || dv[k].x > thr.x || dv[k].y > thr.y;
         v[k] = vn;
         x[k] = fma2(add2(v0[k], vn), hdt2, x0[k]);
         y[k] = fma2(add2(u0[k], u[k]), hdt2, y0[k]);
@@ -338,7 +393,12 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       }
       w = __fmaf_rn(__fadd_rn(wd0, wd), hdt, w0);
       wd = __fmaf_rn(__fadd_rn(wdd0, wdd), hdt, wd0);
-      const float evp = pair_sum8p(dv), fp = pair_sum8p(fl);
+      // the velocity-error sum: lane partials now (ARITH 0), or the whole
+      // sum in the reference's tree order when the tester will run (ARITH 1)
+      float evp = 0.0f, fp = 0.0f;
+      if (ARITH == 0) evp = pair_sum8p(dv);
+      else if (__all_sync(kFull, reset == 0)) evp = ref_tree_sum(dv);
+      if (CTL == 0) fp = pair_sum8p(fl);
 
       // OHC / TM coupling, G and the right-hand side Y (scaled by 1/m).
       const bool tm_update = out_loop < 2;
@@ -354,16 +414,24 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           for (int k = 0; k < 4; ++k) {
             const float2 d = sub2(y[k], x[k]);
             const float2 Pohc = mul2(gs[k], d);
-            const float2 t = own_tanhf2(mul2(f2b(A.ratio), ps[k]));
+            const float2 targ = mul2(f2b(A.ratio), ps[k]);
+            const float2 t = ARITH ? tanhf2(targ) : own_tanhf2(targ);
             const float2 dL = mul2(f2b(A.nas), t);
             const float2 Aa = mul2(f2b(A.al), fma2(t, t, f2b(-1.0f)));
-            const float2 N1 = fma2(f2b(A.e1), d, fma2(f2b(A.e2), v[k], mul2(f2b(A.nw), ps[k])));
+            // ARITH 1: -w psi, + eta_1 d, + eta_2 v (include/cochlea.cuh:3842-3844)
+            const float2 N1 =
+                ARITH ? fma2(f2b(A.e2), v[k], fma2(f2b(A.e1), d, mul2(f2b(A.nw), ps[k])))
+                      : fma2(f2b(A.e1), d, fma2(f2b(A.e2), v[k], mul2(f2b(A.nw), ps[k])));
             const float2 N = fma2(Stm[k], dL, mul2(mul2(N1, Rtm[k]), Aa));
             const float2 Pp = fma2(Stm[k], y[k], Pohc);
             const float2 num = fma2(neg2(gm[k]), N, Pp);
             const float2 den = mul2(Rtm[k], fma2(mul2(gm[k], Aa), f2b(A.e2), f2b(-1.0f)));
-            const float2 q = mul2(num, own_rcpf2(abs2(den)));
-            u[k] = f2(den.x < 0.0f ? -q.x : q.x, den.y < 0.0f ? -q.y : q.y);
+            if (ARITH) {
+              u[k] = fdividef2(num, den);
+            } else {
+              const float2 q = mul2(num, own_rcpf2(abs2(den)));
+              u[k] = f2(den.x < 0.0f ? -q.x : q.x, den.y < 0.0f ? -q.y : q.y);
+            }
             Ptm[k] = fma2(Rtm[k], u[k], mul2(Stm[k], y[k]));
           }
           Ps.put(Ptm);
@@ -380,11 +448,18 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           g = fma2(g, v[k], mul2(Ss[k], x[k]));
           G[k] = sub2(neg2(g), Ptm[k]);
           float2 Yk = mul2(mul2(f2b(A.dx2), G[k]), Qs[k]);
-          if (k == 0 && first)  // section 0
-            Yk.x = __fmul_rn(A.dxa0,
-                             __fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmul_rn(A.gme, smp))));
+          if (k == 0 && first) {  // section 0
+            if (ARITH)  // -a2 w' + -a1 w + Gme smp, then dx a0 (cochlea.cuh:3940-3943)
+              Yk.x = __fmul_rn(A.dxa0, __fmaf_rn(A.gme, smp,
+                                                 __fmaf_rn(A.na1, w, __fmul_rn(A.na2, wd))));
+            else
+              Yk.x = __fmul_rn(A.dxa0,
+                               __fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmul_rn(A.gme, smp))));
+          }
           if (k == 0 && last) Yk.y = 0.0f;  // section 255
-          Yrm[k] = mul2(Yk, rm[k]);
+          // ARITH 0 sweeps with Y/m formed once; ARITH 1 keeps Y (it sweeps
+          // (Y - t) * (1/m), cochlea.cuh:3963-3965)
+          Yrm[k] = ARITH ? Yk : mul2(Yk, rm[k]);
         }
         Gs.put(G);
       }
@@ -486,7 +561,27 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
       };
       int it = 0;
-      if (!TOL && J == 20) {
+      if (ARITH) {
+        // BMOHC_NEW_kernel's sweep, one at a time: p_s <- (Y_s - t_s) / m_s
+        // with t_s = l_s p_{s-1} + p_{s+1} (l_s = 0 on 254, 255) and
+        // p_{-1} = p_256 = 0 (include/cochlea.cuh:3958-3967)
+        for (; it < J; ++it) {
+          float2 H = f2(__shfl_up_sync(kFull, p[0].y, 1), __shfl_down_sync(kFull, p[0].x, 1));
+          if (first) H.x = 0.0f;
+          if (last) H.y = 0.0f;
+          float2 T[4];
+          T[0] = add2(H, p[1]);
+          T[1] = add2(p[2], p[0]);
+          T[2] = add2(p[1], p[3]);
+          T[3] = f2(__fadd_rn(p[2].x, p[3].y), __fadd_rn(p[2].y, p[3].x));
+          if (last) {
+            T[0].y = H.y;
+            T[1].y = p[0].y;
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) p[k] = mul2(sub2(Yrm[k], T[k]), rm[k]);
+        }
+      } else if (!TOL && J == 20) {
         // the reference schedule's slow count, fully unrolled
 #pragma unroll
         for (int r = 0; r < 10; ++r) sweep_pair();
@@ -513,7 +608,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           }
         }
       }
-      if (!TOL && it < J) {
+      if (!TOL && !ARITH && it < J) {
         float2 H = f2(__shfl_up_sync(kFull, p[0].y, 1), __shfl_down_sync(kFull, p[0].x, 1));
         if (first) H.x = 0.0f;
         if (last) H.y = 0.0f;
@@ -544,18 +639,30 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           da[k] = abs2(sub2(a[k], an));
           a[k] = an;
           const float2 d = sub2(y[k], x[k]);
-          dp[k] = fma2(f2b(A.e1), d, fma2(f2b(A.e2), sub2(u[k], v[k]), mul2(f2b(A.nw), ps[k])));
+          if (ARITH)  // eta_2 (u - v), + eta_1 d, + -w psi (cochlea.cuh:4010-4013)
+            dp[k] = fma2(f2b(A.nw), ps[k],
+                         fma2(f2b(A.e1), d, mul2(f2b(A.e2), sub2(u[k], v[k]))));
+          else
+            dp[k] = fma2(f2b(A.e1), d,
+                         fma2(f2b(A.e2), sub2(u[k], v[k]), mul2(f2b(A.nw), ps[k])));
         }
       }
-      wdd = __fdiv_rn(__fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmaf_rn(A.gme, smp, p0))), A.sow);
+      if (ARITH)  // oval window: (-a1 w + -a2 w') + (Gme smp + p_0), times 1/sigma_ow
+        wdd = __fmul_rn(A.rsow, __fadd_rn(__fmaf_rn(A.na2, wd, __fmul_rn(A.na1, w)),
+                                          __fmaf_rn(A.gme, smp, p0)));
+      else
+        wdd = __fdiv_rn(__fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmaf_rn(A.gme, smp, p0))),
+                        A.sow);
 
       if (reset == 0) {
         const float2 m = max2(max2(da[0], da[1]), max2(da[2], da[3]));
         const float eap = fmaxf(0.0f, fmaxf(m.x, m.y));
         const float ea = warp_max_xor(eap);
-        const float ev = warp_sum_xor(evp);
-        const float F = warp_sum_xor(fp);
-        const float L = ev > mmspt ? __fdiv_rn(__fmul_rn(ea, dt), ev) : 0.0f;
+        const float ev = ARITH ? evp : warp_sum_xor(evp);
+        // CTL 0: the summed margin; CTL 1: any failing section
+        const bool faulty = CTL == 0 ? warp_sum_xor(fp) > 0.0f : __any_sync(kFull, fault);
+        const float num = __fmul_rn(ea, dt);
+        const float L = ev > mmspt ? (ARITH ? __fdividef(num, ev) : __fdiv_rn(num, ev)) : 0.0f;
         // Step decisions are the same in every lane (they come from warp
         // reductions and uniform counters); taking them through a vote makes
         // that visible to the compiler, which then branches without
@@ -565,7 +672,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
           if (dt < A.dtmin) dt = A.dtmin;
           another = 0;
           reset = 1;
-        } else if (__all_sync(kFull, F > 0.0f)) {
+        } else if (__all_sync(kFull, faulty)) {
           another = 1;
           reset = 0;
         } else if (__all_sync(kFull, L < 0.5f)) {
@@ -594,8 +701,11 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
     smp_dt = __fadd_rn(smp_dt, dt);
     smp_it = __fadd_rn(smp_it, (float)out_loop);
 
-    if (__all_sync(kFull, tau > A.tout)) {
-      tau -= A.tout;
+    if (__all_sync(kFull, ARITH ? tau_f > A.tout_f : tau > A.tout)) {
+      if (ARITH)
+        tau_f = __fsub_rn(tau_f, A.tout_f);
+      else
+        tau -= A.tout;
       sx0 = sx1;
       sx1 = inb[n + 2];
       if (__all_sync(kFull, n >= un.out_first)) {
@@ -628,7 +738,10 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
     w0 = w;
     wd0 = wd;
     wdd0 = wdd;
-    tau += (double)dt;
+    if (ARITH)
+      tau_f = __fadd_rn(tau_f, dt);
+    else
+      tau += (double)dt;
   }
   if (st && lane == 0) {
     st->substeps = n_sub;
@@ -649,7 +762,7 @@ constexpr int bm_dyn_smem() {
                         (TOL == 2 ? ws::kBlobBytes + WARPS * ws::kWarpScratch : 0);
 }
 
-template <int WARPS, bool PREV_SMEM, int TOL>
+template <int WARPS, bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __device__ __forceinline__ void bm_body(const BMArgs& A) {
   __shared__ __align__(16) float s_par[8 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
@@ -691,16 +804,16 @@ __device__ __forceinline__ void bm_body(const BMArgs& A) {
       s_gam[warp][1][q] = __fmul_rn(gm, s_par[5 * 256 + q]);
     }
     __syncwarp();
-    run_unit<PREV_SMEM, TOL>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
+    run_unit<PREV_SMEM, TOL, CTL, ARITH>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
                              PREV_SMEM ? s_prev[warp] : nullptr, hist, scratch, wblob, lane,
                              A.stats ? A.stats + uid : nullptr);
     __syncwarp();
   }
 }
 
-template <int WARPS, int MINB, bool PREV_SMEM, int TOL>
+template <int WARPS, int MINB, bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs A) {
-  bm_body<WARPS, PREV_SMEM, TOL>(A);
+  bm_body<WARPS, PREV_SMEM, TOL, CTL, ARITH>(A);
 }
 
 // Launch shapes built: (warps per CTA, minimum resident CTAs per SM the
@@ -716,24 +829,27 @@ struct LaunchShape {
   int warps;
 };
 
-template <int W, int M, bool PS, int TOL>
+template <int W, int M, bool PS, int TOL, int CTL, int ARITH>
 void launch_shape(unsigned grid, cudaStream_t st, const BMArgs& A) {
-  bm_warp_kernel<W, M, PS, TOL><<<grid, W * 32, bm_dyn_smem<W, TOL>(), st>>>(A);
+  bm_warp_kernel<W, M, PS, TOL, CTL, ARITH><<<grid, W * 32, bm_dyn_smem<W, TOL>(), st>>>(A);
 }
 
-#define CGB_SHAPE(W, M, PS, TOL)                                                  \
-  {reinterpret_cast<const void*>(bm_warp_kernel<W, M, PS, TOL>), launch_shape<W, M, PS, TOL>, \
-   bm_dyn_smem<W, TOL>(), W}
+#define CGB_SHAPE(W, M, PS, TOL, CTL, ARITH)                                        \
+  {reinterpret_cast<const void*>(bm_warp_kernel<W, M, PS, TOL, CTL, ARITH>),           \
+   launch_shape<W, M, PS, TOL, CTL, ARITH>, bm_dyn_smem<W, TOL>(), W}
 
 const LaunchShape kShapes[] = {
-    CGB_SHAPE(4, 1, false, 0),
-    CGB_SHAPE(4, 3, false, 0),
-    CGB_SHAPE(4, 1, true, 0),
-    CGB_SHAPE(4, 3, true, 0),
+    CGB_SHAPE(4, 1, false, 0, 0, 0),
+    CGB_SHAPE(4, 3, false, 0, 0, 0),
+    CGB_SHAPE(4, 1, true, 0, 0, 0),
+    CGB_SHAPE(4, 3, true, 0, 0, 0),
 };
 // Tolerance-mode kernels: plain / extrapolated guess, and the learned guess.
-const LaunchShape kTolShape = CGB_SHAPE(4, 1, false, 1);
-const LaunchShape kLearnedShape = CGB_SHAPE(4, 1, false, 2);
+const LaunchShape kTolShape = CGB_SHAPE(4, 1, false, 1, 0, 0);
+const LaunchShape kLearnedShape = CGB_SHAPE(4, 1, false, 2, 0, 0);
+// BMOHC_NEW_kernel's controller, in the own order and in the reference's.
+const LaunchShape kCountShape = CGB_SHAPE(4, 1, false, 0, 1, 0);
+const LaunchShape kRefArithShape = CGB_SHAPE(4, 1, false, 0, 1, 1);
 int g_shape = 0;
 
 }  // namespace cgb
@@ -773,6 +889,15 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: bad sizes");
   if (sc->red_lanes != 32 || (sc->jacobi_mode != 0 && sc->jacobi_mode != 2))
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: only red_lanes=32, jacobi_mode 0 or 2 are built");
+  if (sc->controller != 0 && sc->controller != 1)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: controller must be 0 (kernel 17) or 1 "
+                             "(BMOHC_NEW_kernel)");
+  if (sc->arith != 0 && sc->arith != 1)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: arith must be 0 (own order) or 1 (reference)");
+  if (sc->arith == 1 && sc->controller != 1)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: arith 1 is built for controller 1 only");
+  if (sc->controller == 1 && sc->jacobi_mode != 0)
+    return fail(CGB_ERR_ARG, "cgb_bm_run_dev: controller 1 is built for jacobi_mode 0 only");
   if (sc->jacobi_fast < 0 || sc->jacobi_slow < 0 || sc->max_outer < 1 ||
       sc->max_substeps_per_sample < 1)
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: bad loop counts");
@@ -812,7 +937,14 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
   A.conv = d_conv;
   A.stats = d_stats;
   A.work = d_work;
-  A.ratio = sc->alpha_l / sc->alpha_s;
+  const bool ref_arith = sc->arith == 1;
+  // ARITH 1 takes alpha_L / alpha_s formed in double and rounded, as the
+  // reference host does for the kernels' constant (src/cochlea.cu:1104)
+  A.ratio = ref_arith ? (float)((double)sc->alpha_l / (double)sc->alpha_s)
+                      : sc->alpha_l / sc->alpha_s;
+  A.fs_f = (float)(1.0 / (double)sc->Ts);
+  A.rsow = (float)(1.0 / (double)sc->sigma_ow);
+  A.tout_f = sc->time_step_out;
   A.nas = -sc->alpha_s;
   A.al = sc->alpha_l;
   A.e1 = sc->eta_1;
@@ -848,7 +980,11 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
   CGB_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
   CGB_TRY_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev),
                "cudaDeviceGetAttribute");
-  const LaunchShape& shape = learned ? kLearnedShape : tol ? kTolShape : kShapes[g_shape];
+  const LaunchShape& shape = learned               ? kLearnedShape
+                             : tol                 ? kTolShape
+                             : ref_arith           ? kRefArithShape
+                             : sc->controller == 1 ? kCountShape
+                                                   : kShapes[g_shape];
   if (shape.dyn_smem > 48 * 1024) {
     static int configured[64] = {};
     if (dev < 64 && !configured[dev]) {

@@ -381,9 +381,19 @@ extern "C" void BMOHCKernel_Free() {
   release(H.work, H.work_n);
 }
 
+// Kernel selection (src/cochlea.cu:1258-2331).  Run_Fast_BM_Calculation 0,
+// the reference default (src/params.cpp:157), is BMOHC_NEW_kernel: this
+// library runs it with the reference's own step controller and operation
+// order (controller 1, arith 1).  17 is kernel 17, run with the full-sum
+// value of its step controller (controller 0, own operation order).  Other
+// variants are not built and raise.  BMOHC_Kernel_Configuration is only the
+// reference's cudaFuncSetCacheConfig hint (0-3), which changes no result;
+// the OHC nonlinearity and oval window are always on in both kernels, so
+// enable_psi / enable_OW other than 1 raise rather than being ignored.
 extern "C" void BMOHCNewKernel(
     float* input_samples, bool override_input_samples, float w_ohc, float time_step,
-    float time_step_out, float delta_x, float alpha_r, int, int, int, float Ts,
+    float time_step_out, float delta_x, float alpha_r, int enable_psi, int enable_OW, int,
+    float Ts,
     float _ohc_alpha_l, float _ohc_alpha_s, float model_Gme, float model_a0, float model_a1,
     float model_a2, float sigma_ow, float eta_1, float eta_2, float*, int Time_Blocks,
     int samplesBufferLengthP1, int overlap_nodes_for_block, long, int, float cuda_max_time_step,
@@ -391,8 +401,19 @@ extern "C" void BMOHCNewKernel(
     float Max_Tolerance_Parameter, int Relative_Error_Parameters,
     int calculate_boundary_conditions, float M1_SP_Fix_Factor, float Tolerance_Fix_Factor,
     float SPLREfVal, int, int, int, int JACOBBY_Loops_Fast, int JACOBBY_Loops_Slow,
-    int Cuda_Outern_Loops, int, int, cudaEvent_t&, cudaEvent_t&, cudaDeviceProp, Log&) {
+    int Cuda_Outern_Loops, int Run_Fast_BM_Calculation, int BMOHC_Kernel_Configuration,
+    cudaEvent_t&, cudaEvent_t&, cudaDeviceProp, Log&) {
   if (!H.secp) throw std::runtime_error("cochlea_gb300: BMOHCNewKernel before BMOHCKernel_Init");
+  if (Run_Fast_BM_Calculation != 0 && Run_Fast_BM_Calculation != 17)
+    throw std::runtime_error("cochlea_gb300: Run_Fast_BM_Calculation " +
+                             std::to_string(Run_Fast_BM_Calculation) +
+                             " is not built (0: BMOHC_NEW_kernel, 17: kernel 17)");
+  if (BMOHC_Kernel_Configuration < 0 || BMOHC_Kernel_Configuration > 3)
+    throw std::runtime_error("cochlea_gb300: BMOHC_Kernel_Configuration must be 0-3");
+  if (enable_psi != 1 || enable_OW != 1)
+    throw std::runtime_error(
+        "cochlea_gb300: enable_psi and enable_OW must be 1 (the reference's kernels 0 and 17 "
+        "always run the OHC nonlinearity and the oval window)");
   if ((size_t)samplesBufferLengthP1 + 2 > H.input_n)
     throw std::runtime_error("cochlea_gb300: input longer than the BMOHCKernel_Init buffer");
   if (!override_input_samples)
@@ -467,6 +488,8 @@ extern "C" void BMOHCNewKernel(
   sc.red_lanes = 32;
   sc.jacobi_mode = 0;
   sc.max_substeps_per_sample = 1 << 20;
+  sc.controller = Run_Fast_BM_Calculation == 0 ? 1 : 0;
+  sc.arith = Run_Fast_BM_Calculation == 0 ? 1 : 0;
   gpu_check(cudaMemset(H.failed, 0, H.failed_n * sizeof(int32_t)), "reset failed nodes");
   cgb_check(cgb_bm_run_dev(H.secp, H.gamma, 1, &sc, H.units, Time_Blocks, H.input,
                            (int64_t)H.input_n, H.speeds, rows, H.failed, H.conv, H.stats, H.work,

@@ -264,7 +264,11 @@ int main(int argc, char** argv) {
                    1e-6f, 1e-18f, D, (float)P.num("MAX_M1_SP_ERROR", 1e-15),
                    (float)P.num("MAX_TOLERANCE", 1e-10), 0, 0, 0.0f, 0.0f, (float)spl_ref, 0, 0,
                    0, (int)P.num("JACOBBY_Loops_Fast", 2), (int)P.num("JACOBBY_Loops_Slow", 20),
-                   (int)P.num("Cuda_Outern_Loops", 10), 17, 0, e0, e1, prop, log);
+                   (int)P.num("Cuda_Outern_Loops", 10),
+                   // kernel selection and cache hint, with the reference's
+                   // defaults (src/params.cpp:157,188)
+                   (int)P.num("Run_Fast_BM_Calculation", 0),
+                   (int)P.num("BMOHC_Kernel_Configuration", 2), e0, e1, prop, log);
     std::vector<float> v((size_t)total_nodes * 256);
     BMOHCKernel_Copy_Results(v.data(), v.size(), 0);
 

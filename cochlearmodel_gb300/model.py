@@ -92,6 +92,14 @@ class RunConfig:
     cuda_max_time_step: float = 1e-6  # CUDA_MAX_TIME_STEP
     cuda_min_time_step: float = 1e-18  # CUDA_MIN_TIME_STEP
     SPLRef: float = 2e-5
+    # BM kernel (src/cochlea.cu:1258-2331): 17 = kernel 17 with the full-sum
+    # value of its step controller, in this library's own operation order
+    # (the CPU oracle mirrors it bit for bit); 0 = BMOHC_NEW_kernel, the
+    # reference's default, with its fault-count controller and its own
+    # operation order (checked against the reference's compiled kernel).
+    # The reference's CParams defaults to 0; this host mirror defaults to 17,
+    # the kernel the reference recommends for speed (README.md:44,57).
+    Run_Fast_BM_Calculation: int = 17
 
     # --- derived node counts (include/params.h:288-395) ---
     @property
@@ -161,6 +169,10 @@ def bm_scalars(cfg: RunConfig, mv: ModelVectors) -> native.BMScalars:
     sc.jacobi_cap = 0
     sc.guess_mode = 0
     sc.learned_every = 1
+    if cfg.Run_Fast_BM_Calculation not in (0, 17):
+        raise native.CGBError(f"Run_Fast_BM_Calculation {cfg.Run_Fast_BM_Calculation} is not "
+                              "built (0: BMOHC_NEW_kernel, 17: kernel 17)")
+    sc.controller = sc.arith = 1 if cfg.Run_Fast_BM_Calculation == 0 else 0
     return sc
 
 

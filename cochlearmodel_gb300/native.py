@@ -37,7 +37,8 @@ class BMScalars(C.Structure):
             "jacobi_fast", "jacobi_slow", "max_outer", "red_lanes", "jacobi_mode",
             "max_substeps_per_sample")] + [("jacobi_tol", C.c_float), ("jacobi_cap", C.c_int32),
                                            ("guess_mode", C.c_int32),
-                                           ("learned_every", C.c_int32)]
+                                           ("learned_every", C.c_int32),
+                                           ("controller", C.c_int32), ("arith", C.c_int32)]
 
 
 class CGBError(RuntimeError):

@@ -91,6 +91,17 @@ typedef struct cgb_bm_scalars {
                            pressure, 1 linear extrapolation of the last two,
                            2 extrapolation + the network's correction        */
   int32_t learned_every;/* guess 2: network every n-th step (others: 1)      */
+  int32_t controller;   /* step controller: 0 kernel 17 (another iteration
+                           while the summed margin sum(|dv| - max(mtt, v dt))
+                           is positive; include/cochlea.cuh:14021-14105),
+                           1 BMOHC_NEW_kernel, the reference default (while
+                           any section fails |dv| <= max(mtt, v dt);
+                           include/cochlea.cuh:4080-4120); 1 needs
+                           jacobi_mode 0                                   */
+  int32_t arith;        /* 0: own floating-point order (double time
+                           accumulator), mirrored by the CPU oracle;
+                           1: BMOHC_NEW_kernel's operation order (tanhf,
+                           __fdividef, float time), needs controller 1    */
 } cgb_bm_scalars;
 
 /* Optional inputs of cgb_bm_run_ex_dev. */

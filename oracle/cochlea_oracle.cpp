@@ -181,6 +181,8 @@ typedef struct {
   int32_t guess_mode;  // mode 2 first-solve guess: 0 previous pressure, 1 extrapolated
                        // (2, the network's guess, is GPU-only and treated as 1 here)
   int32_t learned_every;
+  int32_t controller;  // 0 kernel 17 (summed margin), 1 BMOHC_NEW_kernel (any faulty section)
+  int32_t arith;       // the FP32 oracle evaluates the own order (0) only; FP64 ignores it
 } orc_bm_scalars;
 
 float orc_tanhf(float x) { return own_tanhf(x); }
@@ -497,19 +499,26 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
       wdd = A::fma(na1, w, A::fma(na2, wd, A::fma(Gme, smp, p[0]))) / sow;
       if (reset == 0) {
         T ea = 0;
+        bool any_fault = false;
         for (int s = 0; s < NS; ++s) {
           ea = A::max(ea, A::abs(aref[s] - a[s]));
-          flt[s] = dv[s] - A::max(mtt, v[s] * dt);
+          const T thr = A::max(mtt, v[s] * dt);
+          flt[s] = dv[s] - thr;
+          any_fault = any_fault || dv[s] > thr;
         }
         T ev = tree_sum<T>(dv, sc.red_lanes);
-        T F = tree_sum<T>(flt, sc.red_lanes);
+        // controller 0 (kernel 17): the summed margin is positive;
+        // controller 1 (BMOHC_NEW_kernel, include/cochlea.cuh:4080-4100):
+        // some section fails the speed test (its fault count is positive)
+        const bool faulty =
+            sc.controller == 1 ? any_fault : tree_sum<T>(flt, sc.red_lanes) > (T)0;
         T L = ev > mmspt ? (ea * dt) / ev : (T)0;
         if (L > (T)6) {
           dt = dt * (T)0.5;
           if (dt < dtmin) dt = dtmin;
           another = 0;
           reset = 1;
-        } else if (F > (T)0) {
+        } else if (faulty) {
           another = 1;
           reset = 0;
         } else if (L < (T)0.5) {

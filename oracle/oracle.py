@@ -33,7 +33,8 @@ class OrcScalars(C.Structure):
             "jacobi_fast", "jacobi_slow", "max_outer", "red_lanes", "jacobi_mode",
             "max_substeps_per_sample")] + [("jacobi_tol", C.c_float), ("jacobi_cap", C.c_int32),
                                            ("guess_mode", C.c_int32),
-                                           ("learned_every", C.c_int32)]
+                                           ("learned_every", C.c_int32),
+                                           ("controller", C.c_int32), ("arith", C.c_int32)]
 
 
 _lib = None
@@ -136,6 +137,9 @@ def bm_run(secp, gamma, sc, units, inp, out_rows, fp64=False, threads=None, jaco
     osc = scalars_from(sc)
     if jacobi_mode is not None:
         osc.jacobi_mode = jacobi_mode
+    if osc.arith and not fp64:
+        raise ValueError("the FP32 oracle evaluates the own operation order (arith 0); the "
+                         "reference order (arith 1) is checked against the reference's kernel")
     units = np.ascontiguousarray(units).view(UNIT_DTYPE)
     secp = np.ascontiguousarray(secp, np.float32)
     gamma = np.ascontiguousarray(gamma, np.float32)

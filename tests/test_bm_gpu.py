@@ -109,3 +109,29 @@ def test_every_launch_shape_bit_exact(mv, bm_solver):
             _compare(mv, bm_solver, case)
     finally:
         native.check(lib.cgb_bm_set_launch_shape(0), "set launch shape")
+
+
+@pytest.mark.parametrize("case", ["cfg1", "decoupled"])
+def test_fault_count_controller_bit_exact(mv, bm_solver, case):
+    """BMOHC_NEW_kernel's controller (another outer iteration while any
+    section fails the speed test) in the own operation order: bit-exact
+    against the oracle's controller 1."""
+    from cochlearmodel_gb300 import native
+    c = (cases.cfg1_slice(mv, ms=5.0) if case == "cfg1" else
+         cases.decoupled_sweep(mv, n_signals=2, decouple=2, block_ms=1.5, overlap_ms=0.5, seed=3))
+    cfg, sc, gamma, units, x, rows = c
+    s1 = native.BMScalars.from_buffer_copy(sc)
+    s1.controller = 1
+    _compare(mv, bm_solver, (cfg, s1, gamma, units, x, rows))
+
+
+def test_controller_arguments_rejected(mv, bm_solver):
+    from cochlearmodel_gb300 import native
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=0.5)
+    for ctl, ar, jm in [(2, 0, 0), (0, 1, 0), (1, 2, 0), (1, 0, 2)]:
+        s = native.BMScalars.from_buffer_copy(sc)
+        s.controller, s.arith, s.jacobi_mode = ctl, ar, jm
+        if jm == 2:
+            s.jacobi_cap, s.jacobi_tol = 8, 1e-6
+        with pytest.raises(native.CGBError):
+            bm_solver.run(s, gamma, units, x, rows)

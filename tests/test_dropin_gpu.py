@@ -26,6 +26,7 @@ JND_Interval_Tail = 0.0005
 AC_Filter_File = "{ac}"
 Input_Noise_File = "{noise}"
 Output_File = "{out}"
+Run_Fast_BM_Calculation = 17
 """
 
 

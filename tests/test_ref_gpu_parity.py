@@ -1,0 +1,107 @@
+"""Parity against the REFERENCE's own compiled kernels.
+
+oracle/_ref/cochlea_ref.cubin is the reference's src/cochlea.cu +
+include/cochlea.cuh compiled for sm_103a (oracle/build_ref_gpu.sh);
+oracle/ref_gpu.cpp launches its BMOHC_NEW_kernel (Run_Fast_BM_Calculation 0,
+the reference default) and kernel 17 with the constants its BMOHCNewKernel
+packs.
+
+- The product's reference-arithmetic mode (controller 1, arith 1) must equal
+  BMOHC_NEW_kernel bit for bit on every row it owns.  BMOHC_NEW_kernel also
+  writes row out_first - 1 of every block after the first, a row the previous
+  block owns (both blocks store it; which store lands is a race), and stores
+  row n's failure flag at index n + 1 (include/cochlea.cuh:4153-4157); the
+  comparison accounts for both.
+- Kernel 17 leaves its step controller's full sums only in lane 0 of warp 0
+  and lets all 32 lanes write the decision (include/cochlea.cuh:169-186,
+  14037-14087).  The product takes lane 0's values (controller 0).  Its
+  velocity is compared with the FP64 method and must be at least as close as
+  the reference's kernel 17 run here.
+"""
+import numpy as np
+import pytest
+
+from cochlearmodel_gb300 import native
+from oracle import oracle as orc
+from oracle import ref_gpu
+from tests import cases
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not ref_gpu.available(),
+                                 reason="reference cubin not built (oracle/build_ref_gpu.sh)")]
+
+
+def _ref_run(variant, cfg, sc, gamma, x, rows):
+    p = ref_gpu.params_from(cfg, sc)
+    secs = ref_gpu.sections_from(orc.model_setup(), gamma[0])
+    mtt = np.full(cfg.Time_Blocks, cfg.Max_Tolerance, np.float32)
+    mmspt = np.full(cfg.Time_Blocks, cfg.Max_M1_SP_Error, np.float32)
+    return ref_gpu.bm_run(variant, p, secs, mtt, mmspt, x, rows)
+
+
+def _owned(units, rows):
+    """Rows each block alone writes: [out_first, end), minus row out_first - 1
+    of every later block (the reference's shared boundary row)."""
+    mask = np.zeros(rows, bool)
+    for u in units:
+        mask[u["out_first"]:u["end"]] = True
+    mask[[int(u["out_first"]) - 1 for u in units[1:]]] = False
+    return mask
+
+
+def _max_rel(a, b):
+    return float(np.abs(a.astype(np.float64) - b).max() / np.abs(b).max())
+
+
+REF_CASES = {
+    "cfg1_60dB_1kHz_50ms": lambda mv: cases.cfg1_slice(mv, ms=50.0, db=60.0, freq=1000.0),
+    "cfg1_100dB_4kHz_10ms": lambda mv: cases.cfg1_slice(mv, ms=10.0, db=100.0, freq=4000.0),
+    "cfg1_20dB_250Hz_10ms": lambda mv: cases.cfg1_slice(mv, ms=10.0, db=20.0, freq=250.0),
+    "decoupled_3x4_blocks": lambda mv: cases.decoupled_sweep(mv, n_signals=3, decouple=4,
+                                                             block_ms=2.5, overlap_ms=1.0,
+                                                             seed=1),
+}
+
+
+@pytest.mark.parametrize("name", sorted(REF_CASES))
+def test_reference_arithmetic_bit_exact(mv, bm_solver, name):
+    cfg, sc, gamma, units, x, rows = REF_CASES[name](mv)
+    r_v, r_f, _ = _ref_run(0, cfg, sc, gamma, x, rows)
+    s1 = native.BMScalars.from_buffer_copy(sc)
+    s1.controller, s1.arith = 1, 1
+    v, f, st = bm_solver.run(s1, gamma, units, x, rows)
+    mask = _owned(units, rows)
+    assert np.abs(r_v[mask]).max() > 0
+    assert np.array_equal(v[mask], r_v[mask]), (
+        "differs from BMOHC_NEW_kernel: max-rel %.3e" % _max_rel(v[mask], r_v[mask]))
+    r_f_row = np.zeros_like(r_f)
+    r_f_row[:-1] = r_f[1:]
+    assert np.array_equal(f[mask], r_f_row[mask])
+
+
+def test_hearing_loss_profile_bit_exact(mv, bm_solver):
+    """A non-uniform OHC profile (0.5 ramping to 0.05 over sections 128-255)."""
+    cfg, sc, _, units, x, rows = cases.cfg1_slice(mv, ms=10.0, db=70.0, freq=1500.0)
+    gamma = cases.hearing_loss_gamma()[None]
+    r_v, _, _ = _ref_run(0, cfg, sc, gamma, x, rows)
+    s1 = native.BMScalars.from_buffer_copy(sc)
+    s1.controller, s1.arith = 1, 1
+    v, _, _ = bm_solver.run(s1, gamma, units, x, rows)
+    mask = _owned(units, rows)
+    assert np.array_equal(v[mask], r_v[mask])
+
+
+def test_kernel17_against_fp64(mv, bm_solver):
+    """Kernel 17 semantics: the product (lane-0 controller values, own
+    operation order) is closer to the FP64 method than the reference's
+    kernel 17 as it runs on this GPU, on full-length configuration 1."""
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=50.0, db=60.0, freq=1000.0)
+    r17, _, _ = _ref_run(17, cfg, sc, gamma, x, rows)
+    v, _, _ = bm_solver.run(sc, gamma, units, x, rows)
+    v64, _, _ = orc.bm_run(mv.section_params(), gamma, sc, units, x, rows, fp64=True)
+    mask = _owned(units, rows)
+    e_prod = _max_rel(v[mask], v64[mask])
+    e_ref = _max_rel(r17[mask], v64[mask])
+    print(f"max-rel vs FP64: product {e_prod:.3e}, reference kernel 17 {e_ref:.3e}")
+    assert e_prod <= 2e-4
+    assert e_prod <= e_ref
