@@ -16,6 +16,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -283,6 +284,121 @@ int refgpu_bm_run(int variant, const refgpu_bm_params* p, const float* const* se
   if (d_out.down(saved_speeds, (size_t)out_rows * kSections * 4)) return 1;
   if (failed_nodes && d_fn.down(failed_nodes, (size_t)out_rows * 4)) return 1;
   if (failed_blocks && d_fb.down(failed_blocks, (size_t)TB * 4)) return 1;
+  return 0;
+}
+
+// The reference's device_params (include/cochlea_common.h:31-49) and
+// vectors_sum_linear_coefficents (:50-54), the structs its IHC and lambda
+// kernels read from global memory; the layout must be the reference's.
+typedef struct {
+  int filter_b_start_index, filter_a_start_index, cochlea_sections, calcTime, writeTime;
+  int time_blocks, order_of_dc_filter, order_of_ac_filter, lambda_count, time_block;
+  int lambda_offset, ovelapNodes, FilterDecoupledMode;
+  double Lambda_SAT;
+  int intervalTimeNodes;
+  float reverseSQRTScaleBMVelocityForLambdaCalculation;
+  int Decouple_Filter;
+} refgpu_device_params;
+
+typedef struct {
+  double A_coefficent, B_coefficent;
+  int reverseCoefficents;
+} refgpu_sum_coefficients;
+
+// Runs the reference's IHC and lambda stage of one Run_Cuda chunk: the
+// unified CudaUnifiedCalcIHC<float> (src/cochlea.cu:3431-3506) on the grid
+// RunIHCKernel uses with Decouple_Unified_IHC_Factor = 0, the default
+// (src/cochlea.cu:3578-3594, src/params.cpp:195), then CudaCalcLambda
+// (src/cochlea.cu:3365-3408) on its setDecoupledRun grid (:3563-3571,
+// 3630-3632).  Parameters and constants are packed as IHCNewKernel packs them
+// (src/cochlea.cu:2485-2593).  In a FIR run RunIHCKernel first launches the
+// IIR kernel as well (:3587-3590); CudaUnifiedCalcIHC overwrites every
+// element that kernel writes before reading it, so it is not launched here.
+//   v            float[calcTime][256] BM velocity (cuda_saved_speeds)
+//   calc_time    rows of the chunk (calcTime; a multiple of 64 in Run_Cuda)
+//   interval     block nodes (intervalTimeNodes); time_blocks, decouple as
+//                Time_Blocks / Decouple_Filter (time_blocks % decouple == 0)
+//   ac, n_ac     AC FIR taps (double), multiplied by `scale` here as
+//                IHCNewKernel does; dc, n_dc the DC taps
+//   ihc_damage   double[256]; nerves float[9] (spont x3, unused x3, W x3);
+//                aihc float[3][256]
+// Outputs ihc float[calcTime][256] (written in place of the velocity) and
+// lam float[3][calcTime][256] (rows below interval * time_blocks valid).
+int refgpu_ihc_lambda(const float* v, int calc_time, int interval, int time_blocks,
+                      int decouple, const double* ac, int n_ac, const double* dc, int n_dc,
+                      double scale, double eta_ac, double eta_dc, double lambda_sat,
+                      const double* ihc_damage, const float* nerves, const float* aihc,
+                      float* ihc, float* lam) {
+  if (!g_mod) return fail("refgpu_ihc_lambda: refgpu_load first");
+  if (!v || !ac || !dc || !ihc_damage || !nerves || !aihc || !ihc || !lam)
+    return fail("refgpu_ihc_lambda: null argument");
+  if (calc_time < 1 || interval < 1 || time_blocks < 1 || decouple < 0 ||
+      (decouple > 0 && time_blocks % decouple) || interval * time_blocks > calc_time)
+    return fail("refgpu_ihc_lambda: bad sizes");
+  if (n_ac < 1 || n_dc < 1 || n_ac + n_dc + 2 > 1024)
+    return fail("refgpu_ihc_lambda: filters exceed DEVICE_MAX_FILTER_ORDER");
+  CUfunction f_ihc = find_fn("_Z18CudaUnifiedCalcIHCIfE");
+  CUfunction f_lam = find_fn("_Z14CudaCalcLambdaIffE");
+  if (!f_ihc || !f_lam) return fail("refgpu_ihc_lambda: kernels not found in the cubin");
+  RG_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+
+  // device_time_filter: [n_dc, dc..., n_ac, ac * scale...] (src/cochlea.cu:2485-2503)
+  std::vector<double> filt(1024, 0.0);
+  filt[0] = n_dc;
+  for (int i = 0; i < n_dc; ++i) filt[1 + i] = dc[i];
+  const int ac_b = n_dc + 1;
+  filt[ac_b] = n_ac;
+  for (int i = 0; i < n_ac; ++i) filt[ac_b + 1 + i] = scale * ac[i];
+  if (set_symbol("device_time_filter", filt.data(), filt.size() * sizeof(double))) return 1;
+  if (set_symbol("CUDA_IHC_DAMAGE", ihc_damage, kSections * sizeof(double))) return 1;
+  if (set_symbol("CUDA_Nerves_Clusters", nerves, 9 * sizeof(float))) return 1;
+  if (set_symbol("model_Aihc", aihc, 3 * kSections * sizeof(float))) return 1;
+
+  // device params and sum coefficients (src/cochlea.cu:2550-2590)
+  refgpu_device_params prm[2] = {};
+  prm[0].Decouple_Filter = decouple;
+  prm[0].cochlea_sections = kSections;
+  prm[0].intervalTimeNodes = interval;
+  prm[0].time_blocks = time_blocks;
+  prm[0].ovelapNodes = 0;
+  prm[0].lambda_offset = 0;
+  prm[0].order_of_dc_filter = n_dc;
+  prm[0].order_of_ac_filter = n_ac;
+  prm[0].lambda_count = 3;
+  prm[0].time_block = calc_time / time_blocks;
+  prm[0].FilterDecoupledMode = decouple > 0;
+  prm[0].reverseSQRTScaleBMVelocityForLambdaCalculation = 1.0f / sqrtf((float)scale);
+  prm[0].Lambda_SAT = (float)lambda_sat;
+  prm[0].calcTime = calc_time;
+  prm[0].writeTime = calc_time;
+  prm[0].filter_b_start_index = ac_b;
+  prm[0].filter_a_start_index = -1;
+  prm[1] = prm[0];
+  prm[1].filter_b_start_index = 0;
+  prm[1].filter_a_start_index = -1;
+  refgpu_sum_coefficients coef[2] = {{scale, -1.0, 0}, {eta_ac, eta_dc, 0}};
+
+  const size_t plane = (size_t)calc_time * kSections;
+  DBuf d_v, d_lam, d_buf1, d_prm, d_coef;
+  if (d_v.alloc(plane * 4) || d_v.up(v, plane * 4)) return 1;
+  if (d_lam.alloc(3 * plane * 4) || d_buf1.alloc(3 * plane * 4)) return 1;
+  if (d_prm.alloc(sizeof(prm)) || d_prm.up(prm, sizeof(prm))) return 1;
+  if (d_coef.alloc(sizeof(coef)) || d_coef.up(coef, sizeof(coef))) return 1;
+
+  CUdeviceptr b2 = d_lam.p, b3 = d_lam.p + plane * 4, b4 = d_lam.p + 2 * plane * 4;
+  int backup_stage = 0;
+  void* a1[] = {&d_v.p, &b2, &b3, &b4, &d_buf1.p, &d_prm.p, &d_coef.p, &backup_stage};
+  // IHC_FILTER_BLOCK x (SECTIONS_PER_IHC_FILTER_BLOCK, THREADS_PER_IHC_FILTER_SECTION)
+  RG_TRY(cuLaunchKernel(f_ihc, kSections / 16, 1, 1, 16, 64, 1, 0, nullptr, a1, nullptr),
+         "cuLaunchKernel (reference CudaUnifiedCalcIHC)");
+  const int dfilter = decouple > 0 ? decouple : time_blocks;
+  int save_lambda = 1;
+  void* a2[] = {&d_v.p, &d_buf1.p, &d_lam.p, &d_prm.p, &save_lambda};
+  RG_TRY(cuLaunchKernel(f_lam, 3 * time_blocks / dfilter, dfilter, 1, kSections, 1, 1, 0, nullptr,
+                        a2, nullptr),
+         "cuLaunchKernel (reference CudaCalcLambda)");
+  RG_TRY(cuCtxSynchronize(), "reference IHC/lambda kernels");
+  if (d_v.down(ihc, plane * 4) || d_lam.down(lam, 3 * plane * 4)) return 1;
   return 0;
 }
 

@@ -58,6 +58,9 @@ def load():
         lib.refgpu_load.argtypes = [C.c_char_p]
         lib.refgpu_bm_run.argtypes = [C.c_int, C.POINTER(RefBMParams), _p, _p, _p, _p,
                                       C.c_longlong, _p, C.c_longlong, _p, _p]
+        lib.refgpu_ihc_lambda.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, _p, C.c_int,
+                                          _p, C.c_int, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, _p, _p, _p, _p, _p]
         if not CUBIN.exists():
             raise FileNotFoundError(f"{CUBIN} is missing (built by oracle/build_ref_gpu.sh)")
         if lib.refgpu_load(str(CUBIN).encode()):
@@ -127,3 +130,28 @@ def bm_run(variant: int, params: RefBMParams, sections, mtt, mmspt, inp, out_row
     if rc:
         raise RuntimeError(lib.refgpu_last_error().decode())
     return out, fn, fb
+
+
+def ihc_lambda(v, calc_time, interval, time_blocks, decouple, ac, dc, scale, eta_ac, eta_dc,
+               lambda_sat, ihc_damage, spont, W, aihc):
+    """The reference's CudaUnifiedCalcIHC + CudaCalcLambda over one chunk of
+    calc_time velocity rows (see refgpu_ihc_lambda); returns
+    (ihc float32[calc_time,256], lambda float32[3, calc_time, 256])."""
+    lib = load()
+    vin = np.zeros((calc_time, 256), np.float32)
+    vin[:len(v)] = v
+    ihc = np.zeros((calc_time, 256), np.float32)
+    lam = np.zeros((3, calc_time, 256), np.float32)
+    ac = np.ascontiguousarray(ac, np.float64)
+    dc = np.ascontiguousarray(dc, np.float64)
+    nerves = np.zeros(9, np.float32)
+    nerves[:3] = spont
+    nerves[6:] = W
+    rc = lib.refgpu_ihc_lambda(_ptr(vin), calc_time, interval, time_blocks, decouple, _ptr(ac),
+                               len(ac), _ptr(dc), len(dc), scale, eta_ac, eta_dc, lambda_sat,
+                               _ptr(np.ascontiguousarray(ihc_damage, np.float64)),
+                               _ptr(nerves), _ptr(np.ascontiguousarray(aihc, np.float32)),
+                               _ptr(ihc), _ptr(lam))
+    if rc:
+        raise RuntimeError(lib.refgpu_last_error().decode())
+    return ihc, lam

@@ -105,3 +105,54 @@ def test_kernel17_against_fp64(mv, bm_solver):
     print(f"max-rel vs FP64: product {e_prod:.3e}, reference kernel 17 {e_ref:.3e}")
     assert e_prod <= 2e-4
     assert e_prod <= e_ref
+
+
+LAMBDA_REL = 1e-4  # the lambda bar: max |a - b| / max |b| per plane
+
+
+@pytest.fixture(scope="module")
+def ihc_stage():
+    from cochlearmodel_gb300 import ihc
+    return ihc.IHCStage("cuda:0")
+
+
+@pytest.mark.parametrize("case", ["decoupled", "cfg1_10ms"])
+def test_lambda_against_reference_kernels(mv, ihc_stage, case):
+    """The fused IHC/lambda kernel against the reference's CudaUnifiedCalcIHC
+    + CudaCalcLambda on the same velocity, one Run_Cuda chunk.  The
+    reference accumulates the FIR in double; this kernel in compensated
+    FP32 (Dot2).  The oracle's restatement of the reference arithmetic (mode
+    0) is checked against the reference kernels too."""
+    from cochlearmodel_gb300 import ihc
+    if case == "decoupled":
+        c = cases.decoupled_sweep(mv, n_signals=2, decouple=2, block_ms=1.5, overlap_ms=0.5)
+    else:
+        c = cases.cfg1_slice(mv, ms=10.0, db=80.0, freq=2000.0)
+    cfg, sc, gamma, units, x, rows = c
+    v, _, _ = orc.bm_run(mv.section_params(), gamma, sc, units, x, rows)
+    fr = ihc.reference_frame(cfg)
+    n, lam_rows = int(fr["rows"][0]), int(fr["lam_rows"][0])
+    v = v[:n]
+    st = ihc_stage
+    lam, ih = st.run(v, fr, lam_rows, want_ihc=True)
+    nerve = st.nerve
+    r_ihc, r_lam = ref_gpu.ihc_lambda(
+        v, int(fr["total"][0]), cfg.calc_time_block_nodes(), cfg.Time_Blocks,
+        cfg.Decouple_Filter, st.ac.astype(np.float64), st.dc.astype(np.float64), nerve.scale,
+        nerve.eta_AC, nerve.eta_DC, nerve.Lambda_SAT, st.dmg_host[0].astype(np.float64),
+        np.asarray(nerve.spontRate, np.float32), np.asarray(nerve.W, np.float32), nerve.aihc())
+    _, o_lam = orc.ihc_lambda(v, int(fr["seg"][0]), int(fr["frdp"][0]), int(fr["total"][0]),
+                              lam_rows, st.ac.astype(np.float64), st.dc.astype(np.float64),
+                              nerve.scale, nerve.eta_AC, nerve.eta_DC,
+                              st.dmg_host[0].astype(np.float64), nerve.aihc(),
+                              np.asarray(nerve.spontRate, np.float32), nerve.Lambda_SAT, mode=0)
+    worst_prod = worst_orc = 0.0
+    for j in range(3):
+        ref = r_lam[j, :lam_rows]
+        worst_prod = max(worst_prod, _max_rel(lam[j, :lam_rows], ref))
+        worst_orc = max(worst_orc, _max_rel(o_lam[j, :lam_rows], ref))
+    print(f"lambda max-rel vs the reference kernels: product {worst_prod:.2e}, "
+          f"oracle mode 0 {worst_orc:.2e}")
+    assert worst_prod <= LAMBDA_REL
+    assert worst_orc <= 1e-6
+    assert np.abs(ih[:lam_rows] - r_ihc[:lam_rows]).max() <= 1e-4 * np.abs(r_ihc).max()
