@@ -402,4 +402,103 @@ int refgpu_ihc_lambda(const float* v, int calc_time, int interval, int time_bloc
   return 0;
 }
 
+// The reference's device_jnd_params (include/cochlea_common.h:56-66).
+typedef struct {
+  double dA, recipdA, dBSPLSignal, dBSPLNoise, Wn;
+  bool isReference;
+  int calculateIndexPosition, referenceIndex;
+  double frequency;
+} refgpu_jnd_params;
+
+// Runs the reference's GlobalCalculateMeanRate and GlobalCalculateJND
+// (src/cochlea.cu:3741-3944) on the grid CudaCalculateJND uses
+// (src/cochlea.cu:4009-4010), over every interval of one run
+// (handeledIntervalsJND = 0, both the AI and the rate JND, dA given).
+//   lam        float[3][plane_rows][256] lambda (cuda_JND_Lambda)
+//   n_int      intervals; interval_nodes, head, length: JNDIntervalLength,
+//              JNDIntervalHeadNodes, lengthOffset
+//   dA         double[n_int]; ref_of int[n_int]: each interval's reference
+//              interval (ref_of[i] == i for a reference)
+//   nihc       double[256]; W float[3]; Fs; factor (JND_Delta_Alpha_Length_Factor)
+// Outputs F_RA and F_AI float[3][n_int] (the references' entries are left 0).
+int refgpu_jnd(const float* lam, int plane_rows, int n_int, int interval_nodes, int head,
+               int length, const double* dA, const int* ref_of, const double* nihc,
+               const float* W, double Fs, double factor, float* F_RA, float* F_AI) {
+  if (!g_mod) return fail("refgpu_jnd: refgpu_load first");
+  if (!lam || !dA || !ref_of || !nihc || !W || !F_RA || !F_AI)
+    return fail("refgpu_jnd: null argument");
+  if (n_int < 1 || length < 1 || head < 0 ||
+      (long long)(n_int - 1) * interval_nodes + head + length > plane_rows)
+    return fail("refgpu_jnd: windows outside the lambda planes");
+  CUfunction f_mr = find_fn(mangled("GlobalCalculateMeanRate"));
+  CUfunction f_jnd = find_fn(mangled("GlobalCalculateJND"));
+  if (!f_mr || !f_jnd) return fail("refgpu_jnd: kernels not found in the cubin");
+  RG_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+  float nerves[9] = {};
+  for (int j = 0; j < 3; ++j) nerves[6 + j] = W[j];
+  if (set_symbol("CUDA_Nerves_Clusters", nerves, sizeof(nerves))) return 1;
+
+  // interval tables as the host JND setup forms them: references, the tested
+  // intervals in order, each interval's position among the tested ones and
+  // each tested position's reference
+  std::vector<refgpu_jnd_params> prm(n_int);
+  std::vector<int> refs, calc, serial(n_int, 0), to_ref;
+  for (int i = 0; i < n_int; ++i) {
+    prm[i] = refgpu_jnd_params{};
+    prm[i].dA = dA[i];
+    prm[i].recipdA = dA[i] != 0.0 ? 1.0 / dA[i] : 0.0;
+    prm[i].isReference = ref_of[i] == i;
+    if (ref_of[i] < 0 || ref_of[i] >= n_int) return fail("refgpu_jnd: bad reference index");
+    if (ref_of[i] == i) {
+      refs.push_back(i);
+    } else {
+      serial[i] = (int)calc.size();
+      calc.push_back(i);
+      to_ref.push_back(ref_of[i]);
+    }
+  }
+  if (refs.empty()) refs.push_back(-1);
+  if (calc.empty()) {
+    calc.push_back(0);
+    to_ref.push_back(0);
+  }
+  const size_t plane = (size_t)plane_rows * kSections;
+  DBuf d_prm, d_lam, d_mr, d_buf, d_nihc, d_refs, d_calc, d_serial, d_toref, d_fra, d_fai, d_gp;
+  if (d_prm.alloc(prm.size() * sizeof(refgpu_jnd_params)) ||
+      d_prm.up(prm.data(), prm.size() * sizeof(refgpu_jnd_params)))
+    return 1;
+  if (d_lam.alloc(3 * plane * 4) || d_lam.up(lam, 3 * plane * 4)) return 1;
+  if (d_mr.alloc((size_t)3 * n_int * kSections * 4) || d_buf.alloc(3 * plane * 4)) return 1;
+  if (d_nihc.alloc(kSections * 8) || d_nihc.up(nihc, kSections * 8)) return 1;
+  if (d_refs.alloc(refs.size() * 4) || d_refs.up(refs.data(), refs.size() * 4)) return 1;
+  if (d_calc.alloc(calc.size() * 4) || d_calc.up(calc.data(), calc.size() * 4)) return 1;
+  if (d_serial.alloc(serial.size() * 4) || d_serial.up(serial.data(), serial.size() * 4)) return 1;
+  if (d_toref.alloc(to_ref.size() * 4) || d_toref.up(to_ref.data(), to_ref.size() * 4)) return 1;
+  if (d_fra.alloc((size_t)3 * n_int * 4) || d_fai.alloc((size_t)3 * n_int * 4)) return 1;
+  if (d_gp.alloc(2 * sizeof(refgpu_device_params))) return 1;
+
+  int calc_matrix = (int)plane, write_matrix = (int)plane, overlap = 0;
+  int jnd_intervals = n_int, jnd_full = n_int, use_spont = 0;
+  void* a1[] = {&d_prm.p, &d_lam.p, &d_mr.p, &length, &calc_matrix, &jnd_intervals,
+                &interval_nodes, &head, &overlap, &use_spont};
+  RG_TRY(cuLaunchKernel(f_mr, n_int, 3, 1, kSections, 1, 1, 0, nullptr, a1, nullptr),
+         "cuLaunchKernel (reference GlobalCalculateMeanRate)");
+  bool calc_ai = true, calc_rms = true;
+  double scale = 1.0;
+  int n_calc = (int)calc.size(), n_refs = refs[0] < 0 ? 0 : (int)refs.size(), handled = 0;
+  int is_da_calced = 0, backup_stage = 0;
+  void* a2[] = {&calc_ai,   &calc_rms,   &d_prm.p,     &d_lam.p,    &d_mr.p,       &d_buf.p,
+                &d_nihc.p,  &Fs,         &scale,       &write_matrix, &calc_matrix, &overlap,
+                &head,      &interval_nodes, &length,  &jnd_intervals, &jnd_full,  &d_calc.p,
+                &n_calc,    &d_refs.p,   &n_refs,      &handled,    &d_serial.p,   &d_toref.p,
+                &d_fra.p,   &d_fai.p,    &factor,      &d_gp.p,     &is_da_calced, &use_spont,
+                &backup_stage};
+  RG_TRY(cuLaunchKernel(f_jnd, n_int, 3, 1, kSections, 1, 1, 0, nullptr, a2, nullptr),
+         "cuLaunchKernel (reference GlobalCalculateJND)");
+  RG_TRY(cuCtxSynchronize(), "reference JND kernels");
+  if (d_fra.down(F_RA, (size_t)3 * n_int * 4) || d_fai.down(F_AI, (size_t)3 * n_int * 4))
+    return 1;
+  return 0;
+}
+
 }  // extern "C"

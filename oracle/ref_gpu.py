@@ -61,6 +61,8 @@ def load():
         lib.refgpu_ihc_lambda.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, _p, C.c_int,
                                           _p, C.c_int, C.c_double, C.c_double, C.c_double,
                                           C.c_double, _p, _p, _p, _p, _p]
+        lib.refgpu_jnd.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _p, _p, _p,
+                                   _p, C.c_double, C.c_double, _p, _p]
         if not CUBIN.exists():
             raise FileNotFoundError(f"{CUBIN} is missing (built by oracle/build_ref_gpu.sh)")
         if lib.refgpu_load(str(CUBIN).encode()):
@@ -155,3 +157,21 @@ def ihc_lambda(v, calc_time, interval, time_blocks, decouple, ac, dc, scale, eta
     if rc:
         raise RuntimeError(lib.refgpu_last_error().decode())
     return ihc, lam
+
+
+def jnd(lam, n_int, interval_nodes, head, length, dA, ref_of, nihc, W, Fs, factor):
+    """The reference's GlobalCalculateMeanRate + GlobalCalculateJND over every
+    interval (see refgpu_jnd); returns (F_RA, F_AI) float32[3, n_int]."""
+    lib = load()
+    lam = np.ascontiguousarray(lam, np.float32)
+    F_RA = np.zeros((3, n_int), np.float32)
+    F_AI = np.zeros((3, n_int), np.float32)
+    rc = lib.refgpu_jnd(_ptr(lam), lam.shape[1], n_int, interval_nodes, head, length,
+                        _ptr(np.ascontiguousarray(dA, np.float64)),
+                        _ptr(np.ascontiguousarray(ref_of, np.int32)),
+                        _ptr(np.ascontiguousarray(nihc, np.float64)),
+                        _ptr(np.ascontiguousarray(W, np.float32)), Fs, factor, _ptr(F_RA),
+                        _ptr(F_AI))
+    if rc:
+        raise RuntimeError(lib.refgpu_last_error().decode())
+    return F_RA, F_AI

@@ -156,3 +156,44 @@ def test_lambda_against_reference_kernels(mv, ihc_stage, case):
     assert worst_prod <= LAMBDA_REL
     assert worst_orc <= 1e-6
     assert np.abs(ih[:lam_rows] - r_ihc[:lam_rows]).max() <= 1e-4 * np.abs(r_ihc).max()
+
+
+JND_DB_TOL = 0.1  # dB
+
+
+def test_jnd_against_reference_kernels(mv):
+    """The profile-mode path's JND against the reference's
+    GlobalCalculateMeanRate + GlobalCalculateJND run on the same lambda.  The
+    reference sums in FP32 with rsqrt-squared reciprocals; this library sums
+    in FP64.  The final JNDs (calcJNDFinal's dB) agree within 0.1 dB, and the
+    Fisher sums within the FP32 summation error."""
+    import torch
+    from cochlearmodel_gb300 import model
+    from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun, ProfileSweep
+    cfg = model.RunConfig(Time_Block_Length=0.002, Decouple_Filter=2, Overlap_Time=0.001,
+                          OHC_Vector=np.linspace(0.5, 0.05, 256, dtype=np.float32),
+                          IHC_Vector=np.linspace(8, 5, 256, dtype=np.float32))
+    sweep = ProfileSweep(frequencies=[1000.0, 3000.0], powers=[40.0, 80.0],
+                         noises=[1111.0, 30.0], calculate_jnd=True)
+    noise = np.random.default_rng(7).standard_normal(400).astype(np.float32)
+    run = ProfileRun("cuda:0", cfg, sweep, noise=noise, mv=mv,
+                     jnd=JNDWindow(head=0.001, tail=0.0005))
+    run.step()
+    torch.cuda.synchronize()
+    lam = run.d_lam.cpu().numpy()
+    r_ra, r_ai = ref_gpu.jnd(lam, run.n_int, run.L, run.head, run.len, run.prof["dA"],
+                             run.ref_of, run.nerve.nihc(), np.asarray(run.nerve.W, np.float32),
+                             float(cfg.Fs), 0.2 * cfg.Fs)
+    rate_db, ai_db, F_RA, F_AI = run.jnd_db()
+    tested = run.ref_of != np.arange(run.n_int)
+    assert tested.sum() == 8
+    worst_db = 0.0
+    for got_db, ref in ((rate_db, r_ra), (ai_db, r_ai)):
+        want_db = np.array([orc.jnd_db(ref[:, i].astype(np.float64).sum())
+                            for i in range(run.n_int)])
+        worst_db = max(worst_db, float(np.abs(got_db[tested] - want_db[tested]).max()))
+    rel = max(float((np.abs(F_RA[:, tested] - r_ra[:, tested]) / np.abs(r_ra[:, tested])).max()),
+              float((np.abs(F_AI[:, tested] - r_ai[:, tested]) / np.abs(r_ai[:, tested])).max()))
+    print(f"JND vs the reference kernels: {worst_db:.2e} dB, Fisher sums max-rel {rel:.2e}")
+    assert worst_db <= JND_DB_TOL
+    assert rel <= 1e-3
