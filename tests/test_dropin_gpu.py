@@ -28,6 +28,9 @@ Input_Noise_File = "{noise}"
 Output_File = "{out}"
 Run_Fast_BM_Calculation = 17
 """
+# the same run with the reference's default kernel selection (no
+# Run_Fast_BM_Calculation key: BMOHC_NEW_kernel)
+PAR_DEFAULT_KERNEL = PAR.replace("Run_Fast_BM_Calculation = 17\n", "")
 
 
 def read_out(path):
@@ -48,7 +51,8 @@ def read_out(path):
     return v, lam, fra, fai, jr, ja
 
 
-def test_harness_matches_pipeline(tmp_path, mv):
+@pytest.mark.parametrize("kernel", [17, 0])
+def test_harness_matches_pipeline(tmp_path, mv, kernel):
     import torch
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -58,7 +62,8 @@ def test_harness_matches_pipeline(tmp_path, mv):
     (tmp_path / "noise.f32").write_bytes(noise.tobytes())
     out = tmp_path / "out.bin"
     par = tmp_path / "run.par"
-    par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32", out=out))
+    text = PAR if kernel == 17 else PAR_DEFAULT_KERNEL
+    par.write_text(text.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32", out=out))
     build.build()
     res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
                          timeout=300)
@@ -67,7 +72,8 @@ def test_harness_matches_pipeline(tmp_path, mv):
 
     cfg = model.RunConfig(Time_Block_Length=0.002, Decouple_Filter=2, Overlap_Time=0.001,
                           OHC_Vector=np.array([0.5, 0.3, 0.1], np.float32),
-                          IHC_Vector=np.array([8.0, 6.0], np.float32))
+                          IHC_Vector=np.array([8.0, 6.0], np.float32),
+                          Run_Fast_BM_Calculation=kernel)
     sweep = ProfileSweep(frequencies=[1000.0, 3000.0], powers=[40.0, 80.0],
                          noises=[1111.0, 30.0], calculate_jnd=True)
     run = ProfileRun("cuda:0", cfg, sweep, noise=noise, mv=mv, ac_taps=ac,
@@ -194,3 +200,24 @@ def test_harness_writes_the_reference_output_files(tmp_path, mv):
     cols = n_calc // (2 * 2) * 2  # tested intervals / (powers x frequencies) x powers
     jnd = np.fromfile(jnd_bin, np.float32)
     assert np.array_equal(jnd, np.concatenate([_transpose(ai, cols), _transpose(rate, cols)]))
+
+
+def test_unbuilt_kernel_selectors_raise(tmp_path, mv):
+    """BMOHCNewKernel raises for Run_Fast_BM_Calculation values, cache hints
+    and enable flags it does not build, instead of running another solver."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
+    (tmp_path / "ac.f32").write_bytes(ihc.design_ac_lowpass().tobytes())
+    (tmp_path / "noise.f32").write_bytes(noise.tobytes())
+    build.build()
+    for extra in ("Run_Fast_BM_Calculation = 5\n", "BMOHC_Kernel_Configuration = 7\n"):
+        par = tmp_path / "bad.par"
+        par.write_text(PAR_DEFAULT_KERNEL.format(ac=tmp_path / "ac.f32",
+                                                 noise=tmp_path / "noise.f32",
+                                                 out=tmp_path / "o.bin") + extra)
+        res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True,
+                             text=True, timeout=300)
+        assert res.returncode != 0
+        assert "Run_Fast_BM_Calculation" in res.stderr or "BMOHC_Kernel_Configuration" in res.stderr

@@ -197,3 +197,51 @@ def test_jnd_against_reference_kernels(mv):
     print(f"JND vs the reference kernels: {worst_db:.2e} dB, Fisher sums max-rel {rel:.2e}")
     assert worst_db <= JND_DB_TOL
     assert rel <= 1e-3
+
+
+def test_whole_profile_path_on_the_reference_default(mv):
+    """Run_Fast_BM_Calculation = 0 end to end: the profile-mode path
+    (generated input -> BM -> IHC/lambda -> JND) against the reference's own
+    kernels chained on the same input.  Velocity is bit-exact; lambda and the
+    JNDs carry only the IHC and JND stages' own differences."""
+    import torch
+    from cochlearmodel_gb300 import ihc, model
+    from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun, ProfileSweep
+    cfg = model.RunConfig(Time_Block_Length=0.003, Decouple_Filter=2, Overlap_Time=0.001,
+                          OHC_Vector=cases.hearing_loss_gamma(),
+                          IHC_Vector=np.linspace(8, 5, 256, dtype=np.float32),
+                          Run_Fast_BM_Calculation=0)
+    sweep = ProfileSweep(frequencies=[1000.0], powers=[30.0, 60.0, 90.0],
+                         noises=[1111.0, 20.0], calculate_jnd=True)
+    noise = np.random.default_rng(5).standard_normal(600).astype(np.float32)
+    run = ProfileRun("cuda:0", cfg, sweep, noise=noise, mv=mv,
+                     jnd=JNDWindow(head=0.001, tail=0.0005))
+    run.step()
+    torch.cuda.synchronize()
+    x = run.d_in.cpu().numpy()
+    r_v, _, _ = _ref_run(0, run.cfg, run.sc, run.cfg.gamma()[None], x, run.rows)
+    v = run.d_v.cpu().numpy()
+    mask = _owned(run.units, run.rows)
+    assert np.array_equal(v[mask], r_v[mask])
+
+    fr = run.frames[0]
+    st, nerve = run.ihc, run.nerve
+    n, lam_rows = int(fr["rows"]), int(fr["lam_rows"])
+    r_vin = v[:n].copy()  # the owned rows agree; the product's copy has no boundary races
+    _, r_lam = ref_gpu.ihc_lambda(
+        r_vin, int(fr["total"]), cfg.calc_time_block_nodes(), cfg.Time_Blocks,
+        cfg.Decouple_Filter, st.ac.astype(np.float64), st.dc.astype(np.float64), nerve.scale,
+        nerve.eta_AC, nerve.eta_DC, nerve.Lambda_SAT, st.dmg_host[0].astype(np.float64),
+        np.asarray(nerve.spontRate, np.float32), np.asarray(nerve.W, np.float32), nerve.aihc())
+    lam = run.d_lam.cpu().numpy()
+    for j in range(3):
+        assert _max_rel(lam[j], r_lam[j, :lam_rows]) <= LAMBDA_REL
+    r_ra, r_ai = ref_gpu.jnd(r_lam[:, :lam_rows], run.n_int, run.L, run.head, run.len,
+                             run.prof["dA"], run.ref_of, nerve.nihc(),
+                             np.asarray(nerve.W, np.float32), float(cfg.Fs), 0.2 * cfg.Fs)
+    rate_db, ai_db, _, _ = run.jnd_db()
+    tested = run.ref_of != np.arange(run.n_int)
+    for got_db, ref in ((rate_db, r_ra), (ai_db, r_ai)):
+        want_db = np.array([orc.jnd_db(ref[:, i].astype(np.float64).sum())
+                            for i in range(run.n_int)])
+        assert np.abs(got_db[tested] - want_db[tested]).max() <= JND_DB_TOL
