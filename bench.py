@@ -32,9 +32,12 @@ single-signal"), and the CPU restatement on the host cores.
 Arms:
   default            the GB300 kernels (value: device time; e2e: host tables in,
                      velocity + lambda back to host, through the C ABI)
-  --impl reference   the reference algorithm on the host cores (the CPU
-                     restatement of the path; the reference ships no runnable
-                     CPU path of its own), bounded sample per step
+  --impl reference   the path on the host cores through the CPU oracle alone
+                     (input generation, BM, IHC/lambda, JND; the reference ships
+                     no runnable CPU path of its own, and its IHC/lambda
+                     restatement equals the reference's kernels bit for bit);
+                     each step a bounded sample of the sweep; no part of the
+                     GPU library is loaded
 """
 from __future__ import annotations
 
@@ -281,6 +284,142 @@ def cpu_sample(run, target_s=15.0, threads=None):
                                f"{dt:.1f} s")
 
 
+class RefSweepCPU:
+    """The JND sweep (configuration 3) on the host cores through the oracle
+    alone: input generation (orc.input_gen), BM in FP32 with the reference
+    schedule (orc.bm_run), IHC/lambda in the reference's mixed precision
+    (orc.ihc_lambda mode 0, which equals the reference's own kernels bit for
+    bit) and the JND Fisher sums in the reference's float arithmetic
+    (orc.jnd).  The signals, lengths, partitions and filters are those of the
+    GPU arm's workload, built from the same seeded description; no part of
+    the product library is loaded (the model, unit tables and section
+    parameters come from the oracle).  A step runs one group's reference
+    interval plus its first m tested intervals; step() returns the audio
+    seconds it simulated."""
+
+    def __init__(self, n_seeds=4, Fs=100000, overlap_time=0.005, block_target=1000):
+        from cochlearmodel_gb300 import batch, ihc
+        from cochlearmodel_gb300.pipeline import JNDWindow
+        from oracle import oracle as orc
+        self.orc = orc
+        self.batch = batch
+        self.Fs, self.overlap_time, self.block_target = Fs, overlap_time, block_target
+        self.specs = batch.jnd_sweep_spec(n_seeds=n_seeds)
+        f = np.float32
+        md = orc.model_setup()
+        self.secp = np.stack([f(1.0) / md["M"].astype(f), f(1.0) / md["diag_m"].astype(f),
+                              md["R"].astype(f), md["S"].astype(f), md["Q"].astype(f),
+                              md["S_ohc"].astype(f), md["S_tm"].astype(f),
+                              md["R_tm"].astype(f)]).astype(f)
+        self.scal = md["scal"]
+        self.gamma = batch.hearing_loss_ohc()[None]
+        self.nerve = ihc.NerveConfig()
+        self.dmg = ihc.ihc_damage(batch.hearing_loss_ihc()).astype(np.float64)
+        self.ac = ihc.design_ac_lowpass().astype(np.float64)
+        self.dc = self.nerve.dc_taps(Fs).astype(np.float64)
+        self.win = JNDWindow()
+        self.ihc = ihc
+        self.n_groups = len(self.specs)
+        self.group_audio = []
+        self.units_total = 0
+        for sp in self.specs:
+            N, D = batch.block_nodes_for(sp["length"], block_target, Fs)
+            n_int = len(sp["sweep"].powers) + 1
+            self.group_audio.append(n_int * N * D / Fs)
+            self.units_total += n_int * D
+        self.audio_seconds = float(sum(self.group_audio))
+
+    def scalars(self, cfg):
+        orc = self.orc
+        s = orc.OrcScalars()
+        F32 = np.float32
+        for name, i in (("w_ohc", 0), ("delta_x", 1), ("alpha_r", 2), ("alpha_l", 3),
+                        ("alpha_s", 4), ("Gme", 5), ("a0", 6), ("a1", 7), ("a2", 8),
+                        ("sigma_ow", 9), ("eta_1", 10), ("eta_2", 11)):
+            setattr(s, name, float(F32(self.scal[i])))
+        s.time_step, s.time_step_out = float(cfg.time_step()), float(cfg.time_step_out())
+        s.Ts = float(cfg.Ts())
+        s.dt_min, s.dt_max = float(F32(cfg.cuda_min_time_step)), float(F32(cfg.cuda_max_time_step))
+        s.jacobi_fast, s.jacobi_slow, s.max_outer = 2, 20, 10
+        s.red_lanes, s.jacobi_mode, s.max_substeps_per_sample = 32, 0, 1 << 20
+        s.learned_every = 1
+        return s
+
+    def step(self, gi: int, cores: int) -> float:
+        """One bounded sample: group gi's noise-only reference interval and its
+        first m tested intervals, m the fewest that give every host thread a
+        BM block (at most the group's 10).  Input generation, BM (threads
+        across blocks), IHC/lambda and the JNDs of the m intervals; returns
+        the audio seconds simulated."""
+        from cochlearmodel_gb300.model import RunConfig
+        from cochlearmodel_gb300.pipeline import ProfileSweep
+        orc = self.orc
+        sp = self.specs[gi]
+        full = sp["sweep"]
+        N, D = self.batch.block_nodes_for(sp["length"], self.block_target, self.Fs)
+        m = max(1, min(len(full.powers), -(-cores // D) - 1))
+        sweep = ProfileSweep(frequencies=full.frequencies, powers=list(full.powers[:m]),
+                             noises=full.noises, calculate_jnd=True)
+        prof, _, ref_of = sweep.build()
+        n_int, L = len(prof), N * D
+        cfg = RunConfig(Fs=self.Fs, Time_Block_Length=N / self.Fs, Decouple_Filter=D,
+                        Time_Blocks=n_int * D, Overlap_Time=self.overlap_time)
+        noise = np.zeros(L, np.float32)
+        nz = np.asarray(sp["noise"], np.float32)[:L]
+        noise[:len(nz)] = nz
+        p1 = cfg.total_time_nodes_p1()
+        rows = p1 + 4
+        # input generation (CudaGenerateInputFromProfile restated)
+        pt = np.stack([prof["dA"], prof["Wn"], prof["frequency"]], 1)
+        x = np.zeros(rows, np.float32)
+        x[:n_int * L] = orc.input_gen(pt, noise, L, 0, float(self.Fs), 0.0, 1.0, 1.0).ravel()
+        # BM over the reference block partition
+        st, of, en = orc.block_partition(cfg.Time_Blocks, p1, cfg.calc_overlap_nodes(), D)
+        units = np.zeros(cfg.Time_Blocks, orc.UNIT_DTYPE)
+        units["start"], units["out_first"], units["end"] = st, of, en
+        units["mtt"], units["mmspt"] = np.float32(1e-10), np.float32(1e-15)
+        v, _, _ = orc.bm_run(self.secp, self.gamma, self.scalars(cfg), units, x, rows,
+                             threads=cores)
+        # IHC / lambda in the reference's mixed precision
+        fr = self.ihc.reference_frame(cfg)[0]
+        nv = self.nerve
+        _, lam = orc.ihc_lambda(v[:int(fr["rows"])], int(fr["seg"]), int(fr["frdp"]),
+                                int(fr["total"]), int(fr["lam_rows"]), self.ac, self.dc,
+                                nv.scale, nv.eta_AC, nv.eta_DC, self.dmg, nv.aihc(),
+                                np.asarray(nv.spontRate, np.float32), nv.Lambda_SAT, mode=0)
+        # JND Fisher sums in the reference's float arithmetic, then dB
+        head, length = self.win.nodes(self.Fs, L)
+        ra, ai = orc.jnd(lam, n_int, L, head, length, prof["dA"], ref_of, nv.nihc(),
+                         np.asarray(nv.W, np.float32), float(self.Fs), 0.2 * self.Fs,
+                         fp64=False)
+        for k in range(n_int):
+            if ref_of[k] != k:
+                orc.jnd_db(ra[:, k].sum())
+                orc.jnd_db(ai[:, k].sum())
+        return n_int * L / self.Fs
+
+
+def ref_cpu_timed(ref, steps, warmup, cores):
+    """Times `steps` bounded sample steps of the CPU sweep after `warmup`
+    (RefSweepCPU.step), the groups taken in turn.  Returns (audio-s/s, mean
+    step ms, description)."""
+    t_sum = a_sum = 0.0
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        audio = ref.step(i % ref.n_groups, cores)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            t_sum += dt
+            a_sum += audio
+    value = a_sum / t_sum
+    desc = (f"{steps} steps, each one JND-sweep group's noise-only reference interval and "
+            f"its first tested intervals (enough for a BM block per thread), groups in "
+            f"turn ({a_sum:.3f} audio-s in all): input generation, BM (FP32, reference "
+            f"schedule), IHC/lambda (reference mixed precision), JND (reference float "
+            f"arithmetic); {cores} threads, {t_sum:.1f} s")
+    return value, t_sum / steps * 1000.0, desc
+
+
 # ----------------------------------------------------------------------------
 # plain single-signal arm (the same kernels, one signal per launch)
 # ----------------------------------------------------------------------------
@@ -328,36 +467,34 @@ def plain_single_signal(run, device, n_sample=12):
 # arms
 # ----------------------------------------------------------------------------
 def run_reference(args, rank, world):
-    """The path's CPU restatement on the host cores.  The sweep's input comes
-    from the GPU input kernel when a GPU is present; the timed work is CPU only."""
+    """The path on the host cores through the oracle only (RefSweepCPU): the
+    reference ships no runnable CPU path of its own.  Rank 0 alone runs it."""
     if rank != 0:
         return None
-    import torch
-    if not torch.cuda.is_available():
-        return {"impl": "reference", "unavailable": "needs the generated input of the sweep"}
-    if args.workload == "mixed_batch":
-        return {"impl": "reference", "unavailable": "the host-core arm times the default "
-                                                    "workload (jnd_sweep) and tone_sweep"}
-    run = make_workload(args.workload, "cuda:0", args.n_freq, args.n_seeds)
-    run.generate_input()
-    torch.cuda.synchronize()
-    vals = []
-    for i in range(args.warmup + args.steps):
-        v, cores, sample = cpu_sample(run, target_s=args.cpu_seconds / max(1, args.steps))
-        if i >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
+    if args.workload != "jnd_sweep":
+        return {"impl": "reference", "unavailable": "the host-core arm is built for the "
+                                                    "default workload (jnd_sweep)"}
+    cores = os.cpu_count() or 1
+    ref = RefSweepCPU(n_seeds=args.n_seeds)
+    value, ms, desc = ref_cpu_timed(ref, args.steps, args.warmup, cores)
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": run.audio_seconds / value * 1000.0, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": run.kind, "signals": n_signals(run),
-                       "units": len(run.units), "audio_s_per_step": run.audio_seconds,
-                       "sample": "bounded"},
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": base_config("jnd_sweep", 66 * args.n_seeds, ref.units_total,
+                                  ref.audio_seconds, args.jacobi),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+
+
+def base_config(kind, signals, units, audio, jacobi):
+    """The workload description both arms print (the GPU arm adds its details)."""
+    return {"workload": kind, "signals": signals, "units": units, "audio_s_per_step": audio,
+            "fs": 100000,
+            "bm_semantics": "kernel 17, reference schedule (20/2 Jacobi sweeps)"
+            if jacobi == "reference" else f"tolerance mode 1e-6, {jacobi} guess"}
 
 
 def run_ours(args, rank, world, device):
@@ -462,14 +599,14 @@ def run_ours(args, rank, world, device):
         "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1000.0,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": run.kind, "signals": n_signals(run), "units": len(run.units),
-                   "audio_s_per_step": run.audio_seconds, "fs": 100000,
-                   "l2": "flushed between timed steps (256 MB write)",
-                   "path": " -> ".join(nm for nm, _ in stages(run)),
-                   "bm_semantics": "reference (20/2 Jacobi sweeps)" if args.jacobi == "reference"
-                   else f"tolerance mode 1e-6, {args.jacobi} guess",
-                   "cuda_graph": use_graph, "launch_shape": args.shape,
-                   "stage_ms": stage_ms},
+        "config": base_config(run.kind, n_signals(run), len(run.units), run.audio_seconds,
+                              args.jacobi),
+        "details": {"l2": "flushed between timed steps (256 MB write)",
+                    "path": " -> ".join(nm for nm, _ in stages(run)),
+                    "cuda_graph": use_graph, "launch_shape": args.shape, "stage_ms": stage_ms,
+                    "value_is": "the batched solver with the reference's fixed Jacobi "
+                                "schedule; the learned warm start is measured in 'learned'"
+                    if args.jacobi == "reference" else f"--jacobi {args.jacobi}"},
         "gpu_launches": int(per_step_launches * args.steps),
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(sum(t.numel() * t.element_size() for t in h_tables)),
@@ -484,7 +621,55 @@ def run_ours(args, rank, world, device):
     if plain is not None:
         line["plain_single_signal"] = plain
         line["speedup_vs_plain"] = value / plain["value"]
+    if rank == 0 and run.kind == "jnd_sweep" and args.jacobi == "reference" and not args.no_learned:
+        line["learned"] = learned_record(device, run.mv)
     return line, run
+
+
+def learned_record(device, mv, n_groups=3):
+    """The learned warm start measured in the same run: the first n_groups
+    groups of the JND sweep, batched, with the reference's fixed Jacobi
+    schedule and with the tolerance-mode solve started from the network's
+    guess; audio-s/s of the whole path, Jacobi sweeps per time step, and the
+    learned velocity's max-rel from the fixed schedule's (max |a-b| / max |b|
+    over each signal's rows, worst signal)."""
+    import torch
+    from cochlearmodel_gb300 import batch, model, native, warmstart
+    spec = batch.jnd_sweep_spec(n_seeds=4)[:n_groups]
+    out = {}
+    runs = {}
+    for name in ("reference_schedule", "learned"):
+        b = batch.BatchSweep(device, spec, mv=mv)
+        if name == "learned":
+            b.sc = model.tolerance_mode(b.sc, guess=2)
+            net = warmstart.WarmStartNet.load(warmstart.WEIGHTS, device)
+            b.extras = net.extras()
+        b.step()
+        torch.cuda.synchronize(device)
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        b.step()
+        e.record()
+        torch.cuda.synchronize(device)
+        st = b.d_stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
+        out[name] = {"value": b.audio_seconds / (a.elapsed_time(e) / 1000.0), "unit": UNIT,
+                     "sweeps_per_step": float(st["sweeps"].sum() / max(1, st["substeps"].sum()))}
+        runs[name] = b
+    v0 = runs["reference_schedule"].d_v.cpu().numpy()
+    v1 = runs["learned"].d_v.cpu().numpy()
+    worst = 0.0
+    for g in runs["learned"].groups:
+        n_int, L = len(g.prof), g.L
+        for k in range(n_int):
+            r = slice(g.v_row0 + k * L, g.v_row0 + (k + 1) * L)
+            den = np.abs(v0[r]).max()
+            if den > 0:
+                worst = max(worst, float(np.abs(v1[r].astype(np.float64) - v0[r]).max() / den))
+    out["learned"]["max_rel_vs_reference_schedule"] = worst
+    out["sample"] = (f"the first {n_groups} groups of the JND sweep "
+                     f"({runs['learned'].audio_seconds:.3f} audio-s), batched, one step each "
+                     f"after a warm-up step")
+    return out
 
 
 def main():
@@ -498,9 +683,13 @@ def main():
     ap.add_argument("--n-signals", type=int, default=1024, help="mixed_batch signals")
     ap.add_argument("--jacobi", default="reference", choices=list(JACOBI),
                     help="pressure solve: reference schedule or tolerance-mode guess")
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0,
+                    help="tone_sweep: seconds of the CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=4,
+                    help="jnd_sweep: sample steps of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--shape", type=int, default=0, help="BM kernel launch shape")
     ap.add_argument("--n-freq", type=int, default=64,
@@ -525,7 +714,12 @@ def main():
         torch.distributed.init_process_group("nccl", device_id=device)
     line, run = run_ours(args, rank, world, device)
     if rank == 0 and world == 1 and not args.no_cpu_baseline and run.kind != "mixed_batch":
-        v, cores, sample = cpu_sample(run, target_s=args.cpu_seconds)
+        if run.kind == "jnd_sweep":
+            cores = os.cpu_count() or 1
+            v, _, sample = ref_cpu_timed(RefSweepCPU(n_seeds=args.n_seeds), args.cpu_steps,
+                                         1, cores)
+        else:
+            v, cores, sample = cpu_sample(run, target_s=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": sample}
     if world > 1:
