@@ -200,7 +200,8 @@ class BatchSweep:
         else:
             native.check_host_mirror(h_lam, self.d_lam, "h_lam")
             native.check(self.lib.cgb_ihc_lambda_launch_mirror_dev(
-                *args, native.ptr(h_lam), self._stream(stream)),
+                *args, native.ptr(h_lam), h_lam.numel() * h_lam.element_size(),
+                self._stream(stream)),
                 "cgb_ihc_lambda_launch_mirror_dev")
 
     def jnd_sums(self, stream=None):

@@ -919,6 +919,8 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
   if ((reinterpret_cast<uintptr_t>(d_out) & 15) || (reinterpret_cast<uintptr_t>(d_secp) & 15))
     return fail(CGB_ERR_ARG, "cgb_bm_run_dev: d_out and d_secp must be 16-byte aligned");
   if (ex && ex->h_out) {
+    if (ex->h_out_bytes < out_rows * 256 * (int64_t)sizeof(float))
+      return fail(CGB_ERR_RANGE, "cgb_bm_run_dev: h_out is shorter than out_rows x 256 floats");
     const int rc = check_host_mirror(ex->h_out, "cgb_bm_run_dev: h_out");
     if (rc) return rc;
   }

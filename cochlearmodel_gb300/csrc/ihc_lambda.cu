@@ -29,6 +29,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -42,7 +43,8 @@ constexpr int kSecTile = 32;   // sections per CTA (one per lane)
 constexpr int kBoxRows = 64;   // rows per TMA box
 constexpr int kIhcWarps = 16;
 constexpr int kRB = 8;         // output rows per register block
-constexpr long long kWaitPolls = 1ll << 26;
+// bound on one staging wait, in nanoseconds of the GPU's global timer
+constexpr unsigned long long kWaitNs = 1000000000ull;
 constexpr int kTilesPerRun = 8;  // consecutive tiles per CTA (short runs)
 
 struct IHCArgs {
@@ -65,7 +67,13 @@ struct IHCArgs {
   int ac_sym;                  // AC taps symmetric: FIR over tap pairs
   int run;                     // tiles per CTA (consecutive, one frame)
   const float* ac_ext;         // AC by velocity row (the IIR path), or null: the FIR
+  int skip_first_copy;         // test-only: arm the first staging wait but issue no copy
 };
+
+// Test-only fault injection (cgb_ihc_set_fault_injection): the next launches
+// arm the first staging mbarrier without issuing its copies, so the bounded
+// wait runs out with nothing in flight and the kernel reports status bit 1.
+int g_fault_skip_copy = 0;
 
 __device__ __forceinline__ int taps_used(int k, const cgb_ihc_frame& f, int taps) {
   const int sg = k < f.frdp - 1 ? f.seg : f.total;
@@ -248,12 +256,13 @@ __device__ __forceinline__ float fir_row(const float* __restrict__ src,
 // ends all reads of X; the proxy fence orders those generic-proxy reads
 // before the asynchronous writes.
 __device__ __forceinline__ void stage_rows(const CUtensorMap* vmap, float* X, uint64_t* mbar,
-                                           int boxes, int y0, int s0) {
+                                           int boxes, int y0, int s0, bool skip = false) {
   const uint32_t bytes = (uint32_t)boxes * kBoxRows * kSecTile * 4;
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
                "r"(bytes)
                : "memory");
+  if (skip) return;  // test-only: the transaction count is never met
   for (int bxi = 0; bxi < boxes; ++bxi) {
     const int y = y0 + bxi * kBoxRows;  // may be negative or past the end: zero fill
     asm volatile(
@@ -264,18 +273,25 @@ __device__ __forceinline__ void stage_rows(const CUtensorMap* vmap, float* X, ui
   }
 }
 
-// Bounded wait on phase `parity` of mbar by every thread, then a block-wide
-// vote so that all threads take the same branch.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait on phase `parity` of mbar by every thread, for at most kWaitNs of the
+// global timer (each try_wait returns within a short system-defined time),
+// then a block-wide vote so that all threads take the same branch.
 __device__ __forceinline__ bool wait_stage(uint64_t* mbar, uint32_t parity) {
   uint32_t done = 0;
-  long long polls = 0;
-  while (!done && polls < kWaitPolls) {
+  const unsigned long long t_start = global_ns();
+  while (!done) {
     asm volatile(
         "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
         : "=r"(done)
         : "r"(smem_u32(mbar)), "r"(parity)
         : "memory");
-    ++polls;
+    if (!done && global_ns() - t_start > kWaitNs) break;
   }
   return __syncthreads_and(done) != 0;
 }
@@ -326,7 +342,8 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
   // staged rows of the first tile start one row below the oldest row either
   // filter reads; those of later tiles below the oldest row the AC filter reads
   if (threadIdx.x == 0)
-    stage_rows(&vmap, X, mbar, boxes_first, (int)f.v_row0 + t0 * A.TR - A.n_ac - A.n_dc + 1, s0);
+    stage_rows(&vmap, X, mbar, boxes_first, (int)f.v_row0 + t0 * A.TR - A.n_ac - A.n_dc + 1, s0,
+               A.skip_first_copy != 0);
 
   const float* bac = TP;
   const float* bdc = TP + A.n_ac;
@@ -580,10 +597,16 @@ int pick_run(const cgb_ihc_frame* frames, int n_frames, int TR, int n_dc) {
 }  // namespace
 }  // namespace cgb
 
-extern "C" int64_t cgb_ihc_lambda_scratch_bytes(int n_frames, int n_ac, int n_dc) {
+namespace cgb {
+// bytes of the per-call tables: frames, tile prefix, taps, each 256-aligned
+constexpr int64_t ihc_table_bytes(int n_frames, int n_taps) {
   return ((int64_t)n_frames * (int64_t)sizeof(cgb_ihc_frame) + 255) / 256 * 256 +
-         ((int64_t)(n_frames + 1) * 4 + 255) / 256 * 256 +
-         ((int64_t)(n_ac + n_dc) * 4 + 255) / 256 * 256;
+         ((int64_t)(n_frames + 1) * 4 + 255) / 256 * 256 + ((int64_t)n_taps * 4 + 255) / 256 * 256;
+}
+}  // namespace cgb
+
+extern "C" int64_t cgb_ihc_lambda_scratch_bytes(int n_frames, int n_ac, int n_dc) {
+  return cgb::ihc_table_bytes(n_frames, n_ac + n_dc);
 }
 
 namespace cgb {
@@ -600,7 +623,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
                     const float* d_aihc, float* d_lam, int64_t lam_plane_rows, float* d_ihc,
                     void* d_scratch, int64_t scratch_bytes, int32_t* d_status, void* stream,
                     int mode,
-                    const float* ac_ext = nullptr, float* lam_host = nullptr) {
+                    const float* ac_ext = nullptr, float* lam_host = nullptr,
+                    int32_t* stage_prefix = nullptr, float* stage_taps = nullptr) {
   if (n_frames == 0) return CGB_OK;
   if (!frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_scratch ||
       ((mode & kLaunch) && (!d_v || !d_dmg || !d_aihc || !d_lam || !d_status)))
@@ -617,7 +641,15 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   }
   if (v_rows > INT32_MAX)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: more than 2^31-1 velocity rows");
-  std::vector<int32_t> prefix(n_frames + 1, 0);
+  // host staging of the tile prefix and the taps: a vector, or the caller's
+  // fixed arrays (stage_prefix: n_frames + 1 entries, stage_taps: n_ac + n_dc)
+  std::vector<int32_t> prefix_v;
+  int32_t* prefix = stage_prefix;
+  if (!prefix) {
+    prefix_v.assign(n_frames + 1, 0);
+    prefix = prefix_v.data();
+  }
+  prefix[0] = 0;
   int TR = 0, xrows = 0;
   pick_tile(n_ac, n_dc, &TR, &xrows);
   if (TR < 32) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
@@ -642,16 +674,21 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   const size_t fbytes = ((size_t)n_frames * sizeof(cgb_ihc_frame) + 255) / 256 * 256;
   const size_t pbytes = ((size_t)(n_frames + 1) * 4 + 255) / 256 * 256;
   if (mode & kUpload) {
-    std::vector<float> taps(n_ac + n_dc);
+    std::vector<float> taps_v;
+    float* taps = stage_taps;
+    if (!taps) {
+      taps_v.resize(n_ac + n_dc);
+      taps = taps_v.data();
+    }
     for (int i = 0; i < n_ac; ++i) taps[i] = ac_taps[i] * prm->scale;
     for (int i = 0; i < n_dc; ++i) taps[n_ac + i] = dc_taps[i];
     CGB_TRY_CUDA(cudaMemcpyAsync(sc, frames, (size_t)n_frames * sizeof(cgb_ihc_frame),
                                  cudaMemcpyHostToDevice, st),
                  "upload frames");
-    CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes, prefix.data(), (size_t)(n_frames + 1) * 4,
+    CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes, prefix, (size_t)(n_frames + 1) * 4,
                                  cudaMemcpyHostToDevice, st),
                  "upload tile prefix");
-    CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes + pbytes, taps.data(), taps.size() * 4,
+    CGB_TRY_CUDA(cudaMemcpyAsync(sc + fbytes + pbytes, taps, (size_t)(n_ac + n_dc) * 4,
                                  cudaMemcpyHostToDevice, st),
                  "upload taps");
   }
@@ -695,6 +732,7 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   A.xrows = xrows;
   A.status = d_status;
   A.ac_ext = ac_ext;
+  A.skip_first_copy = g_fault_skip_copy;
   A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
@@ -712,6 +750,11 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
 
 }  // namespace
 }  // namespace cgb
+
+extern "C" int cgb_ihc_set_fault_injection(int skip_first_copy) {
+  cgb::g_fault_skip_copy = skip_first_copy ? 1 : 0;
+  return CGB_OK;
+}
 
 extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
                                   int n_frames, const float* ac_taps, int n_ac,
@@ -754,8 +797,11 @@ extern "C" int cgb_ihc_lambda_launch_mirror_dev(
     const float* ac_taps, int n_ac, const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
     const float* d_dmg, int n_dmg_profiles, const float* d_aihc, float* d_lam,
     int64_t lam_plane_rows, float* d_ihc, void* d_scratch, int64_t scratch_bytes,
-    int32_t* d_status, float* h_lam, void* stream) {
+    int32_t* d_status, float* h_lam, int64_t h_lam_bytes, void* stream) {
   if (!h_lam) return cgb::fail(CGB_ERR_ARG, "cgb_ihc_lambda_launch_mirror_dev: null h_lam");
+  if (h_lam_bytes < 3 * lam_plane_rows * 256 * (int64_t)sizeof(float))
+    return cgb::fail(CGB_ERR_RANGE, "cgb_ihc_lambda_launch_mirror_dev: h_lam is shorter than "
+                                    "3 x lam_plane_rows x 256 floats");
   return cgb::ihc_lambda_impl(d_v, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc, prm,
                               d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc,
                               d_scratch, scratch_bytes, d_status, stream, cgb::kLaunch, nullptr,
@@ -769,44 +815,52 @@ extern "C" int cgb_ihc_lambda_launch_mirror_dev(
 // __device__ array instead of caller scratch, for callers that cannot
 // allocate device memory: a host that hands the library only the buffers it
 // already owns, or a real-time audio thread that must not enter the device
-// allocator.  The array is 192 KiB, holds at most kNoAllocMaxFrames frames and
-// kNoAllocMaxTaps taps, and stays resident on every GPU that loads this
-// library until the process exits.  All calls share it, so calls whose GPU
-// work overlaps (different streams, or a second call enqueued before the
-// first one ran) race on its contents; serialise them on one stream.  Each
-// call rewrites every table byte it reads, so nothing needs clearing.
+// allocator (nor the host heap: the host-side staging of the prefix and taps
+// is a pair of static arrays too).  The array is 192 KiB, holds at most
+// kNoAllocMaxFrames frames and kNoAllocMaxTaps taps, and stays resident on
+// every GPU that loads this library until the process exits.  All calls
+// share it and the static staging, so calls must come from one host thread
+// at a time and calls whose GPU work overlaps (different streams, or a
+// second call enqueued before the first one ran) race on its contents;
+// serialise them on one stream.  Each call rewrites every table byte it
+// reads, so nothing needs clearing.  The tables are the same layout as the
+// caller-scratch path's (frames, then the prefix, then the taps, each
+// 256-byte aligned), sized for the maximum.
 // ---------------------------------------------------------------------------
 namespace cgb {
 namespace {
 
 constexpr int kNoAllocMaxFrames = 4096;
 constexpr int kNoAllocMaxTaps = 2048;  // n_ac + n_dc
-constexpr size_t kNoAllocFrameBytes = (size_t)kNoAllocMaxFrames * sizeof(cgb_ihc_frame);
-constexpr size_t kNoAllocPrefixOff = (kNoAllocFrameBytes + 255) / 256 * 256;
-constexpr size_t kNoAllocTapsOff =
-    kNoAllocPrefixOff + ((size_t)(kNoAllocMaxFrames + 1) * 4 + 255) / 256 * 256;
 constexpr size_t kNoAllocBytes = 192 * 1024;
-static_assert(kNoAllocTapsOff + (size_t)kNoAllocMaxTaps * 4 <= kNoAllocBytes,
+static_assert((size_t)ihc_table_bytes(kNoAllocMaxFrames, kNoAllocMaxTaps) <= kNoAllocBytes,
               "no-allocation scratch too small");
 
 __device__ __align__(256) unsigned char g_ihc_noalloc_scratch[kNoAllocBytes];
 
+// host staging of the tile prefix and the taps (no heap use per call)
+int32_t g_noalloc_prefix[kNoAllocMaxFrames + 1];
+float g_noalloc_taps[kNoAllocMaxTaps];
+
 constexpr int kMaxDevices = 64;
-void* g_noalloc_ptr[kMaxDevices] = {};
+std::atomic<void*> g_noalloc_ptr[kMaxDevices] = {};
 
 // Device address of the array on the current device, looked up once per
 // device (the host-side symbol is only a stand-in, not a device address).
+// Concurrent first calls may both look it up; they store the same address.
+// The cache is not cleared by cudaDeviceReset: after a reset, a process that
+// calls this entry point again must be a new process.
 int noalloc_scratch(void** out) {
   int dev = 0;
   CGB_TRY_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: device index beyond 63");
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
+  void* p = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
     CGB_TRY_CUDA(cudaGetSymbolAddress(&p, g_ihc_noalloc_scratch), "cudaGetSymbolAddress");
-    g_noalloc_ptr[dev] = p;
+    g_noalloc_ptr[dev].store(p, std::memory_order_release);
   }
-  *out = g_noalloc_ptr[dev];
+  *out = p;
   return CGB_OK;
 }
 
@@ -823,105 +877,18 @@ extern "C" int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows,
                                           int32_t* d_status, void* stream) {
   using namespace cgb;
   if (n_frames == 0) return CGB_OK;
-  if (!d_v || !frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_dmg || !d_aihc ||
-      !d_lam || !d_status)
-    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_noalloc_dev: null pointer argument");
   if (n_frames > kNoAllocMaxFrames)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: more than 4096 frames (the fixed "
                                "scratch holds at most 4096)");
   if (n_ac < 1 || n_dc < 1 || n_ac > 1024 || n_dc > 1024 || n_ac + n_dc > kNoAllocMaxTaps)
     return fail(CGB_ERR_RANGE,
                 "cgb_ihc_lambda_noalloc_dev: filter lengths must be in [1, 1024]");
-  if (reinterpret_cast<uintptr_t>(d_v) & 15)
-    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_noalloc_dev: d_v must be 16-byte aligned");
-  if (v_rows > INT32_MAX)
-    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: more than 2^31-1 velocity rows");
-  int TR = 0, xrows = 0;
-  pick_tile(n_ac, n_dc, &TR, &xrows);
-  if (TR < 32)
-    return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: filters too long for one tile");
-  const int run = pick_run(frames, n_frames, TR, n_dc);
-  int32_t prefix[kNoAllocMaxFrames + 1];
-  prefix[0] = 0;
-  for (int i = 0; i < n_frames; ++i) {
-    const cgb_ihc_frame& fr = frames[i];
-    const bool ok = fr.v_row0 >= 0 && fr.lam_rows >= 0 && fr.lam_rows <= fr.rows &&
-                    fr.v_row0 + fr.rows <= v_rows && fr.lam_row0 >= 0 &&
-                    fr.lam_row0 + fr.lam_rows <= lam_plane_rows && fr.seg > 0 && fr.frdp > 0 &&
-                    fr.total > 0 && fr.ihc_profile >= 0 && fr.ihc_profile < n_dmg_profiles;
-    if (!ok)
-      return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_noalloc_dev: frame " + std::to_string(i) +
-                                     " out of range");
-    const int tiles = (fr.lam_rows + TR - 1) / TR;
-    prefix[i + 1] = prefix[i] + (tiles + run - 1) / run;
-  }
-  const int n_tiles = prefix[n_frames];
-  if (n_tiles == 0) return CGB_OK;
   void* scratch = nullptr;
   if (int st = noalloc_scratch(&scratch)) return st;
-  unsigned char* sc = static_cast<unsigned char*>(scratch);
-  float taps[kNoAllocMaxTaps];
-  for (int i = 0; i < n_ac; ++i) taps[i] = ac_taps[i] * prm->scale;
-  for (int i = 0; i < n_dc; ++i) taps[n_ac + i] = dc_taps[i];
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  CGB_TRY_CUDA(cudaMemcpyAsync(sc, frames, (size_t)n_frames * sizeof(cgb_ihc_frame),
-                               cudaMemcpyHostToDevice, st),
-               "upload frames");
-  CGB_TRY_CUDA(cudaMemcpyAsync(sc + kNoAllocPrefixOff, prefix, (size_t)(n_frames + 1) * 4,
-                               cudaMemcpyHostToDevice, st),
-               "upload tile prefix");
-  CGB_TRY_CUDA(cudaMemcpyAsync(sc + kNoAllocTapsOff, taps, (size_t)(n_ac + n_dc) * 4,
-                               cudaMemcpyHostToDevice, st),
-               "upload taps");
-  auto encode = get_encode();
-  if (!encode) return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  CUtensorMap map;
-  cuuint64_t dims[2] = {256, (cuuint64_t)v_rows};
-  cuuint64_t strides[1] = {256 * 4};
-  cuuint32_t box[2] = {(cuuint32_t)kSecTile, (cuuint32_t)kBoxRows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(d_v), dims,
-                       strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (cr != CUDA_SUCCESS)
-    return fail(CGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)cr) + ")");
-  IHCArgs A{};
-  A.frames = reinterpret_cast<const cgb_ihc_frame*>(sc);
-  A.tile_prefix = reinterpret_cast<const int32_t*>(sc + kNoAllocPrefixOff);
-  A.n_frames = n_frames;
-  A.taps = reinterpret_cast<const float*>(sc + kNoAllocTapsOff);
-  A.n_ac = n_ac;
-  A.n_dc = n_dc;
-  A.scale = prm->scale;
-  A.eta_ac = prm->eta_ac;
-  A.eta_dc = prm->eta_dc;
-  A.sat = prm->lambda_sat;
-  A.spont0 = prm->spont[0];
-  A.spont1 = prm->spont[1];
-  A.spont2 = prm->spont[2];
-  A.dmg = d_dmg;
-  A.aihc = d_aihc;
-  A.lam = d_lam;
-  A.lam_plane_rows = lam_plane_rows;
-  A.ihc = d_ihc;
-  A.TR = TR;
-  A.xrows = xrows;
-  A.status = d_status;
-  A.ac_ext = nullptr;
-  A.run = run;
-  A.dc_uniform = 1;
-  for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
-  A.ac_sym = ac_symmetric(ac_taps, n_ac, prm->scale);
-  const size_t smem = smem_bytes(TR, xrows, n_ac, n_dc);
-  CGB_TRY_CUDA(cudaFuncSetAttribute(ihc_lambda_kernel,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-               "cudaFuncSetAttribute(ihc smem)");
-  dim3 grid((unsigned)n_tiles, 256 / kSecTile);
-  ihc_lambda_kernel<<<grid, kIhcWarps * 32, smem, st>>>(map, A);
-  CGB_TRY_CUDA(cudaGetLastError(), "ihc_lambda_kernel launch");
-  note_launch();
-  return CGB_OK;
+  return ihc_lambda_impl(d_v, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc, prm,
+                         d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc, scratch,
+                         (int64_t)kNoAllocBytes, d_status, stream, kUpload | kLaunch, nullptr,
+                         nullptr, g_noalloc_prefix, g_noalloc_taps);
 }
 
 // ---------------------------------------------------------------------------

@@ -245,7 +245,10 @@ int main(int argc, char** argv) {
                              (int)P.num("Normalize_Sigma_Type_Signal", 3), 0.16, 0.0, 0, 0, 0, 0,
                              n_int, false, 0, n_int, overlap, L, 0, L, (float)Fs, 0, nullptr,
                              false, true, (float)P.num("MAX_M1_SP_ERROR", 1e-15),
-                             (float)P.num("MAX_TOLERANCE", 1e-10), 0, 0.0f, 0.0f, D, 0,
+                             (float)P.num("MAX_TOLERANCE", 1e-10),
+                             (int)P.num("RELATIVE_ERRORS", 0),
+                             (float)P.num("M1_SP_Fix_Factor", 0.0),
+                             (float)P.num("Tolerance_Fix_Factor", 0.0), D, 0,
                              ha_fir.data(), (int)ha_fir.size(), ha_iir.data(),
                              (int)ha_iir.size(), log);
 
@@ -262,7 +265,9 @@ int main(int argc, char** argv) {
                    (float)sc[5], (float)sc[6], (float)sc[7], (float)sc[8], (float)sc[9],
                    (float)sc[10], (float)sc[11], &tres, TB, (int)samples_p1, overlap, ov_us, 1,
                    1e-6f, 1e-18f, D, (float)P.num("MAX_M1_SP_ERROR", 1e-15),
-                   (float)P.num("MAX_TOLERANCE", 1e-10), 0, 0, 0.0f, 0.0f, (float)spl_ref, 0, 0,
+                   (float)P.num("MAX_TOLERANCE", 1e-10), (int)P.num("RELATIVE_ERRORS", 0), 0,
+                   (float)P.num("M1_SP_Fix_Factor", 0.0),
+                   (float)P.num("Tolerance_Fix_Factor", 0.0), (float)spl_ref, 0, 0,
                    0, (int)P.num("JACOBBY_Loops_Fast", 2), (int)P.num("JACOBBY_Loops_Slow", 20),
                    (int)P.num("Cuda_Outern_Loops", 10),
                    // kernel selection and cache hint, with the reference's
@@ -300,6 +305,9 @@ int main(int argc, char** argv) {
                  (int)(samples_p1 + 4), N, 0, 0, 500.0f, 1.0f, 100.0f, true, true, false, true,
                  false, false, 1.0f, calc_jnd, n_int, overlap, D, 0, log);
     allocateBuffer(LAMBDA_COUNT * calc_time * 256, 0, e0, e1, prop);
+    // harness-only test key (not a reference key): make the IHC kernel's
+    // staging wait run out, to exercise the drop-in's error path
+    if (P.num("Test_Fault_IHC_Staging", 0) != 0) cgb_ihc_set_fault_injection(1);
     RunIHCKernel(nullptr, 0, 1, -1, 0, log);
     std::vector<float> lam((size_t)LAMBDA_COUNT * calc_time * 256);
     BMOHCKernel_Copy_Lambda(lam.data(), lam.size(), 0);

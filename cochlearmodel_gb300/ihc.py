@@ -242,7 +242,8 @@ class IHCStage:
         else:
             native.check_host_mirror(h_lam, lam, "h_lam")
             native.check(self.lib.cgb_ihc_lambda_launch_mirror_dev(
-                *args, native.ptr(h_lam), C.c_void_p(stream.cuda_stream)),
+                *args, native.ptr(h_lam), h_lam.numel() * h_lam.element_size(),
+                C.c_void_p(stream.cuda_stream)),
                 "cgb_ihc_lambda_launch_mirror_dev")
 
     def run_iir(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, b, a,

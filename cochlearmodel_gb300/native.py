@@ -67,7 +67,8 @@ _SIGS = {
     "cgb_ihc_lambda_launch_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _i64,
                                        _p, _p, _i64, _p, _p]),
     "cgb_ihc_lambda_launch_mirror_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p,
-                                              _p, _i64, _p, _p, _i64, _p, _p, _p]),
+                                              _p, _i64, _p, _p, _i64, _p, _p, _i64, _p]),
+    "cgb_ihc_set_fault_injection": (_i, [_i]),
     "cgb_ihc_lambda_noalloc_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p,
                                         _i64, _p, _p, _p]),
     "cgb_input_gen_dev": (_i, [_p, _i, _p, _p, _i, _i, _i, C.c_float, _d, _d, _d, _d, _p, _p]),
@@ -113,7 +114,7 @@ class BMExtras(C.Structure):
     mirror of the velocity output (fields left at zero are unused)."""
     _fields_ = [("d_ws_blob", C.c_void_p), ("d_log", C.c_void_p), ("log_cap", C.c_int64),
                 ("log_every", C.c_int32), ("pad_", C.c_int32), ("d_log_count", C.c_void_p),
-                ("h_out", C.c_void_p)]
+                ("h_out_bytes", C.c_int64), ("h_out", C.c_void_p)]
 
 
 def lib_path() -> Path:

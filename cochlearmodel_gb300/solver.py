@@ -95,6 +95,7 @@ class BMSolver:
             if extras is not None:
                 C.memmove(C.addressof(ex), C.addressof(extras), C.sizeof(ex))
             ex.h_out = h_out.data_ptr()
+            ex.h_out_bytes = h_out.numel() * h_out.element_size()
             extras = ex
         native.check(self.lib.cgb_bm_run_ex_dev(
             native.ptr(self.secp), native.ptr(gamma), int(gamma.shape[0]), C.byref(sc),

@@ -113,6 +113,8 @@ typedef struct cgb_bm_extras {
   int32_t log_every;      /* record every n-th step start of each unit       */
   int32_t pad_;
   int32_t* d_log_count;   /* records claimed (may exceed log_cap)            */
+  int64_t h_out_bytes;    /* size of h_out in bytes; at least out_rows * 256 * 4
+                             when h_out is set (checked before the launch)  */
   float* h_out;           /* host mirror of d_out, or NULL: pinned host memory
                              mapped at the same address on the device, 16-byte
                              aligned, out_rows x 256 floats.  The kernel stores
@@ -276,8 +278,10 @@ int cgb_ihc_lambda_launch_dev(const float* d_v, int64_t v_rows, const cgb_ihc_fr
                               int64_t scratch_bytes, int32_t* d_status, void* stream);
 /* cgb_ihc_lambda_launch_dev with a host mirror of d_lam: h_lam is pinned host
  * memory mapped at the same address on the device (16-byte aligned, the
- * layout of d_lam).  The kernel stores every lambda value there too, so the
- * three planes reach the host while the stage runs, with no copy after it. */
+ * layout of d_lam), h_lam_bytes long, at least 3 * lam_plane_rows * 256 * 4
+ * (CGB_ERR_RANGE otherwise).  The kernel stores every lambda value there
+ * too, so the three planes reach the host while the stage runs, with no copy
+ * after it. */
 int cgb_ihc_lambda_launch_mirror_dev(const float* d_v, int64_t v_rows,
                                      const cgb_ihc_frame* frames, int n_frames,
                                      const float* ac_taps, int n_ac, const float* dc_taps,
@@ -285,6 +289,7 @@ int cgb_ihc_lambda_launch_mirror_dev(const float* d_v, int64_t v_rows,
                                      int n_dmg_profiles, const float* d_aihc, float* d_lam,
                                      int64_t lam_plane_rows, float* d_ihc, void* d_scratch,
                                      int64_t scratch_bytes, int32_t* d_status, float* h_lam,
+                                     int64_t h_lam_bytes,
                                      void* stream);
 
 /* IHC + lambda with the AC stage by IIR (the reference's is_ac_iir_filter
@@ -308,18 +313,30 @@ int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame
                            void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
                            void* stream);
 
+/* Test-only fault injection for the IHC/lambda kernel's bounded staging
+ * wait -- no counterpart in the reference.  With skip_first_copy = 1, later
+ * launches arm each CTA's first staging mbarrier but issue none of its copies,
+ * so the wait runs out after about one second with no copy in flight and the
+ * kernel sets bit 1 of *d_status; 0 restores normal launches. */
+int cgb_ihc_set_fault_injection(int skip_first_copy);
+
 /* IHC + lambda without any device allocation -- no counterpart in the
  * reference.  For callers that cannot allocate device memory (a host that
  * gives the library only buffers it already owns, a real-time audio thread
- * that must not enter the device allocator): the same computation as
- * cgb_ihc_lambda_dev, but the per-call tables live in a fixed 192 KiB
- * __device__ array inside the library instead of caller scratch.  Limits:
- * at most 4096 frames and n_ac + n_dc <= 2048 taps (CGB_ERR_RANGE beyond).
- * The array stays resident on every GPU that loads the library until exit
- * and is shared by all calls: calls whose GPU work overlaps race on it, so
- * serialise them on one stream.  The first call on a device looks the array's
- * device address up (cudaGetSymbolAddress); make that first call before any
- * stream capture. */
+ * that must not enter the device allocator or the host heap): the same
+ * computation as cgb_ihc_lambda_dev, but the per-call tables live in a fixed
+ * 192 KiB __device__ array inside the library instead of caller scratch, and
+ * their host-side staging in static arrays (no stack or heap use per call).
+ * Limits: at most 4096 frames and n_ac + n_dc <= 2048 taps (CGB_ERR_RANGE
+ * beyond).  The array stays resident on every GPU that loads the library
+ * until exit and is shared by all calls: call from one host thread at a
+ * time, and serialise the calls on one stream (calls whose GPU work
+ * overlaps race on the array).  Each call copies its frame table from
+ * `frames` with cudaMemcpyAsync on `stream`: a pinned `frames` buffer must
+ * stay valid until the stream has run that copy.  The first call on a device
+ * looks the array's device address up (cudaGetSymbolAddress) and keeps it
+ * for the process (not refreshed after cudaDeviceReset); make that first
+ * call before any stream capture. */
 int cgb_ihc_lambda_noalloc_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
                                int n_frames, const float* ac_taps, int n_ac,
                                const float* dc_taps, int n_dc, const cgb_ihc_params* prm,

@@ -113,13 +113,17 @@ def test_host_mirror_rejects_bad_buffers(sweep):
         b.ihc_lambda(h_lam=torch.empty(b.d_lam.shape, dtype=torch.float32))
     lib = native.load()
     pageable = np.zeros((b.d_v.shape[0], 256), np.float32)
-    for bad in (pageable.ctypes.data, b.d_v.data_ptr()):
+    full = b.d_v.numel() * 4
+    pinned = torch.empty(b.d_v.shape, dtype=torch.float32).pin_memory()
+    for bad, nbytes, msg in ((pageable.ctypes.data, full, b"host mirror"),
+                             (b.d_v.data_ptr(), full, b"host mirror"),
+                             (pinned.data_ptr(), full - 4, b"shorter")):
         ex = native.BMExtras()
-        ex.h_out = bad
+        ex.h_out, ex.h_out_bytes = bad, nbytes
         rc = lib.cgb_bm_run_ex_dev(
             native.ptr(b.bm.secp), native.ptr(b.d_gamma), 1, C.byref(b.sc), native.ptr(b.d_units),
             len(b.units), native.ptr(b.d_in), int(b.d_in.numel()), native.ptr(b.d_v),
             int(b.d_v.shape[0]), None, None, None, native.ptr(b.bm.work),
             C.cast(C.byref(ex), C.c_void_p), None)
-        assert rc == 1 and b"host mirror" in lib.cgb_last_error()
+        assert rc != 0 and msg in lib.cgb_last_error()
     torch.cuda.synchronize()

@@ -221,3 +221,68 @@ def test_unbuilt_kernel_selectors_raise(tmp_path, mv):
                              text=True, timeout=300)
         assert res.returncode != 0
         assert "Run_Fast_BM_Calculation" in res.stderr or "BMOHC_Kernel_Configuration" in res.stderr
+
+
+def test_relative_error_tolerances(tmp_path, mv):
+    """RELATIVE_ERRORS = 1: setupToleranceProfile scales each block's throw and
+    m1-sp tolerances by 10^(factor x the interval's dB SPL)
+    (src/cochlea.cu:4256-4287).  The harness's velocity equals the solver run
+    on the same input with those per-block tolerances, and differs from the
+    run with the plain constants."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cochlearmodel_gb300.solver import BMSolver
+    noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
+    (tmp_path / "ac.f32").write_bytes(ihc.design_ac_lowpass().tobytes())
+    (tmp_path / "noise.f32").write_bytes(noise.tobytes())
+    out = tmp_path / "out.bin"
+    par = tmp_path / "rel.par"
+    par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32", out=out) +
+                   "RELATIVE_ERRORS = 1\nM1_SP_Fix_Factor = 0.1\nTolerance_Fix_Factor = 0.1\n")
+    build.build()
+    res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stderr
+    v = read_out(out)[0]
+
+    cfg = model.RunConfig(Time_Block_Length=0.002, Decouple_Filter=2, Overlap_Time=0.001,
+                          OHC_Vector=np.array([0.5, 0.3, 0.1], np.float32),
+                          IHC_Vector=np.array([8.0, 6.0], np.float32))
+    sweep = ProfileSweep(frequencies=[1000.0, 3000.0], powers=[40.0, 80.0],
+                         noises=[1111.0, 30.0], calculate_jnd=True)
+    run = ProfileRun("cuda:0", cfg, sweep, noise=noise, mv=mv, ac_taps=ihc.design_ac_lowpass(),
+                     jnd=JNDWindow(head=0.001, tail=0.0005))
+    run.step()
+    torch.cuda.synchronize()
+    plain = run.d_v.cpu().numpy()[:v.shape[0]]
+    units = run.units.copy()
+    D = cfg.Decouple_Filter
+    f32 = np.float32
+    for i in range(run.n_int):
+        db = 0.0 if run.is_ref[i] else [40.0, 80.0][(i % 5) // 2]
+        units["mtt"][i * D:(i + 1) * D] = f32(f32(1e-10) * np.power(f32(10), f32(0.1) * f32(db)))
+        units["mmspt"][i * D:(i + 1) * D] = f32(f32(1e-15) * np.power(f32(10), f32(0.1) * f32(db)))
+    x = run.d_in.cpu().numpy()
+    want, _, _ = BMSolver("cuda:0", mv).run(run.sc, cfg.gamma()[None], units, x, run.rows)
+    assert np.array_equal(v.view(np.uint32), want[:v.shape[0]].view(np.uint32))
+    assert not np.array_equal(v, plain)
+
+
+def test_ihc_staging_timeout_raises_in_the_drop_in(tmp_path, mv):
+    """The drop-in's RunIHCKernel turns the IHC kernel's timed-out staging
+    wait (made to run out by the harness's test key) into std::runtime_error."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
+    (tmp_path / "ac.f32").write_bytes(ihc.design_ac_lowpass().tobytes())
+    (tmp_path / "noise.f32").write_bytes(noise.tobytes())
+    par = tmp_path / "fault.par"
+    par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
+                              out=tmp_path / "o.bin") + "Test_Fault_IHC_Staging = 1\n")
+    build.build()
+    res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode != 0
+    assert "IHC staging copy timed out" in res.stderr

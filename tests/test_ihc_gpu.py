@@ -157,3 +157,26 @@ def test_iir_ac_frames_with_rule_switch(stage):
         lam0 += frames[i]["lam_rows"]
     b, a = ihc.design_ac_iir_lowpass(order=2)
     _check_iir(stage, v, frames, lam0, b, a)
+
+
+def test_staging_wait_runs_out_and_reports(stage):
+    """Failure detection without a GPU fault: with the test-only injection on,
+    each CTA arms its first staging wait but issues no copy, so the wait runs
+    out after about one second (nothing in flight) and the kernel reports
+    status bit 1, which the host turns into an error.  The context stays
+    usable: the next launch without injection gives the normal result."""
+    from cochlearmodel_gb300 import native
+    lib = native.load()
+    rng = np.random.default_rng(4)
+    v = (1e-3 * rng.standard_normal((600, 256))).astype(np.float32)
+    frames = np.zeros(1, ihc.FRAME_DTYPE)
+    frames[0] = (0, 0, 600, 600, 600, 600, ihc.round64(600), 0)
+    want, _ = stage.run(v, frames, 600)
+    native.check(lib.cgb_ihc_set_fault_injection(1), "fault injection")
+    try:
+        with pytest.raises(native.CGBError, match="did not complete"):
+            stage.run(v, frames, 600)
+    finally:
+        native.check(lib.cgb_ihc_set_fault_injection(0), "fault injection")
+    again, _ = stage.run(v, frames, 600)
+    assert np.array_equal(again.view(np.uint32), want.view(np.uint32))
