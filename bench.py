@@ -503,7 +503,13 @@ def run_ours(args, rank, world, device):
 
     run = make_workload(args.workload, device, args.n_freq, args.n_seeds, args.n_signals)
     set_jacobi(run, args.jacobi, device)
-    native.check(native.load().cgb_bm_set_launch_shape(args.shape), "launch shape")
+    tuning = None
+    if args.tune != "off" and hasattr(run, "tune") and args.jacobi == "reference":
+        choice, source = run.tune(use_cache=args.tune == "cache")
+        tuning = {"bm_shape": choice.bm_shape, "ihc_run": choice.ihc_run, "source": source}
+        args.shape = choice.bm_shape
+    else:
+        native.check(native.load().cgb_bm_set_launch_shape(args.shape), "launch shape")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
 
@@ -604,6 +610,7 @@ def run_ours(args, rank, world, device):
         "details": {"l2": "flushed between timed steps (256 MB write)",
                     "path": " -> ".join(nm for nm, _ in stages(run)),
                     "cuda_graph": use_graph, "launch_shape": args.shape, "stage_ms": stage_ms,
+                    "autotune": tuning,
                     "value_is": "the batched solver with the reference's fixed Jacobi "
                                 "schedule; the learned warm start is measured in 'learned'"
                     if args.jacobi == "reference" else f"--jacobi {args.jacobi}"},
@@ -691,7 +698,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
-    ap.add_argument("--shape", type=int, default=0, help="BM kernel launch shape")
+    ap.add_argument("--shape", type=int, default=0, help="BM kernel launch shape (--tune off)")
+    ap.add_argument("--tune", default="cache", choices=["cache", "search", "off"],
+                    help="launch choices: cached autotuner result (searched when absent), "
+                         "a fresh search, or --shape with the automatic IHC run length")
     ap.add_argument("--n-freq", type=int, default=64,
                     help="tone_sweep: tones per level (64 = configuration 2)")
     ap.add_argument("--n-seeds", type=int, default=4,

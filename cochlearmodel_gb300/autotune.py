@@ -1,0 +1,192 @@
+"""Autotuner for the launch choices that change speed but not results.
+
+The reference hand-picks occupancy variants of its BM kernel
+(TripleAggKernelLauncher<Occ>, include/cochlea.cuh:187-1011, dispatched at
+src/cochlea.cu:1258-1435).  This module searches the equivalent choices of
+this library on the workload and GPU at hand, and caches the winner:
+
+- the BM launch shape (cgb_bm_set_launch_shape: warps per CTA, register bound,
+  previous-step state in registers or shared memory);
+- the IHC/lambda run length (cgb_ihc_set_run_length: consecutive tiles per CTA).
+
+Every candidate gives the same results bit for bit (the search checks it); the
+tile rows of the IHC kernel are fixed by the filters (the largest tile that fits
+shared memory and holds the DC look-back), and the JND kernel's row groups set
+its FP64 summation order, so neither is searched.
+
+The cache is a JSON file (CGB_TUNE_CACHE, default cochlearmodel_gb300/_tune/
+tuning.json) keyed by the device name, a hash of the library and a description
+of the workload.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+from dataclasses import asdict, dataclass
+from pathlib import Path
+from typing import Callable, Sequence
+
+from . import build, native
+
+IHC_RUNS = (0, 8, 16, 32)  # 0: the automatic rule
+
+
+@dataclass
+class Choice:
+    bm_shape: int = 0
+    ihc_run: int = 0
+
+
+def cache_path() -> Path:
+    env = os.environ.get("CGB_TUNE_CACHE")
+    return Path(env) if env else Path(__file__).resolve().parent / "_tune" / "tuning.json"
+
+
+def library_hash() -> str:
+    """First 16 hex digits of the SHA-256 of the built library."""
+    h = hashlib.sha256()
+    with open(build.lib_path(), "rb") as f:
+        for chunk in iter(lambda: f.read(1 << 20), b""):
+            h.update(chunk)
+    return h.hexdigest()[:16]
+
+
+def cache_key(device_name: str, workload: str, lib_hash: str | None = None) -> str:
+    return f"{device_name}|{lib_hash or library_hash()}|{workload}"
+
+
+def load_cache(path: Path | None = None) -> dict:
+    p = path or cache_path()
+    if not p.exists():
+        return {}
+    try:
+        return json.loads(p.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def store(key: str, choice: Choice, timings: dict, path: Path | None = None) -> None:
+    p = path or cache_path()
+    p.parent.mkdir(parents=True, exist_ok=True)
+    data = load_cache(p)
+    data[key] = {"choice": asdict(choice), "timings_ms": timings}
+    tmp = p.with_suffix(".tmp")
+    tmp.write_text(json.dumps(data, indent=1, sort_keys=True))
+    os.replace(tmp, p)
+
+
+def lookup(key: str, path: Path | None = None) -> Choice | None:
+    e = load_cache(path).get(key)
+    return Choice(**e["choice"]) if e else None
+
+
+def pick(timings: dict) -> object:
+    """The candidate with the smallest time (ties: the first listed)."""
+    best, best_t = None, None
+    for cand, t in timings.items():
+        if best_t is None or t < best_t:
+            best, best_t = cand, t
+    return best
+
+
+def apply(choice: Choice) -> None:
+    lib = native.load()
+    native.check(lib.cgb_bm_set_launch_shape(choice.bm_shape), "cgb_bm_set_launch_shape")
+    native.check(lib.cgb_ihc_set_run_length(choice.ihc_run), "cgb_ihc_set_run_length")
+
+
+def search(stage_bm: Callable[[], None], stage_ihc: Callable[[], None],
+           timer: Callable[[Callable[[], None]], float], outputs: Callable[[], tuple],
+           shapes: Sequence[int] | None = None, runs: Sequence[int] = IHC_RUNS,
+           prepare_bm: Callable[[], None] = lambda: None,
+           prepare_ihc: Callable[[], None] = lambda: None):
+    """Times every candidate of each stage (timer(fn) -> ms) and checks that its
+    outputs (outputs() -> (velocity bytes, lambda bytes)) equal the first
+    candidate's.  prepare_bm / prepare_ihc run after a candidate is set and
+    before it is timed: they must clear the stage's outputs (so that a
+    candidate that leaves rows unwritten is caught) and re-upload anything the
+    setting applies to.  Returns (Choice, timings)."""
+    lib = native.load()
+    shapes = list(range(lib.cgb_bm_launch_shape_count())) if shapes is None else list(shapes)
+    timings = {"bm_shape": {}, "ihc_run": {}}
+    ref = None
+    for sh in shapes:
+        native.check(lib.cgb_bm_set_launch_shape(sh), "cgb_bm_set_launch_shape")
+        prepare_bm()
+        timings["bm_shape"][sh] = timer(stage_bm)
+        v = outputs()[0]
+        if ref is None:
+            ref = v
+        elif v != ref:
+            raise native.CGBError(f"BM launch shape {sh} changed the velocity")
+    best_shape = pick(timings["bm_shape"])
+    native.check(lib.cgb_bm_set_launch_shape(best_shape), "cgb_bm_set_launch_shape")
+    stage_bm()
+    ref = None
+    for r in runs:
+        native.check(lib.cgb_ihc_set_run_length(r), "cgb_ihc_set_run_length")
+        prepare_ihc()
+        timings["ihc_run"][r] = timer(stage_ihc)
+        lam = outputs()[1]
+        if ref is None:
+            ref = lam
+        elif lam != ref:
+            raise native.CGBError(f"IHC run length {r} changed lambda")
+    choice = Choice(bm_shape=int(best_shape), ihc_run=int(pick(timings["ihc_run"])))
+    apply(choice)
+    prepare_ihc()
+    return choice, {k: {str(c): t for c, t in v.items()} for k, v in timings.items()}
+
+
+def tune_sweep(run, device, reps: int = 2, use_cache: bool = True):
+    """Tunes a BatchSweep or ProfileRun on `device` (or takes the cached
+    choice) and applies it; returns (Choice, source) with source 'cache' or
+    'search'."""
+    import torch
+    name = torch.cuda.get_device_name(device)
+    workload = (f"{type(run).__name__}:units={len(run.units)}:"
+                f"frames={len(run.frames)}:lam_rows={int(run.d_lam.shape[1])}")
+    key = cache_key(name, workload)
+    if use_cache:
+        hit = lookup(key)
+        if hit is not None:
+            apply(hit)
+            if hasattr(run, "upload_ihc_tables"):
+                run.upload_ihc_tables()
+            return hit, "cache"
+    stream = torch.cuda.current_stream(device)
+    if hasattr(run, "generate_input"):
+        run.generate_input()
+
+    def timer(fn):
+        fn()
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    def outputs():
+        torch.cuda.synchronize(device)
+        return (run.d_v.cpu().numpy().tobytes(), run.d_lam.cpu().numpy().tobytes())
+
+    def prepare_bm():
+        run.d_v.fill_(float("nan"))
+
+    def prepare_ihc():
+        if hasattr(run, "upload_ihc_tables"):
+            run.upload_ihc_tables()
+        run.d_lam.fill_(float("nan"))
+
+    choice, timings = search(run.solve_bm, run.ihc_lambda, timer, outputs,
+                             prepare_bm=prepare_bm, prepare_ihc=prepare_ihc)
+    run.solve_bm()
+    run.ihc_lambda()
+    store(key, choice, timings)
+    return choice, "search"

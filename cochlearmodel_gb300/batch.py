@@ -128,12 +128,7 @@ class BatchSweep:
                                    dtype=torch.uint8, device=d)
         self.d_lam = torch.zeros((3, self.lam_rows, 256), dtype=torch.float32, device=d)
         self.ihc = IHCStage(d, self.nerve, ihc_vec[None], ac_taps, Fs)
-        sc = self.ihc.scratch(len(self.frames))
-        native.check(self.lib.cgb_ihc_lambda_upload_dev(
-            native.ptr(self.frames), len(self.frames), native.ptr(self.ihc.ac), len(self.ihc.ac),
-            native.ptr(self.ihc.dc), len(self.ihc.dc), C.byref(self.ihc.prm), self.v_rows,
-            self.lam_rows, 1, native.ptr(sc), int(sc.numel()), self._stream(None)),
-            "cgb_ihc_lambda_upload_dev")
+        self.upload_ihc_tables()
         self.W = np.asarray(self.nerve.W, np.float32)
         self.d_nihc = torch.from_numpy(self.nerve.nihc()).to(d)
         self.per_group = []
@@ -169,6 +164,22 @@ class BatchSweep:
     def _stream(self, stream):
         s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
         return C.c_void_p(s.cuda_stream)
+
+    def upload_ihc_tables(self, stream=None):
+        """Uploads the IHC/lambda per-call tables (frames, tile prefix, taps) for
+        ihc_lambda(); again after a change of the IHC run length."""
+        sc = self.ihc.scratch(len(self.frames))
+        native.check(self.lib.cgb_ihc_lambda_upload_dev(
+            native.ptr(self.frames), len(self.frames), native.ptr(self.ihc.ac), len(self.ihc.ac),
+            native.ptr(self.ihc.dc), len(self.ihc.dc), C.byref(self.ihc.prm), self.v_rows,
+            self.lam_rows, 1, native.ptr(sc), int(sc.numel()), self._stream(stream)),
+            "cgb_ihc_lambda_upload_dev")
+
+    def tune(self, use_cache: bool = True):
+        """Applies the autotuner's launch choices for this sweep on this GPU
+        (cached, or searched and cached); returns (Choice, 'cache'|'search')."""
+        from . import autotune
+        return autotune.tune_sweep(self, self.device, use_cache=use_cache)
 
     def generate_input(self, stream=None):
         for g, pg in zip(self.groups, self.per_group):

@@ -31,6 +31,8 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <mutex>
+#include <unordered_map>
 #include <vector>
 
 #include "cgb_device.cuh"
@@ -576,8 +578,18 @@ int ac_symmetric(const float* ac_taps, int n_ac, float scale) {
 // else 8.  Runs need TR >= n_dc (the look-back is inherited in place).  The
 // choice depends only on the frame table and the device, so the upload and
 // the launch of one table agree.
+// Tiles per run forced by cgb_ihc_set_run_length (the autotuner), 0: the rule below.
+int g_forced_run = 0;
+
+// The run length each scratch buffer's tables were uploaded with: the tile
+// prefix on the device depends on it, so a launch of uploaded tables must use
+// the same run length whatever the setting is by then.
+std::mutex g_upload_run_mu;
+std::unordered_map<const void*, int> g_upload_run;
+
 int pick_run(const cgb_ihc_frame* frames, int n_frames, int TR, int n_dc) {
   if (TR < n_dc) return 1;
+  if (g_forced_run > 0) return g_forced_run;
   int dev = 0, n_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
@@ -653,7 +665,16 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   int TR = 0, xrows = 0;
   pick_tile(n_ac, n_dc, &TR, &xrows);
   if (TR < 32) return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: filters too long for one tile");
-  const int run = pick_run(frames, n_frames, TR, n_dc);
+  int run = pick_run(frames, n_frames, TR, n_dc);
+  {
+    std::lock_guard<std::mutex> lock(g_upload_run_mu);
+    if (mode & kUpload) {
+      g_upload_run[d_scratch] = run;
+    } else {
+      const auto it = g_upload_run.find(d_scratch);
+      if (it != g_upload_run.end()) run = it->second;
+    }
+  }
   for (int i = 0; i < n_frames; ++i) {
     const cgb_ihc_frame& fr = frames[i];
     const bool ok = fr.v_row0 >= 0 && fr.lam_rows >= 0 && fr.lam_rows <= fr.rows &&
@@ -750,6 +771,13 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
 
 }  // namespace
 }  // namespace cgb
+
+extern "C" int cgb_ihc_set_run_length(int tiles) {
+  if (tiles < 0 || tiles > 64)
+    return cgb::fail(CGB_ERR_ARG, "cgb_ihc_set_run_length: tiles must be 0 (automatic) or 1-64");
+  cgb::g_forced_run = tiles;
+  return CGB_OK;
+}
 
 extern "C" int cgb_ihc_set_fault_injection(int skip_first_copy) {
   cgb::g_fault_skip_copy = skip_first_copy ? 1 : 0;

@@ -69,6 +69,7 @@ _SIGS = {
     "cgb_ihc_lambda_launch_mirror_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p,
                                               _p, _i64, _p, _p, _i64, _p, _p, _i64, _p]),
     "cgb_ihc_set_fault_injection": (_i, [_i]),
+    "cgb_ihc_set_run_length": (_i, [_i]),
     "cgb_ihc_lambda_noalloc_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p,
                                         _i64, _p, _p, _p]),
     "cgb_input_gen_dev": (_i, [_p, _i, _p, _p, _i, _i, _i, C.c_float, _d, _d, _d, _d, _p, _p]),

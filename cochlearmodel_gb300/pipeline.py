@@ -203,6 +203,12 @@ class ProfileRun:
         s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
         return C.c_void_p(s.cuda_stream)
 
+    def tune(self, use_cache: bool = True):
+        """Applies the autotuner's launch choices for this run on this GPU
+        (cached, or searched and cached); returns (Choice, 'cache'|'search')."""
+        from . import autotune
+        return autotune.tune_sweep(self, self.device, use_cache=use_cache)
+
     def generate_input(self, stream=None):
         native.check(self.lib.cgb_input_gen_dev(
             native.ptr(self.d_prof), self.n_int, native.ptr(self.d_wn), None, 0, self.L, 0,

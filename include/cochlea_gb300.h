@@ -313,6 +313,15 @@ int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame
                            void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
                            void* stream);
 
+/* Tiles each IHC/lambda CTA walks in a run (the DC look-back is recomputed
+ * once per run): 0 restores the automatic choice (32 or 16 tiles while at
+ * least two CTAs per SM remain, else 8); 1-64 forces that run length.  It
+ * takes effect at the next upload of the per-call tables (cgb_ihc_lambda_dev,
+ * _upload_dev, _noalloc_dev): a launch of tables uploaded earlier keeps the
+ * run length they were uploaded with.  Every choice gives the same results
+ * bit for bit; the autotuner times them. */
+int cgb_ihc_set_run_length(int tiles);
+
 /* Test-only fault injection for the IHC/lambda kernel's bounded staging
  * wait -- no counterpart in the reference.  With skip_first_copy = 1, later
  * launches arm each CTA's first staging mbarrier but issue none of its copies,
