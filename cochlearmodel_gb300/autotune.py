@@ -190,3 +190,69 @@ def tune_sweep(run, device, reps: int = 2, use_cache: bool = True):
     run.ihc_lambda()
     store(key, choice, timings)
     return choice, "search"
+
+
+def occupancy_profile(run, shapes: Sequence[int], prefixes: Sequence[int], reps: int = 3):
+    """BM stage time (ms, best of reps) of the first n units of `run`'s unit
+    table (longest first) for each launch shape and n in `prefixes`.  With
+    n below one wave the time is that of the longest units at n / (SMs x 4)
+    warps per scheduler, so the table separates per-warp speed, throughput
+    per scheduler and the last wave's fill."""
+    import torch
+    lib = native.load()
+    dev = run.d_v.device
+    stream = torch.cuda.current_stream(dev)
+    if hasattr(run, "generate_input"):
+        run.generate_input()
+
+    def solve(n):
+        run.bm.run_dev(run.sc, run.d_gamma, run.d_units, n, run.d_in, run.d_v, run.d_failed,
+                       run.d_stats, stream, extras=getattr(run, "extras", None))
+
+    out = {}
+    try:
+        for sh in shapes:
+            native.check(lib.cgb_bm_set_launch_shape(sh), "cgb_bm_set_launch_shape")
+            row = {}
+            for n in prefixes:
+                n = min(int(n), len(run.units))
+                solve(n)
+                best = None
+                for _ in range(reps):
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    solve(n)
+                    b.record(stream)
+                    torch.cuda.synchronize(dev)
+                    ms = a.elapsed_time(b)
+                    best = ms if best is None else min(best, ms)
+                row[n] = best
+            out[sh] = row
+    finally:
+        native.check(lib.cgb_bm_set_launch_shape(0), "cgb_bm_set_launch_shape")
+    solve(len(run.units))  # the per-unit statistics of the whole table
+    stats = run.d_stats.cpu().numpy().view(native.STATS_DTYPE).reshape(-1)
+    return out, stats
+
+
+def _main(argv=None) -> None:
+    import argparse
+    import json as _json
+    ap = argparse.ArgumentParser(description="BM launch-shape occupancy profile on the JND sweep")
+    ap.add_argument("--shapes", default="0,3")
+    ap.add_argument("--prefixes", default="152,608,912,1216,1824,2432,100000")
+    ap.add_argument("--n-seeds", type=int, default=4)
+    a = ap.parse_args(argv)
+    from . import batch
+    run = batch.BatchSweep("cuda:0", batch.jnd_sweep_spec(n_seeds=a.n_seeds))
+    prof, stats = occupancy_profile(run, [int(s) for s in a.shapes.split(",")],
+                                    [int(n) for n in a.prefixes.split(",")])
+    ss = stats["substeps"]
+    print(_json.dumps({"units": len(run.units), "substeps_total": int(ss.sum()),
+                       "substeps_longest": int(ss.max()),
+                       "ms": {str(k): {str(n): t for n, t in v.items()} for k, v in prof.items()}}))
+
+
+if __name__ == "__main__":
+    _main()

@@ -256,10 +256,6 @@ __device__ __forceinline__ float ref_tree_sum(const float2 (&t)[4]) {
 // reference's BMOHC_NEW_kernel (ARITH 1) evaluates.  CTL and ARITH: see the
 // head of this file.
 //
-// HALO 4 (TOL 0, ARITH 0): the 20-sweep solve runs as five groups of four
-// sweeps, each from one shuffle round with a four-section halo, instead of
-// ten pairs with a two-section halo.
-//
 // TOL 0: fixed sweep counts (the reference schedule).  TOL 1: tolerance
 // mode; each solve sweeps in pairs until max|p2 - p1| <= jtol * max|p2|
 // (jcap sweeps at most), and the first solve of a step starts from the
@@ -268,7 +264,7 @@ __device__ __forceinline__ float ref_tree_sum(const float2 (&t)[4]) {
 // network's correction of the extrapolation every learn_every-th step.
 // hist: two 256-float slots per warp holding the pressure at the start of
 // the last two steps; ws_scratch / wblob: inference scratch and weights.
-template <bool PREV_SMEM, int TOL, int CTL, int ARITH, int HALO>
+template <bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
                                          const float* __restrict__ sp,
                                          const float* __restrict__ sg,
@@ -282,12 +278,6 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   load8q(sp + 1 * 256 + qb, rm);
   // 1/m of the halo sections 8l-1 and 8l+8 (used by the paired sweeps)
   float2 rmh = f2(__shfl_up_sync(kFull, rm[0].y, 1), __shfl_down_sync(kFull, rm[0].x, 1));
-  // HALO 4: 1/m of the halo sections (8l-2, 8l+9) and (8l-3, 8l+10)
-  float2 rmh1 = f2b(0.0f), rmh2 = f2b(0.0f);
-  if (HALO == 4) {
-    rmh1 = f2(__shfl_up_sync(kFull, rm[1].y, 1), __shfl_down_sync(kFull, rm[1].x, 1));
-    rmh2 = f2(__shfl_up_sync(kFull, rm[2].y, 1), __shfl_down_sync(kFull, rm[2].x, 1));
-  }
   // Boundary sections without per-sweep fix-ups (reference schedule and
   // tolerance mode with the previous or extrapolated guess).  There the
   // pressure of section 255 is +0 at every point: Y_255 = 0 and its update
@@ -404,9 +394,10 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       w = __fmaf_rn(__fadd_rn(wd0, wd), hdt, w0);
       wd = __fmaf_rn(__fadd_rn(wdd0, wdd), hdt, wd0);
       // The velocity-error sum (ARITH 1: in the reference's tree order) and,
-      // for CTL 0, the summed margin.  The whole-warp reductions are issued here, where nothing waits on
-      // them, so their shuffle latency overlaps the TM update and the sweeps
-      // (the tester runs only when reset == 0, a warp-uniform condition).
+      // for CTL 0, the summed margin.  The whole-warp reductions are issued
+      // here, where nothing waits on them, so their shuffle latency overlaps
+      // the TM update and the sweeps (the tester runs only when reset == 0,
+      // a warp-uniform condition).
       float ev = 0.0f, Fsum = 0.0f;
       bool faulty = false;
       if (__all_sync(kFull, reset == 0)) {
@@ -596,45 +587,6 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
 #pragma unroll
           for (int k = 0; k < 4; ++k) p[k] = mul2(sub2(Yrm[k], T[k]), rm[k]);
         }
-      } else if (!TOL && J == 20 && HALO == 4) {
-        // Four sweeps per shuffle round.  Halo pair k holds sections
-        // (8l-1-k, 8l+8+k); after sweep i the halo pairs 0..3-i are current.
-        // Each halo value is the neighbour's own update of that section (the
-        // same operands, addition commutes), except where the neighbour is
-        // across the wrap: lane 0's left halo and lane 31's right halo are
-        // finite stand-ins that reach only sections -1 and 255, whose
-        // coefficient is 0 (the argument of the pair path above).
-        const float2 Yrmh1 = f2(__shfl_sync(kFull, Yrm[1].y, src_l),
-                                __shfl_down_sync(kFull, Yrm[1].x, 1));
-        const float2 Yrmh2 = f2(__shfl_sync(kFull, Yrm[2].y, src_l),
-                                __shfl_down_sync(kFull, Yrm[2].x, 1));
-        auto own = [&](const float2 (&src)[4], float2 h, float2 (&dst)[4]) {
-          float2 T[4];
-          T[0] = add2(h, src[1]);
-          T[1] = fma2(lo1, src[2], src[0]);
-          T[2] = add2(src[1], src[3]);
-          T[3] = f2(__fadd_rn(src[2].x, src[3].y), __fadd_rn(src[2].y, src[3].x));
-#pragma unroll
-          for (int k = 0; k < 4; ++k) dst[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
-        };
-#pragma unroll 1
-        for (int r = 0; r < 5; ++r) {
-          float2 h[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            h[k] = f2(__shfl_sync(kFull, p[k].y, src_l), __shfl_down_sync(kFull, p[k].x, 1));
-          float2 g0 = fma2(neg2(add2(p[0], h[1])), rmh, Yrmh);
-          float2 g1 = fma2(neg2(add2(h[0], h[2])), rmh1, Yrmh1);
-          const float2 g2 = fma2(neg2(add2(h[1], h[3])), rmh2, Yrmh2);
-          own(p, h[0], q);                                           // sweep 1
-          const float2 e0 = fma2(neg2(add2(q[0], g1)), rmh, Yrmh);
-          const float2 e1 = fma2(neg2(add2(g0, g2)), rmh1, Yrmh1);
-          own(q, g0, p);                                             // sweep 2
-          g0 = fma2(neg2(add2(p[0], e1)), rmh, Yrmh);
-          own(p, e0, q);                                             // sweep 3
-          own(q, g0, p);                                             // sweep 4
-        }
-        it = 20;
       } else if (!TOL && J == 20) {
         // the reference schedule's slow count, fully unrolled
 #pragma unroll
@@ -815,7 +767,7 @@ constexpr int bm_dyn_smem() {
                         (TOL == 2 ? ws::kBlobBytes + WARPS * ws::kWarpScratch : 0);
 }
 
-template <int WARPS, bool PREV_SMEM, int TOL, int CTL, int ARITH, int HALO>
+template <int WARPS, bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __device__ __forceinline__ void bm_body(const BMArgs& A) {
   __shared__ __align__(16) float s_par[8 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
@@ -857,16 +809,16 @@ __device__ __forceinline__ void bm_body(const BMArgs& A) {
       s_gam[warp][1][q] = __fmul_rn(gm, s_par[5 * 256 + q]);
     }
     __syncwarp();
-    run_unit<PREV_SMEM, TOL, CTL, ARITH, HALO>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
+    run_unit<PREV_SMEM, TOL, CTL, ARITH>(A, un, s_par, s_gam[warp][0], s_gam[warp][1],
                              PREV_SMEM ? s_prev[warp] : nullptr, hist, scratch, wblob, lane,
                              A.stats ? A.stats + uid : nullptr);
     __syncwarp();
   }
 }
 
-template <int WARPS, int MINB, bool PREV_SMEM, int TOL, int CTL, int ARITH, int HALO>
+template <int WARPS, int MINB, bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __global__ void __launch_bounds__(WARPS * 32, MINB) bm_warp_kernel(const BMArgs A) {
-  bm_body<WARPS, PREV_SMEM, TOL, CTL, ARITH, HALO>(A);
+  bm_body<WARPS, PREV_SMEM, TOL, CTL, ARITH>(A);
 }
 
 // Launch shapes built: (warps per CTA, minimum resident CTAs per SM the
@@ -882,23 +834,20 @@ struct LaunchShape {
   int warps;
 };
 
-template <int W, int M, bool PS, int TOL, int CTL, int ARITH, int HALO>
+template <int W, int M, bool PS, int TOL, int CTL, int ARITH>
 void launch_shape(unsigned grid, cudaStream_t st, const BMArgs& A) {
-  bm_warp_kernel<W, M, PS, TOL, CTL, ARITH, HALO>
-      <<<grid, W * 32, bm_dyn_smem<W, TOL>(), st>>>(A);
+  bm_warp_kernel<W, M, PS, TOL, CTL, ARITH><<<grid, W * 32, bm_dyn_smem<W, TOL>(), st>>>(A);
 }
 
-#define CGB_SHAPE_H(W, M, PS, TOL, CTL, ARITH, HALO)                                  \
-  {reinterpret_cast<const void*>(bm_warp_kernel<W, M, PS, TOL, CTL, ARITH, HALO>),       \
-   launch_shape<W, M, PS, TOL, CTL, ARITH, HALO>, bm_dyn_smem<W, TOL>(), W}
-#define CGB_SHAPE(W, M, PS, TOL, CTL, ARITH) CGB_SHAPE_H(W, M, PS, TOL, CTL, ARITH, 2)
+#define CGB_SHAPE(W, M, PS, TOL, CTL, ARITH)                                        \
+  {reinterpret_cast<const void*>(bm_warp_kernel<W, M, PS, TOL, CTL, ARITH>),           \
+   launch_shape<W, M, PS, TOL, CTL, ARITH>, bm_dyn_smem<W, TOL>(), W}
 
 const LaunchShape kShapes[] = {
     CGB_SHAPE(4, 1, false, 0, 0, 0),
     CGB_SHAPE(4, 3, false, 0, 0, 0),
     CGB_SHAPE(4, 1, true, 0, 0, 0),
     CGB_SHAPE(4, 3, true, 0, 0, 0),
-    CGB_SHAPE_H(4, 1, false, 0, 0, 0, 4),
 };
 // Tolerance-mode kernels: plain / extrapolated guess, and the learned guess.
 const LaunchShape kTolShape = CGB_SHAPE(4, 1, false, 1, 0, 0);

@@ -77,6 +77,9 @@ def load():
                                            _p, C.c_int, _p, C.c_int, C.c_double, C.c_double,
                                            C.c_double, _p, _p, _p, C.c_double, _p, _p, C.c_int64,
                                            C.c_int, _p]
+        lib.orc_ihc_lambda_ac.argtypes = [_p, _p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          _p, C.c_int, C.c_double, C.c_double, C.c_double, _p,
+                                          _p, _p, C.c_double, _p, _p, C.c_int64, C.c_int]
         lib.orc_hearing_aid.argtypes = [_p, C.c_int, C.c_int, _p, C.c_int, _p, C.c_int, _p]
         lib.orc_ws_param_count.restype = C.c_int
         lib.orc_ws_forward_backward.argtypes = [_p, _p, _p, C.c_int, C.c_float, C.c_int, _p, _p,
@@ -212,6 +215,26 @@ def ws_forward_backward(params, feat, target, s_out, round_bf16=True, want_grad=
     load().orc_ws_forward_backward(_ptr(params), _ptr(feat), _ptr(target), n, s_out,
                                    1 if round_bf16 else 0, _ptr(out), _ptr(loss), _ptr(grad))
     return out, float(loss[0]), grad
+
+
+def ihc_lambda_ac(v, ac, seg, frdp, total, lam_rows, dc_taps, scale, eta_ac, eta_dc,
+                  ihc_damage, aihc, spont, lambda_sat, mode=0):
+    """IHC/lambda with the AC stage given (rows x 256 floats) in place of the
+    FIR; the rest in `mode` as ihc_lambda.  Returns (ihc, lambda)."""
+    v = np.ascontiguousarray(v, np.float32)
+    ac = np.ascontiguousarray(ac, np.float32)
+    assert ac.shape == v.shape
+    rows = v.shape[0]
+    ihc = np.zeros((rows, 256), np.float32)
+    lam = np.zeros((3, lam_rows, 256), np.float32)
+    dc = np.ascontiguousarray(dc_taps, np.float64)
+    load().orc_ihc_lambda_ac(_ptr(v), _ptr(ac), rows, seg, frdp, total, lam_rows, _ptr(dc),
+                             len(dc), scale, eta_ac, eta_dc,
+                             _ptr(np.ascontiguousarray(ihc_damage, np.float64)),
+                             _ptr(np.ascontiguousarray(aihc, np.float32)),
+                             _ptr(np.ascontiguousarray(spont, np.float32)), lambda_sat,
+                             _ptr(ihc), _ptr(lam), lam_rows, mode)
+    return ihc, lam
 
 
 def ihc_lambda_iir(v, seg, frdp, total, lam_rows, b, a, dc_taps, scale, eta_ac, eta_dc,

@@ -85,3 +85,20 @@ def test_launch_keeps_the_run_length_of_its_upload(mv):
     finally:
         native.check(lib.cgb_ihc_set_run_length(0), "run length")
         b.upload_ihc_tables()
+
+
+def test_occupancy_profile_times_prefixes(mv):
+    """The occupancy profile times each launch shape on prefixes of the unit
+    table and returns the statistics of the whole table."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    spec = batch.jnd_sweep_spec(n_seeds=1, seed=5, min_ms=4.0, max_ms=8.0,
+                                noises=(1111.0, 30.0), powers=(40.0, 80.0))
+    b = batch.BatchSweep("cuda:0", spec, mv=mv, overlap_time=0.001, block_target=200,
+                         jnd=JNDWindow(head=0.0005, tail=0.0002))
+    n = len(b.units)
+    prof, stats = autotune.occupancy_profile(b, [0, 3], [1, n], reps=1)
+    assert set(prof) == {0, 3} and all(set(r) == {1, n} for r in prof.values())
+    assert all(t > 0 for r in prof.values() for t in r.values())
+    assert len(stats) == n and (stats["written_samples"] > 0).all()

@@ -1,0 +1,117 @@
+"""Why the AC FIR of the IHC stage stays on the FP32 pipe: its tensor-core
+forms miss the lambda bar (1e-4 max-rel against the reference's double FIR,
+src/cochlea.cu:2712-2730).
+
+A tensor-core FIR (tcgen05.mma kind::tf32 over a Toeplitz tile of the taps)
+is emulated here on real BM velocity, with exact products and round-to-nearest
+FP32 adds.  That is the most favourable model of the tensor core's
+accumulation: the emulated errors are lower bounds.
+- tf32: one pass, both operands in TF32 (taps rounded, velocity truncated);
+- 3xtf32: operands split as hi + lo (hi rounded to TF32, lo truncated), the
+  products lo*hi, hi*lo and hi*hi, one FP32 accumulator over all taps;
+- 3xtf32_blocks: as 3xtf32, each block of 8 taps (one MMA K step) in its own
+  FP32 accumulator, the block partials summed with TwoSum compensation.
+Everything after the AC stage runs in the reference's mixed precision (oracle
+mode 0), so the errors are the AC arithmetic's alone.  The kernel's own
+compensated FIR (Dot2, oracle mode 2) is checked on the same inputs.
+"""
+import numpy as np
+import pytest
+
+from cochlearmodel_gb300 import ihc, model
+from oracle import oracle as orc
+from tests import cases
+
+BAR = 1e-4
+
+
+def _tf32_round(x):
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x1000) & 0xFFFFE000).astype(np.uint32).view(np.float32)
+
+
+def _tf32_trunc(x):
+    return (np.ascontiguousarray(x, np.float32).view(np.uint32) & np.uint32(0xFFFFE000)).view(
+        np.float32)
+
+
+def _taps_used(rows, seg, frdp, total, n):
+    """The decoupled look-back rule of the FIR (src/cochlea.cu:2712-2730)."""
+    k = np.arange(rows)
+    sg = k // (frdp - 1)
+    sg = sg * total + (1 - sg) * seg
+    return np.minimum((k + 1) % sg, n)
+
+
+def _delayed(v, i):
+    out = np.zeros_like(v)
+    out[i:] = v[:v.shape[0] - i]
+    return out
+
+
+def _ac_tensor(v, bt, tu, kind, block=8):
+    f32 = np.float32
+    acc = np.zeros_like(v)
+    comp = np.zeros_like(v)
+    part = np.zeros_like(v)
+    bh = _tf32_round(bt)
+    bl = _tf32_trunc((bt - bh).astype(f32))
+    for i in range(len(bt)):
+        m = (tu > i)[:, None]
+        x = _delayed(v, i)
+        if kind == "tf32":
+            acc = np.where(m, (acc + (bh[i] * _tf32_trunc(x)).astype(f32)).astype(f32), acc)
+            continue
+        xh = _tf32_round(x)
+        xl = _tf32_trunc((x - xh).astype(f32))
+        tgt = part if kind == "3xtf32_blocks" else acc
+        for t in (bl[i] * xh, bh[i] * xl, bh[i] * xh):
+            tgt = np.where(m, (tgt + t.astype(f32)).astype(f32), tgt)
+        if kind == "3xtf32":
+            acc = tgt
+            continue
+        part = tgt
+        if (i + 1) % block == 0 or i == len(bt) - 1:
+            s = (acc + part).astype(f32)
+            z = (s - acc).astype(f32)
+            e = ((acc - (s - z)) + (part - z)).astype(f32)
+            acc, comp = s, (comp + e).astype(f32)
+            part = np.zeros_like(v)
+    return (acc + comp).astype(f32) if kind == "3xtf32_blocks" else acc
+
+
+def _max_rel(a, b):
+    return max(float(np.abs(a[j] - b[j]).max() / np.abs(b[j]).max()) for j in range(3))
+
+
+@pytest.mark.parametrize("freq,db", [(1000.0, 60.0), (500.0, 100.0)])
+def test_tensor_core_ac_fir_misses_the_lambda_bar(freq, db):
+    mv = model.ModelVectors.build()
+    nerve = ihc.NerveConfig()
+    ac = ihc.design_ac_lowpass().astype(np.float32)
+    bt = (ac.astype(np.float64) * nerve.scale).astype(np.float32)
+    dc = nerve.dc_taps(100000).astype(np.float64)
+    dmg = ihc.ihc_damage(np.full(256, 8.0, np.float32)).astype(np.float64)
+    aihc, spont = nerve.aihc(), np.asarray(nerve.spontRate, np.float32)
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=20.0, db=db, freq=freq)
+    v, _, _ = orc.bm_run(mv.section_params(), gamma, sc, units, x, rows)
+    fr = ihc.reference_frame(cfg)[0]
+    v = np.ascontiguousarray(v[:int(fr["rows"])])
+    seg, frdp, total, lam_rows = (int(fr[k]) for k in ("seg", "frdp", "total", "lam_rows"))
+    tail = (dc, nerve.scale, nerve.eta_AC, nerve.eta_DC, dmg, aihc, spont, nerve.Lambda_SAT)
+    fir = (v, seg, frdp, total, lam_rows, ac.astype(np.float64)) + tail
+    _, ref = orc.ihc_lambda(*fir, mode=0)
+    _, dot2 = orc.ihc_lambda(*fir, mode=2)
+    errs = {"dot2": _max_rel(dot2, ref)}
+    tu = _taps_used(v.shape[0], seg, frdp, total, len(bt))
+    for kind in ("tf32", "3xtf32", "3xtf32_blocks"):
+        a = _ac_tensor(v, bt, tu, kind)
+        _, lam = orc.ihc_lambda_ac(v, a, seg, frdp, total, lam_rows, *tail, mode=0)
+        errs[kind] = _max_rel(lam, ref)
+    print(f"{freq:.0f} Hz {db:.0f} dB lambda max-rel vs the reference: "
+          + ", ".join(f"{k} {e:.2e}" for k, e in errs.items()))
+    assert errs["dot2"] <= 1e-6
+    assert errs["tf32"] > 100 * BAR
+    assert errs["3xtf32"] > BAR
+    if (freq, db) == (1000.0, 60.0):
+        assert errs["3xtf32_blocks"] > BAR

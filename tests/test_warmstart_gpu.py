@@ -105,17 +105,45 @@ def test_forward_and_gradients_match_oracle(ws_data):
         assert rel <= 5e-3, (k, rel)
 
 
-def test_learned_guess_in_the_solver(mv, bm_solver, ws_data):
-    """The network's guess inside the BM kernel: the solve still runs to the
-    tolerance, so the velocity agrees with the extrapolated-guess run to the
-    tolerance's effect, and every step still converges."""
+@pytest.mark.parametrize("which", ["fixture", "trained"])
+def test_learned_guess_in_the_solver(mv, bm_solver, ws_data, which):
+    """The network's guess inside the BM kernel (the fixture's barely trained
+    network and the shipped weights): the solve still runs to the tolerance,
+    every step converges, and the velocity is as close to the FP64 exact solve
+    (exact tridiagonal pressure, FP64 state) as with the other guesses.
+
+    Two tolerance-mode runs are not held to 1e-4 of each other: the 1e-6
+    pressure tolerance leaves each FP32 run 1e-4 to 3e-3 from the FP64 exact
+    solve.  Measured on four seeds of this batch: previous-pressure guess
+    1.2e-4 to 3.3e-3, extrapolated 1.3e-4 to 3.3e-3, trained network 1.5e-4 to
+    1.2e-3, reference schedule 1.2e-4 to 8.2e-4.  So each run is checked
+    against FP64: with the shipped weights the learned run within 1.5x the
+    worse of the two plain guesses, and every run within 5e-3.
+
+    The stopping rule compares successive sweeps (|p2 - p1| <= tol |p2|), not
+    the residual, so a poor start can stop further from the exact pressure:
+    the fixture's network leaves 6.3e-3 on seed 5 against 3.3e-3 for the plain
+    guesses.  It is held to 1e-2."""
     W, net, rec, feat, target, nr = ws_data
+    if which == "trained":
+        net = W.WarmStartNet.load(W.WEIGHTS)
     batch = W.signal_batch(4, ms=3.0, seed=5)
+    r0 = W.evaluate(bm_solver, batch, guess=0)
     r1 = W.evaluate(bm_solver, batch, guess=1)
     r2 = W.evaluate(bm_solver, batch, guess=2, net=net)
-    assert r1["status"] == 0 and r2["status"] == 0
-    assert W.max_rel(r2["velocity"], r1["velocity"]) <= 2e-2
+    assert r0["status"] == 0 and r1["status"] == 0 and r2["status"] == 0
     assert r2["failed"].sum() <= r1["failed"].sum() + 2
+    sc = model.bm_scalars(batch.cfg, mv)
+    v64, _, _ = orc.bm_run(mv.section_params(), batch.cfg.gamma()[None], sc, batch.units,
+                           batch.inp, batch.out_rows, fp64=True, jacobi_mode=1)
+    e0, e1, e2 = (W.max_rel(r["velocity"], v64) for r in (r0, r1, r2))
+    print(f"{which} network: velocity max-rel vs the FP64 exact solve: previous {e0:.2e}, "
+          f"extrapolated {e1:.2e}, learned {e2:.2e}")
+    assert max(e0, e1) <= 5e-3
+    if which == "trained":
+        assert e2 <= 1.5 * max(e0, e1)
+    else:
+        assert e2 <= 1e-2
 
 
 def test_trained_network_gain(mv, bm_solver):
