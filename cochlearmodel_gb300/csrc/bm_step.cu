@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 
 #include "cgb_device.cuh"
@@ -66,6 +67,9 @@ struct BMArgs {
   // ARITH 1: the reference's float constants 1/Ts, 1/sigma_ow (each formed in
   // double and rounded, src/cochlea.cu:1099,1105) and time_step_out
   float fs_f, rsow, tout_f;
+  // sigma_ow is a power of two (its reciprocal rsow is exact), so x / sigma_ow
+  // is x * rsow bit for bit
+  int ow_pow2;
   int jfast, jslow, max_outer, max_sub;
   double tout, invts;
   // tolerance mode (jacobi_mode 2)
@@ -656,9 +660,10 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       if (ARITH)  // oval window: (-a1 w + -a2 w') + (Gme smp + p_0), times 1/sigma_ow
         wdd = __fmul_rn(A.rsow, __fadd_rn(__fmaf_rn(A.na2, wd, __fmul_rn(A.na1, w)),
                                           __fmaf_rn(A.gme, smp, p0)));
-      else
-        wdd = __fdiv_rn(__fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmaf_rn(A.gme, smp, p0))),
-                        A.sow);
+      else {
+        const float ws = __fmaf_rn(A.na1, w, __fmaf_rn(A.na2, wd, __fmaf_rn(A.gme, smp, p0)));
+        wdd = A.ow_pow2 ? __fmul_rn(ws, A.rsow) : __fdiv_rn(ws, A.sow);
+      }
 
       if (reset == 0) {
         const float2 m = max2(max2(da[0], da[1]), max2(da[2], da[3]));
@@ -667,12 +672,19 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         // CTL 0: the summed margin; CTL 1: any failing section
         if (CTL == 0) faulty = Fsum > 0.0f;
         const float num = __fmul_rn(ea, dt);
-        const float L = ev > mmspt ? (ARITH ? __fdividef(num, ev) : __fdiv_rn(num, ev)) : 0.0f;
+        // L = ea dt / ev (0 unless ev > mmspt).  ARITH 1 divides as the
+        // reference does; ARITH 0 tests L > 6 as num > 6 ev and L < 0.5 as
+        // num < 0.5 ev, with 6 ev rounded once (no division on the step's
+        // critical path).
+        const bool lcheck = ev > mmspt;
+        const float L = lcheck && ARITH ? __fdividef(num, ev) : 0.0f;
+        const bool l_big = ARITH ? L > 6.0f : lcheck && num > __fmul_rn(6.0f, ev);
+        const bool l_small = ARITH ? L < 0.5f : !lcheck || num < __fmul_rn(0.5f, ev);
         // Step decisions are the same in every lane (they come from warp
         // reductions and uniform counters); taking them through a vote makes
         // that visible to the compiler, which then branches without
         // reconvergence barriers.
-        if (__all_sync(kFull, L > 6.0f)) {
+        if (__all_sync(kFull, l_big)) {
           dt = __fmul_rn(dt, 0.5f);
           if (dt < A.dtmin) dt = A.dtmin;
           another = 0;
@@ -680,7 +692,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         } else if (__all_sync(kFull, faulty)) {
           another = 1;
           reset = 0;
-        } else if (__all_sync(kFull, L < 0.5f)) {
+        } else if (__all_sync(kFull, l_small)) {
           dt = __fmul_rn(dt, 2.0f);
           if (dt > A.dtmax) dt = A.dtmax;
           another = 0;
@@ -951,6 +963,13 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
                       : sc->alpha_l / sc->alpha_s;
   A.fs_f = (float)(1.0 / (double)sc->Ts);
   A.rsow = (float)(1.0 / (double)sc->sigma_ow);
+  {
+    int e = 0;
+    const double m = std::frexp((double)sc->sigma_ow, &e);
+    // a normal power of two whose reciprocal is normal too
+    A.ow_pow2 = m == 0.5 && std::fpclassify(sc->sigma_ow) == FP_NORMAL &&
+                std::fpclassify(A.rsow) == FP_NORMAL;
+  }
   A.tout_f = sc->time_step_out;
   A.nas = -sc->alpha_s;
   A.al = sc->alpha_l;

@@ -496,6 +496,8 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
         T d = y[s] - x[s];
         dp[s] = A::fma(e1, d, A::fma(e2, u[s] - v[s], nw * ps[s]));
       }
+      // (the kernels multiply by 1/sigma_ow where sigma_ow is a power of two:
+      // the same value)
       wdd = A::fma(na1, w, A::fma(na2, wd, A::fma(Gme, smp, p[0]))) / sow;
       if (reset == 0) {
         T ea = 0;
@@ -512,8 +514,21 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
         // some section fails the speed test (its fault count is positive)
         const bool faulty =
             sc.controller == 1 ? any_fault : tree_sum<T>(flt, sc.red_lanes) > (T)0;
-        T L = ev > mmspt ? (ea * dt) / ev : (T)0;
-        if (L > (T)6) {
+        // L = ea dt / ev (0 unless ev > mmspt).  In FP32 the kernels test
+        // L > 6 as ea dt > 6 ev and L < 0.5 as ea dt < 0.5 ev (6 ev rounded
+        // once); the FP64 method divides.
+        const T num = ea * dt;
+        const bool lcheck = ev > mmspt;
+        bool l_big, l_small;
+        if (std::is_same<T, float>::value) {
+          l_big = lcheck && num > (T)6 * ev;
+          l_small = !lcheck || num < (T)0.5 * ev;
+        } else {
+          const T L = lcheck ? num / ev : (T)0;
+          l_big = L > (T)6;
+          l_small = L < (T)0.5;
+        }
+        if (l_big) {
           dt = dt * (T)0.5;
           if (dt < dtmin) dt = dtmin;
           another = 0;
@@ -521,7 +536,7 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
         } else if (faulty) {
           another = 1;
           reset = 0;
-        } else if (L < (T)0.5) {
+        } else if (l_small) {
           dt = dt * (T)2;
           if (dt > dtmax) dt = dtmax;
           another = 0;

@@ -32,6 +32,18 @@ def test_cfg1_slice_bit_exact(mv, bm_solver):
     assert st["written_samples"][0] == units["end"][0] - units["out_first"][0]
 
 
+@pytest.mark.parametrize("sigma_ow", [0.25, 0.3])
+def test_oval_window_scale_bit_exact(mv, bm_solver, sigma_ow):
+    """The oval-window acceleration divides by sigma_ow; where sigma_ow is a
+    power of two the kernel multiplies by its exact reciprocal instead.  Both
+    forms are bit-exact against the oracle's division."""
+    from cochlearmodel_gb300 import native
+    cfg, sc, gamma, units, x, rows = cases.cfg1_slice(mv, ms=1.5, db=80.0)
+    s2 = native.BMScalars.from_buffer_copy(sc)
+    s2.sigma_ow = sigma_ow
+    _compare(mv, bm_solver, (cfg, s2, gamma, units, x, rows))
+
+
 @pytest.mark.parametrize("db", [20.0, 100.0])
 def test_levels_bit_exact(mv, bm_solver, db):
     _compare(mv, bm_solver, cases.cfg1_slice(mv, ms=1.5, db=db, freq=4000.0))
