@@ -22,13 +22,14 @@
 //   1  BMOHC_NEW_kernel: another iteration while ANY section has
 //      |v - v_ref| > max(mtt, v dt) (its fault count, cochlea.cuh:4080-4100).
 // Arithmetic (ARITH):
-//   0  own fixed order (explicit __fmaf_rn, own tanh and reciprocal, double
-//      simulated-time accumulator), reproduced bit for bit by the CPU oracle.
+//   0  own fixed order, reproduced bit for bit by the CPU oracle: explicit
+//      __fmaf_rn, own tanh and reciprocal, the step-size tests as products
+//      (no division).
 //   1  BMOHC_NEW_kernel's own operation order: its fmaf placement, CUDA's
 //      tanhf, __fdividef where it divides, its shared-memory tree order for
-//      the velocity-error sum, one Jacobi sweep at a time and a float time
-//      accumulator; checked bit for bit against the reference's compiled
-//      kernel.  (CUDA's tanhf gives the same bits under --fmad=false as under
+//      the velocity-error sum and one Jacobi sweep at a time; checked bit for
+//      bit against the reference's compiled kernel.
+//   Both keep simulated time in a float accumulator, as the reference does.  (CUDA's tanhf gives the same bits under --fmad=false as under
 //      the reference's default --fmad=true, checked on every float input.)
 //
 // Floating-point order is fixed: the file is compiled with --fmad=false and
@@ -64,14 +65,13 @@ struct BMArgs {
   int32_t* work;
   float ratio, nas, al, e1, e2, nw, ar, dx2, dxa0, na1, na2, gme, sow;
   float dt0, dtmin, dtmax;
-  // ARITH 1: the reference's float constants 1/Ts, 1/sigma_ow (each formed in
-  // double and rounded, src/cochlea.cu:1099,1105) and time_step_out
+  // the reference's float constants 1/Ts, 1/sigma_ow (each formed in double
+  // and rounded, src/cochlea.cu:1099,1105) and time_step_out
   float fs_f, rsow, tout_f;
   // sigma_ow is a power of two (its reciprocal rsow is exact), so x / sigma_ow
   // is x * rsow bit for bit
   int ow_pow2;
   int jfast, jslow, max_outer, max_sub;
-  double tout, invts;
   // tolerance mode (jacobi_mode 2)
   float jtol;
   int jcap, guess, learn_every;
@@ -325,8 +325,9 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
   float* cb = A.conv ? A.conv + un.out_base * 3 : nullptr;
 
   float dt = A.dt0;
-  double tau = 0.0;   // ARITH 0: simulated time since the current sample
-  float tau_f = 0.0f; // ARITH 1: the reference's float accumulator (curr_time_f)
+  // simulated time since the current sample: a float accumulator, as the
+  // reference's curr_time_f (include/cochlea.cuh:13642,14230)
+  float tau_f = 0.0f;
   int n = un.start;
   float sx0 = inb[n], sx1 = inb[n + 1];
   int fail_flag = 0;
@@ -348,9 +349,9 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
       dt_prev = dt;
       store8q(hist + (n_sub & 1) * 256 + qb, p);
     }
-    // ARITH 1: sx[9] = curr_time_f * Fs, sx[10] = 1 - sx[9]
+    // sx[9] = curr_time_f * Fs, sx[10] = 1 - sx[9]
     // (include/cochlea.cuh:3925-3927)
-    const float delta = ARITH ? __fmul_rn(tau_f, A.fs_f) : (float)(tau * A.invts);
+    const float delta = __fmul_rn(tau_f, A.fs_f);
     const float smp = __fmaf_rn(sx1, delta, __fmul_rn(sx0, __fsub_rn(1.0f, delta)));
     // (s * 0.5) * dt == s * (dt * 0.5) exactly, so each trapezoid update is
     // one fma with the half step
@@ -718,11 +719,8 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
     smp_dt = __fadd_rn(smp_dt, dt);
     smp_it = __fadd_rn(smp_it, (float)out_loop);
 
-    if (__all_sync(kFull, ARITH ? tau_f > A.tout_f : tau > A.tout)) {
-      if (ARITH)
-        tau_f = __fsub_rn(tau_f, A.tout_f);
-      else
-        tau -= A.tout;
+    if (__all_sync(kFull, tau_f > A.tout_f)) {
+      tau_f = __fsub_rn(tau_f, A.tout_f);
       sx0 = sx1;
       sx1 = inb[n + 2];
       if (__all_sync(kFull, n >= un.out_first)) {
@@ -755,10 +753,7 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
     w0 = w;
     wd0 = wd;
     wdd0 = wdd;
-    if (ARITH)
-      tau_f = __fadd_rn(tau_f, dt);
-    else
-      tau += (double)dt;
+    tau_f = __fadd_rn(tau_f, dt);
   }
   if (st && lane == 0) {
     st->substeps = n_sub;
@@ -990,8 +985,6 @@ extern "C" int cgb_bm_run_ex_dev(const float* d_secp, const float* d_gamma, int 
   A.jslow = sc->jacobi_slow;
   A.max_outer = sc->max_outer;
   A.max_sub = sc->max_substeps_per_sample;
-  A.tout = (double)sc->time_step_out;
-  A.invts = 1.0 / (double)sc->Ts;
   A.jtol = sc->jacobi_tol;
   A.jcap = sc->jacobi_cap;
   A.guess = tol ? sc->guess_mode : 0;

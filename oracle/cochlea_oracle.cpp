@@ -371,7 +371,13 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
   float smp_dt = 0.0f, smp_sub = 0.0f, smp_it = 0.0f;
 
   T dt = (T)sc.time_step;
+  // simulated time since the current sample: FP32 keeps it in a float
+  // accumulator as the kernels (and the reference's curr_time_f) do, with
+  // 1/Ts formed in double and rounded; the FP64 method in double
+  constexpr bool kF32 = std::is_same<T, float>::value;
   double tau = 0.0;
+  float tau_f = 0.0f;
+  const float fs_f = (float)(1.0 / (double)sc.Ts), tout_f = sc.time_step_out;
   int64_t n = un.start;
   // tolerance mode: pressure at the start of the last two steps, dt ratio
   T hist[2][NS] = {};
@@ -391,7 +397,7 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
       dt_prev = dt;
       for (int s = 0; s < NS; ++s) hist[S.substeps & 1][s] = p[s];
     }
-    const T delta = std::is_same<T, float>::value ? (T)(float)(tau * invTs) : (T)(tau * invTs);
+    const T delta = kF32 ? (T)(tau_f * fs_f) : (T)(tau * invTs);
     const T smp = A::fma(sx1, delta, sx0 * ((T)1 - delta));
     // (s * 0.5) * dt == s * (dt * 0.5) exactly (power-of-two scaling), so
     // each trapezoid update is one fma with the half step
@@ -561,8 +567,11 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
     smp_sub = smp_sub + 1.0f;
     smp_dt = smp_dt + (float)dt;
     smp_it = smp_it + (float)out_loop;
-    if (tau > Tout) {
-      tau -= Tout;
+    if (kF32 ? tau_f > tout_f : tau > Tout) {
+      if (kF32)
+        tau_f = tau_f - tout_f;
+      else
+        tau -= Tout;
       sx0 = sx1;
       sx1 = (T)inb[n + 2];
       if (n >= un.out_first) {
@@ -594,7 +603,10 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
     w0 = w;
     wd0 = wd;
     wdd0 = wdd;
-    tau += (double)dt;
+    if (kF32)
+      tau_f = tau_f + (float)dt;
+    else
+      tau += (double)dt;
   }
   if (st) *st = S;
 }

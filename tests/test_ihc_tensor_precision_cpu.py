@@ -1,6 +1,6 @@
 """Why the AC FIR of the IHC stage stays on the FP32 pipe: its tensor-core
 forms miss the lambda bar (1e-4 max-rel against the reference's double FIR,
-src/cochlea.cu:2712-2730).
+src/cochlea.cu:2712-2730) or sit on it.
 
 A tensor-core FIR (tcgen05.mma kind::tf32 over a Toeplitz tile of the taps)
 is emulated here on real BM velocity, with exact products and round-to-nearest
@@ -16,7 +16,6 @@ mode 0), so the errors are the AC arithmetic's alone.  The kernel's own
 compensated FIR (Dot2, oracle mode 2) is checked on the same inputs.
 """
 import numpy as np
-import pytest
 
 from cochlearmodel_gb300 import ihc, model
 from oracle import oracle as orc
@@ -84,8 +83,27 @@ def _max_rel(a, b):
     return max(float(np.abs(a[j] - b[j]).max() / np.abs(b[j]).max()) for j in range(3))
 
 
-@pytest.mark.parametrize("freq,db", [(1000.0, 60.0), (500.0, 100.0)])
-def test_tensor_core_ac_fir_misses_the_lambda_bar(freq, db):
+def test_tensor_core_ac_fir_has_no_margin_on_the_lambda_bar():
+    """Two 20 ms tones (1 kHz / 60 dB, 500 Hz / 100 dB): the one-accumulator
+    forms miss the bar, and the blocked 3xTF32 form uses at least half of it
+    under the most favourable accumulation model.  It measured 2.2e-4 at
+    1 kHz / 60 dB, and 9.4e-5 on the velocity of a trial BM operation order
+    1.4e-4 away, so 1e-4-level changes in the input move it by 2x.  Dot2 stays
+    500x inside the bar."""
+    errs = {}
+    for freq, db in [(1000.0, 60.0), (500.0, 100.0)]:
+        e = _study(freq, db)
+        print(f"{freq:.0f} Hz {db:.0f} dB lambda max-rel vs the reference: "
+              + ", ".join(f"{k} {x:.2e}" for k, x in e.items()))
+        for k, x in e.items():
+            errs[k] = max(errs.get(k, 0.0), x)
+    assert errs["dot2"] <= 1e-6
+    assert errs["tf32"] > 100 * BAR
+    assert errs["3xtf32"] > BAR
+    assert errs["3xtf32_blocks"] > 0.5 * BAR
+
+
+def _study(freq, db):
     mv = model.ModelVectors.build()
     nerve = ihc.NerveConfig()
     ac = ihc.design_ac_lowpass().astype(np.float32)
@@ -108,10 +126,4 @@ def test_tensor_core_ac_fir_misses_the_lambda_bar(freq, db):
         a = _ac_tensor(v, bt, tu, kind)
         _, lam = orc.ihc_lambda_ac(v, a, seg, frdp, total, lam_rows, *tail, mode=0)
         errs[kind] = _max_rel(lam, ref)
-    print(f"{freq:.0f} Hz {db:.0f} dB lambda max-rel vs the reference: "
-          + ", ".join(f"{k} {e:.2e}" for k, e in errs.items()))
-    assert errs["dot2"] <= 1e-6
-    assert errs["tf32"] > 100 * BAR
-    assert errs["3xtf32"] > BAR
-    if (freq, db) == (1000.0, 60.0):
-        assert errs["3xtf32_blocks"] > BAR
+    return errs
