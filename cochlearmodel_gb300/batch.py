@@ -146,7 +146,10 @@ class BatchSweep:
             for i in range(n):
                 ivs.append((r0 + i * g.L + head, r0 + int(g.ref_of[i]) * g.L + head,
                             float(g.prof["dA"][i]), length, len(ivs)))
-        self.jnd_iv = np.array(ivs, dtype=native.JND_INTERVAL_DTYPE)
+        # longest windows first (each keeps its output slot): the kernel issues
+        # the table in order, so the long intervals do not trail the launch
+        iv = np.array(ivs, dtype=native.JND_INTERVAL_DTYPE)
+        self.jnd_iv = iv[np.argsort(-iv["len"], kind="stable")]
         self.d_jnd_iv = torch.from_numpy(self.jnd_iv.view(np.uint8).copy()).to(d)
         self.d_FRA = torch.zeros((3, len(ivs)), dtype=torch.float64, device=d)
         self.d_FAI = torch.zeros((3, len(ivs)), dtype=torch.float64, device=d)

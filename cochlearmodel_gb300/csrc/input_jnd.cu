@@ -190,8 +190,9 @@ __global__ void __launch_bounds__(kJndThreads)
                      const double* __restrict__ nihc, double w0, double w1, double w2, double Fs,
                      double T, double* __restrict__ F_RA, double* __restrict__ F_AI,
                      double* __restrict__ MR) {
-  const cgb_jnd_interval d = iv[blockIdx.x];
-  const int j = blockIdx.y;
+  // CTA b: descriptor b / 3, plane b % 3 (table order, planes together)
+  const int b = (int)blockIdx.x, i = b / 3, j = b - 3 * i;
+  const cgb_jnd_interval d = iv[i];
   jnd_interval(lam, plane_rows, j, d.row, d.ref_row, d.len, d.dA, d.out, n_out, nihc,
                j == 0 ? w0 : (j == 1 ? w1 : w2), Fs, T, F_RA, F_AI, MR);
 }
@@ -283,10 +284,10 @@ extern "C" int cgb_jnd_batch_dev(const float* d_lam, int64_t plane_rows,
   if (!d_lam || !d_iv || !d_nihc || !W || !d_F_RA || !d_F_AI || n_iv < 0 || n_out <= 0 ||
       plane_rows <= 0)
     return fail(CGB_ERR_ARG, "cgb_jnd_batch_dev: bad arguments");
-  if (n_iv > 2147483647 / 2) return fail(CGB_ERR_RANGE, "cgb_jnd_batch_dev: too many intervals");
+  if (n_iv > 2147483647 / 3) return fail(CGB_ERR_RANGE, "cgb_jnd_batch_dev: too many intervals");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const double T = delta_alpha_len_factor / Fs;
-  dim3 grid((unsigned)n_iv, 3);
+  dim3 grid((unsigned)(3 * n_iv));
   jnd_batch_kernel<<<grid, kJndThreads, 0, st>>>(d_lam, plane_rows, d_iv, n_out, d_nihc,
                                                  (double)W[0], (double)W[1], (double)W[2], Fs, T,
                                                  d_F_RA, d_F_AI, d_MR);

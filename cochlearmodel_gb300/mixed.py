@@ -182,7 +182,10 @@ class MixedBatch:
             ref_row = r0 + L + head if n_int == 2 else sil_row0 + head
             self.jnd_of[i] = len(ivs)
             ivs.append((r0 + head, ref_row, s.dA, length, len(ivs)))
-        self.jnd_iv = np.array(ivs, dtype=native.JND_INTERVAL_DTYPE)
+        # longest windows first (each keeps its output slot): the kernel issues
+        # the table in order, so the long intervals do not trail the launch
+        iv = np.array(ivs, dtype=native.JND_INTERVAL_DTYPE)
+        self.jnd_iv = iv[np.argsort(-iv["len"], kind="stable")]
         self.d_jnd_iv = torch.from_numpy(self.jnd_iv.view(np.uint8).copy()).to(d)
         m = max(1, len(ivs))
         self.d_FRA = torch.zeros((3, m), dtype=torch.float64, device=d)

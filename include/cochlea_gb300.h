@@ -407,8 +407,10 @@ typedef struct cgb_jnd_interval {
 /* cgb_jnd_dev over intervals of any number of runs (signal groups of
  * different lengths) in one launch; d_iv is a device table of n_iv
  * descriptors, outputs are double[3][n_out] (MR double[3][n_out][256]).
- * Same arithmetic as cgb_jnd_dev.  No counterpart in the reference, which
- * runs one interval length per call. */
+ * Same arithmetic as cgb_jnd_dev.  The work is issued in table order, each
+ * descriptor's three lambda planes together: a table sorted by len, longest
+ * first, balances the GPU.  No counterpart in the reference, which runs one
+ * interval length per call. */
 int cgb_jnd_batch_dev(const float* d_lam, int64_t plane_rows, const cgb_jnd_interval* d_iv,
                       int n_iv, int n_out, const double* d_nihc, const float* W, double Fs,
                       double delta_alpha_len_factor, double* d_F_RA, double* d_F_AI,
