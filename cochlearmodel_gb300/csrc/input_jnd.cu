@@ -74,17 +74,33 @@ __global__ void hearing_aid_iir_kernel(const float* __restrict__ aux, float* __r
 constexpr int kJndSections = 256;
 constexpr int kJndGroups = 4;   // row groups per CTA (threads = 4 x 256)
 constexpr int kJndThreads = kJndSections * kJndGroups;
-constexpr int kJndRows = 8;     // rows folded in FP32 before an FP64 add
+constexpr int kJndRows = 8;     // rows per block of the walk
+
+// A compensated FP32 sum (Kahan summation): s - c carries the sum of the
+// added terms with an error of about 2 ulp of the total plus n eps^2 times
+// the sum of |terms|; the terms here are never negative, so that is about
+// 2 ulp of the total.
+struct KahanF {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
 
 // The Fisher sums of one (interval, lambda plane): thread (g, s) walks the
 // 8-row blocks b = g, g + 4, ... of the window of section s and of the same
-// rows of the reference window, accumulating in FP64 the sums of lambda and
-// lambda_ref (the two mean rates) and of (lambda - lambda_ref)^2 / lambda_ref
-// (the AI term); each term is formed in FP32 and 8 rows are folded in FP32
-// before the FP64 add.  Rows past the last full block are added one by one
-// by the group that owns the next block.  The four groups' sums are then
-// combined in group order and the 256 section terms reduced in FP64, so
-// the result does not depend on scheduling.
+// rows of the reference window, summing lambda and lambda_ref (the two mean
+// rates) and (lambda - lambda_ref)^2 / lambda_ref (the AI term).  Each term
+// is formed in FP32 and added to a compensated FP32 sum (KahanF), so the
+// walk needs no FP64 operation (GB300's FP64 rate would bound it).  Rows past
+// the last full block are added by the group that owns the next block.  The
+// four groups' sums are then combined in FP64 in group order and the 256
+// section terms reduced in FP64, so the result does not depend on
+// scheduling.
 __device__ __forceinline__ void jnd_interval(const float* __restrict__ lam, int64_t plane_rows,
                                              int j, int64_t row, int64_t ref_row, int len,
                                              double da, int out, int n_out,
@@ -95,36 +111,37 @@ __device__ __forceinline__ void jnd_interval(const float* __restrict__ lam, int6
   const int s = threadIdx.x & (kJndSections - 1), g = threadIdx.x / kJndSections;
   const float* c = lam + ((int64_t)j * plane_rows + row) * 256 + s;
   const float* rf = lam + ((int64_t)j * plane_rows + ref_row) * 256 + s;
-  double sum_c = 0.0, sum_r = 0.0, sum_ai = 0.0;
+  KahanF kc, kr, ka;
   const int nb = len / kJndRows;
   // two blocks per pass keep twice the loads in flight (same order of sums)
 #pragma unroll 2
   for (int b = g; b < nb; b += kJndGroups) {
     const int t = b * kJndRows;
-    float pc = 0.0f, pr = 0.0f, pa = 0.0f;
+    float lc[kJndRows], lr[kJndRows];
 #pragma unroll
     for (int k = 0; k < kJndRows; ++k) {
-      const float lc = c[(int64_t)(t + k) * 256];
-      const float lr = rf[(int64_t)(t + k) * 256];
-      const float d = __fsub_rn(lc, lr);
-      pc = __fadd_rn(pc, lc);
-      pr = __fadd_rn(pr, lr);
-      pa = __fmaf_rn(__fmul_rn(d, d), own_rcpf(lr), pa);
+      lc[k] = c[(int64_t)(t + k) * 256];
+      lr[k] = rf[(int64_t)(t + k) * 256];
     }
-    sum_c += (double)pc;
-    sum_r += (double)pr;
-    sum_ai += (double)pa;
+#pragma unroll
+    for (int k = 0; k < kJndRows; ++k) {
+      const float d = __fsub_rn(lc[k], lr[k]);
+      kc.add(lc[k]);
+      kr.add(lr[k]);
+      ka.add(__fmul_rn(__fmul_rn(d, d), own_rcpf(lr[k])));
+    }
   }
   if (g == nb % kJndGroups) {
     for (int t = nb * kJndRows; t < len; ++t) {
       const float lc = c[(int64_t)t * 256];
       const float lr = rf[(int64_t)t * 256];
       const float d = __fsub_rn(lc, lr);
-      sum_c += (double)lc;
-      sum_r += (double)lr;
-      sum_ai += (double)__fmul_rn(__fmul_rn(d, d), own_rcpf(lr));
+      kc.add(lc);
+      kr.add(lr);
+      ka.add(__fmul_rn(__fmul_rn(d, d), own_rcpf(lr)));
     }
   }
+  double sum_c = kc.value(), sum_r = kr.value(), sum_ai = ka.value();
   __shared__ double sh[3][kJndGroups][kJndSections];
   __shared__ double red[2][kJndSections / 32];
   sh[0][g][s] = sum_c;

@@ -378,7 +378,8 @@ int cgb_noise_normalization(const float* src, int normalize_type, double normali
  *   d_nihc  double[256] nerve fibres per section; W: host float[3]
  *   d_F_RA, d_F_AI  double[3][n_int] rate and all-information Fisher sums
  *   d_MR    double[3][n_int][256] mean rates over the window (may be null)
- * Time and section sums are FP64. */
+ * Time sums are compensated FP32 (Kahan) over FP32 terms; group and
+ * section sums are FP64. */
 int cgb_jnd_dev(const float* d_lam, int64_t plane_rows, int n_int, int interval_nodes, int head,
                 int len, const double* d_dA, const int32_t* d_ref_of, const double* d_nihc,
                 const float* W, double Fs, double delta_alpha_len_factor, double* d_F_RA,

@@ -10,7 +10,7 @@ from oracle import oracle as orc
 pytestmark = pytest.mark.gpu
 
 JND_DB_TOL = 0.1    # dB, final JND against the reference float arithmetic
-F_REL_FP64 = 1e-6   # Fisher sums against the FP64 oracle (FP32 terms, FP64 sums)
+F_REL_FP64 = 1e-6   # Fisher sums against the FP64 oracle (FP32 terms, compensated sums)
 
 
 @pytest.fixture(scope="module")
