@@ -413,8 +413,15 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
 
       // OHC / TM coupling, G and the right-hand side Y (scaled by 1/m).
       const bool tm_update = out_loop < 2;
+      // the G/Y section tables are loaded here, so that their shared-memory
+      // latency passes under the TM update (2% of the step against loading
+      // them next to their use)
+      float2 Rs[4], Ss[4], Qs[4];
+      load8q(sp + 2 * 256 + qb, Rs);
+      load8q(sp + 3 * 256 + qb, Ss);
+      load8q(sp + 4 * 256 + qb, Qs);
       {
-        // section tables are loaded next to their use (short live ranges)
+        // the TM tables are loaded next to their use (short live ranges)
         if (tm_update) {
           float2 Stm[4], Rtm[4], gs[4], gm[4], Ptm[4];
           load8q(sp + 6 * 256 + qb, Stm);
@@ -449,10 +456,6 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         }
         float2 Ptm[4], G[4];
         Ps.get(Ptm);
-        float2 Rs[4], Ss[4], Qs[4];
-        load8q(sp + 2 * 256 + qb, Rs);
-        load8q(sp + 3 * 256 + qb, Ss);
-        load8q(sp + 4 * 256 + qb, Qs);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           float2 g = mul2(Rs[k], fma2(f2b(A.ar), mul2(v[k], v[k]), f2b(1.0f)));
@@ -597,6 +600,10 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
 #pragma unroll
         for (int r = 0; r < 10; ++r) sweep_pair();
         it = 20;
+      } else if (!TOL && J == 2) {
+        // and its fast count, one pair without the loop
+        sweep_pair();
+        it = 2;
       } else {
 #pragma unroll 2
         for (; it + 1 < J; it += 2) {
