@@ -12,7 +12,7 @@ this library on the workload and GPU at hand, and caches the winner:
 Every candidate gives the same results bit for bit (the search checks it); the
 tile rows of the IHC kernel are fixed by the filters (the largest tile that fits
 shared memory and holds the DC look-back), and the JND kernel's row groups set
-its FP64 summation order, so neither is searched.
+its summation order, so neither is searched.
 
 The cache is a JSON file (CGB_TUNE_CACHE, default cochlearmodel_gb300/_tune/
 tuning.json) keyed by the device name, a hash of the library and a description
@@ -81,13 +81,22 @@ def lookup(key: str, path: Path | None = None) -> Choice | None:
     return Choice(**e["choice"]) if e else None
 
 
-def pick(timings: dict) -> object:
-    """The candidate with the smallest time (ties: the first listed)."""
-    best, best_t = None, None
-    for cand, t in timings.items():
-        if best_t is None or t < best_t:
+MARGIN = 0.02  # a candidate replaces the default only when this much faster
+
+
+def pick(timings: dict, margin: float = MARGIN) -> object:
+    """The candidate with the smallest time (ties: the first listed), unless
+    it beats the first listed candidate, the default, by less than `margin`
+    (a fraction of the default's time): then the default.  Stage times on a
+    shared GPU vary by a few percent from call to call, so a smaller gap is
+    not a reason to leave the default."""
+    items = list(timings.items())
+    default, t0 = items[0]
+    best, best_t = default, t0
+    for cand, t in items[1:]:
+        if t < best_t:
             best, best_t = cand, t
-    return best
+    return best if best_t < (1.0 - margin) * t0 else default
 
 
 def apply(choice: Choice) -> None:
@@ -96,50 +105,65 @@ def apply(choice: Choice) -> None:
     native.check(lib.cgb_ihc_set_run_length(choice.ihc_run), "cgb_ihc_set_run_length")
 
 
+def _rounds(stage: Callable[[], None], timer, cands, set_cand, prepare, output, what: str,
+            changed: str, rounds: int, warmup: int) -> dict:
+    """Best time of each candidate over `rounds` round-robin rounds, after
+    `warmup` untimed calls of the stage (so that the first candidate is not
+    timed while clocks and caches settle); the outputs of every candidate are
+    checked against the first's in the first round."""
+    for _ in range(warmup):
+        stage()
+    best = {c: float("inf") for c in cands}
+    ref = None
+    for r in range(rounds):
+        for c in cands:
+            set_cand(c)
+            prepare()
+            best[c] = min(best[c], timer(stage))
+            if r == 0:
+                out = output()
+                if ref is None:
+                    ref = out
+                elif out != ref:
+                    raise native.CGBError(f"{what} {c} changed the {changed}")
+    return best
+
+
 def search(stage_bm: Callable[[], None], stage_ihc: Callable[[], None],
            timer: Callable[[Callable[[], None]], float], outputs: Callable[[], tuple],
            shapes: Sequence[int] | None = None, runs: Sequence[int] = IHC_RUNS,
            prepare_bm: Callable[[], None] = lambda: None,
-           prepare_ihc: Callable[[], None] = lambda: None):
-    """Times every candidate of each stage (timer(fn) -> ms) and checks that its
-    outputs (outputs() -> (velocity bytes, lambda bytes)) equal the first
-    candidate's.  prepare_bm / prepare_ihc run after a candidate is set and
-    before it is timed: they must clear the stage's outputs (so that a
-    candidate that leaves rows unwritten is caught) and re-upload anything the
-    setting applies to.  Returns (Choice, timings)."""
+           prepare_ihc: Callable[[], None] = lambda: None, rounds: int = 3, warmup: int = 3,
+           margin: float = MARGIN):
+    """Times every candidate of each stage (timer(fn) -> ms), round-robin over
+    `rounds` rounds after `warmup` untimed calls, and checks that its outputs
+    (outputs() -> (velocity bytes, lambda bytes)) equal the first candidate's.
+    prepare_bm / prepare_ihc run after a candidate is set and before it is
+    timed: they must clear the stage's outputs (so that a candidate that leaves
+    rows unwritten is caught) and re-upload anything the setting applies to.
+    The first candidate of each list is the default, kept unless another is
+    faster by `margin` (pick).  Returns (Choice, timings)."""
     lib = native.load()
     shapes = list(range(lib.cgb_bm_launch_shape_count())) if shapes is None else list(shapes)
-    timings = {"bm_shape": {}, "ihc_run": {}}
-    ref = None
-    for sh in shapes:
-        native.check(lib.cgb_bm_set_launch_shape(sh), "cgb_bm_set_launch_shape")
-        prepare_bm()
-        timings["bm_shape"][sh] = timer(stage_bm)
-        v = outputs()[0]
-        if ref is None:
-            ref = v
-        elif v != ref:
-            raise native.CGBError(f"BM launch shape {sh} changed the velocity")
-    best_shape = pick(timings["bm_shape"])
+    timings = {}
+    timings["bm_shape"] = _rounds(
+        stage_bm, timer, shapes,
+        lambda sh: native.check(lib.cgb_bm_set_launch_shape(sh), "cgb_bm_set_launch_shape"),
+        prepare_bm, lambda: outputs()[0], "BM launch shape", "velocity", rounds, warmup)
+    best_shape = pick(timings["bm_shape"], margin)
     native.check(lib.cgb_bm_set_launch_shape(best_shape), "cgb_bm_set_launch_shape")
     stage_bm()
-    ref = None
-    for r in runs:
-        native.check(lib.cgb_ihc_set_run_length(r), "cgb_ihc_set_run_length")
-        prepare_ihc()
-        timings["ihc_run"][r] = timer(stage_ihc)
-        lam = outputs()[1]
-        if ref is None:
-            ref = lam
-        elif lam != ref:
-            raise native.CGBError(f"IHC run length {r} changed lambda")
-    choice = Choice(bm_shape=int(best_shape), ihc_run=int(pick(timings["ihc_run"])))
+    timings["ihc_run"] = _rounds(
+        stage_ihc, timer, list(runs),
+        lambda r: native.check(lib.cgb_ihc_set_run_length(r), "cgb_ihc_set_run_length"),
+        prepare_ihc, lambda: outputs()[1], "IHC run length", "lambda", rounds, warmup)
+    choice = Choice(bm_shape=int(best_shape), ihc_run=int(pick(timings["ihc_run"], margin)))
     apply(choice)
     prepare_ihc()
     return choice, {k: {str(c): t for c, t in v.items()} for k, v in timings.items()}
 
 
-def tune_sweep(run, device, reps: int = 2, use_cache: bool = True):
+def tune_sweep(run, device, rounds: int = 3, use_cache: bool = True):
     """Tunes a BatchSweep or ProfileRun on `device` (or takes the cached
     choice) and applies it; returns (Choice, source) with source 'cache' or
     'search'."""
@@ -160,17 +184,12 @@ def tune_sweep(run, device, reps: int = 2, use_cache: bool = True):
         run.generate_input()
 
     def timer(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
         fn()
-        best = None
-        for _ in range(reps):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            b.record(stream)
-            torch.cuda.synchronize(device)
-            ms = a.elapsed_time(b)
-            best = ms if best is None else min(best, ms)
-        return best
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        return a.elapsed_time(b)
 
     def outputs():
         torch.cuda.synchronize(device)
@@ -185,7 +204,7 @@ def tune_sweep(run, device, reps: int = 2, use_cache: bool = True):
         run.d_lam.fill_(float("nan"))
 
     choice, timings = search(run.solve_bm, run.ihc_lambda, timer, outputs,
-                             prepare_bm=prepare_bm, prepare_ihc=prepare_ihc)
+                             prepare_bm=prepare_bm, prepare_ihc=prepare_ihc, rounds=rounds)
     run.solve_bm()
     run.ihc_lambda()
     store(key, choice, timings)

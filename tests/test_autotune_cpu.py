@@ -55,6 +55,36 @@ def test_search_picks_fastest_and_checks_outputs(fake):
         autotune.search(stage_bm, stage_ihc, timer, lambda: next(outs))
 
 
+def test_pick_keeps_the_default_within_the_margin():
+    assert autotune.pick({0: 10.0, 1: 9.9, 2: 9.85}) == 0
+    assert autotune.pick({0: 10.0, 1: 9.7}) == 1
+    assert autotune.pick({0: 10.0, 1: 9.7, 3: 9.5}) == 3
+    assert autotune.pick({0: 10.0, 1: 9.9}, margin=0.0) == 1
+
+
+def test_search_warms_up_and_times_round_robin(fake):
+    """Untimed warm-up calls come first; then the candidates are timed in
+    turn, round after round, and each keeps its best time."""
+    order, t = [], iter(range(100))
+
+    def stage_bm():
+        order.append(("bm", fake.shape))
+
+    def stage_ihc():
+        order.append(("ihc", fake.run))
+
+    def timer(fn):
+        fn()
+        order.append("timed")
+        return 10.0 - 0.001 * next(t)  # later calls a little faster
+
+    autotune.search(stage_bm, stage_ihc, timer, lambda: (b"v", b"l"), shapes=[0, 1],
+                    runs=[0, 8], rounds=2, warmup=3)
+    bm = [o for o in order if o != "timed" and o[0] == "bm"]
+    assert bm[:3] == [("bm", 0)] * 3            # warm-up on the default
+    assert bm[3:7] == [("bm", 0), ("bm", 1), ("bm", 0), ("bm", 1)]
+
+
 def test_cache_round_trip(tmp_path, monkeypatch):
     monkeypatch.setenv("CGB_TUNE_CACHE", str(tmp_path / "t.json"))
     key = autotune.cache_key("NVIDIA GB300", "BatchSweep:units=3025", lib_hash="abc")
