@@ -73,7 +73,7 @@ extern "C" {
 
 const char* cgb_last_error(void) { return cgb::g_last_error.c_str(); }
 
-int cgb_abi_version(void) { return 3; }
+int cgb_abi_version(void) { return 4; }
 
 int64_t cgb_kernel_launch_count(void) { return cgb::g_launches.load(); }
 

@@ -571,10 +571,10 @@ extern "C" void RunIHCKernel(JNDFloat* host_backup, int, int save_lambda, int ba
                              Log&) {
   if (!H.ihc_ready) throw std::runtime_error("cochlea_gb300: RunIHCKernel before IHCNewKernel");
   if (!H.d_aihc) throw std::runtime_error("cochlea_gb300: RunIHCKernel before loadAihc");
+  // debug stages (CudaUnifiedCalcIHC, src/cochlea.cu:3431-3506): 9 AC, 10 DC,
+  // 11 and 12 dS, 13 and 14 IHC, each copied to host_backup
   const bool want_ihc = backup_stage == 13 || backup_stage == 14;
-  const bool want_ac = backup_stage == 9 && H.ac_iir;  // the IIR path keeps AC
-  if (backup_stage >= 9 && backup_stage <= 12 && !want_ac)
-    throw std::runtime_error("cochlea_gb300: the fused IHC kernel exposes no AC/DC/dS stage");
+  const bool want_stage = backup_stage >= 9 && backup_stage <= 12;
   const int64_t v_rows = (int64_t)(H.speeds_n / 256);
   cgb_ihc_frame fr{};
   fr.v_row0 = 0;
@@ -594,39 +594,53 @@ extern "C" void RunIHCKernel(JNDFloat* host_backup, int, int save_lambda, int ba
   if (need < 0) throw std::runtime_error("cochlea_gb300: bad IIR filter");
   ensure(H.scratch, H.scratch_n, (size_t)need, "IHC scratch");
   float* ihc = nullptr;
-  if (want_ihc) {
+  float* stage_buf = nullptr;
+  if (want_ihc || want_stage) {
     ensure(H.buffer1, H.buffer1_n, (size_t)H.calc_time * 256, "IHC stage buffer");
-    ihc = H.buffer1;
+    gpu_check(cudaMemset(H.buffer1, 0, (size_t)H.calc_time * 256 * sizeof(float)),
+              "clear stage buffer");
+    (want_ihc ? ihc : stage_buf) = H.buffer1;
   }
   gpu_check(cudaMemset(H.status, 0, sizeof(int32_t)), "reset status");
   if (H.ac_iir) {
     ensure(H.ac_buf, H.ac_buf_n, (size_t)v_rows * 256, "AC buffer");
-    cgb_check(cgb_ihc_lambda_iir_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
+    const int rc =
+        want_stage
+            ? cgb_ihc_lambda_iir_stage_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
+                                           H.ac_a_taps.data(), (int)H.ac_taps.size(),
+                                           H.dc_taps.data(), (int)H.dc_taps.size(), &H.ihc_prm,
+                                           H.dmg, 1, H.d_aihc, H.lam, H.calc_time, ihc,
+                                           H.ac_buf, backup_stage, stage_buf, H.scratch,
+                                           (int64_t)H.scratch_n, H.status, nullptr)
+            : cgb_ihc_lambda_iir_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
                                      H.ac_a_taps.data(), (int)H.ac_taps.size(),
                                      H.dc_taps.data(), (int)H.dc_taps.size(), &H.ihc_prm, H.dmg,
                                      1, H.d_aihc, H.lam, H.calc_time, ihc, H.ac_buf, H.scratch,
-                                     (int64_t)H.scratch_n, H.status, nullptr),
-              "IHC/lambda (IIR AC)");
+                                     (int64_t)H.scratch_n, H.status, nullptr);
+    cgb_check(rc, "IHC/lambda (IIR AC)");
   } else {
-    cgb_check(cgb_ihc_lambda_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
+    const int rc =
+        want_stage
+            ? cgb_ihc_lambda_stage_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
+                                       (int)H.ac_taps.size(), H.dc_taps.data(),
+                                       (int)H.dc_taps.size(), &H.ihc_prm, H.dmg, 1, H.d_aihc,
+                                       H.lam, H.calc_time, ihc, backup_stage, stage_buf,
+                                       H.scratch, (int64_t)H.scratch_n, H.status, nullptr)
+            : cgb_ihc_lambda_dev(H.speeds, v_rows, &fr, 1, H.ac_taps.data(),
                                  (int)H.ac_taps.size(), H.dc_taps.data(), (int)H.dc_taps.size(),
                                  &H.ihc_prm, H.dmg, 1, H.d_aihc, H.lam, H.calc_time, ihc,
-                                 H.scratch, (int64_t)H.scratch_n, H.status, nullptr),
-              "IHC/lambda");
+                                 H.scratch, (int64_t)H.scratch_n, H.status, nullptr);
+    cgb_check(rc, "IHC/lambda");
   }
   gpu_check(cudaDeviceSynchronize(), "IHC/lambda");
   int32_t status = 0;
   gpu_check(cudaMemcpy(&status, H.status, sizeof(int32_t), cudaMemcpyDeviceToHost), "status");
   if (status) throw std::runtime_error("cochlea_gb300: IHC staging copy timed out");
-  if (want_ac && host_backup)
-    gpu_check(cudaMemcpy(host_backup, H.ac_buf, (size_t)fr.rows * 256 * sizeof(float),
-                         cudaMemcpyDeviceToHost),
-              "AC backup");
-  if (want_ihc && host_backup)
+  if ((want_ihc || want_stage) && host_backup)
     gpu_check(cudaMemcpy(host_backup, H.buffer1, (size_t)H.calc_time * 256 * sizeof(float),
                          cudaMemcpyDeviceToHost),
-              "IHC backup");
-  if (save_lambda && !want_ihc) {
+              "IHC stage backup");
+  if (save_lambda && !want_ihc && !want_stage) {
     const size_t n = (size_t)LAMBDA_COUNT * H.calc_time * 256;
     ensure(H.buffer1, H.buffer1_n, n, "lambda buffer");
     gpu_check(cudaMemcpy(H.buffer1, H.lam, n * sizeof(float), cudaMemcpyDeviceToDevice),

@@ -70,6 +70,10 @@ struct IHCArgs {
   int run;                     // tiles per CTA (consecutive, one frame)
   const float* ac_ext;         // AC by velocity row (the IIR path), or null: the FIR
   int skip_first_copy;         // test-only: arm the first staging wait but issue no copy
+  // RunIHCKernel's debug stage: 9 AC, 10 DC, 11 dS (0 none), stored by lambda
+  // row into stage_out [lam rows][256]
+  int stage;
+  float* stage_out;
 };
 
 // Test-only fault injection (cgb_ihc_set_fault_injection): the next launches
@@ -405,8 +409,13 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
         if (r < nr) {
           const int k = kb + r;
           const float ms = __fmaf_rn(src[r * kSecTile], scale, -acc[r]);
-          DS[(size_t)(k - dsbase) * kSecTile + lane] = __fmul_rn(ms, ms);
-          if (k >= row0) ACb[(size_t)(k - row0) * kSecTile + lane] = acc[r];
+          const float ds = __fmul_rn(ms, ms);
+          DS[(size_t)(k - dsbase) * kSecTile + lane] = ds;
+          if (k >= row0) {
+            ACb[(size_t)(k - row0) * kSecTile + lane] = acc[r];
+            if (A.stage == 9 || A.stage == 11)
+              A.stage_out[((int64_t)f.lam_row0 + k) * 256 + s] = A.stage == 9 ? acc[r] : ds;
+          }
         }
       }
     }
@@ -424,6 +433,7 @@ __global__ void __launch_bounds__(kIhcWarps * 32)
     auto set_pre = [&](int k, float dc) {
       float& slot = ACb[(size_t)(k - row0) * kSecTile + lane];
       slot = __fmaf_rn(slot, A.eta_ac, __fmul_rn(dc, A.eta_dc));
+      if (A.stage == 10) A.stage_out[((int64_t)f.lam_row0 + k) * 256 + s] = dc;
     };
     if (A.dc_uniform) {
       // tiles start on multiples of 32 rows, so every 32-row block opens on
@@ -636,7 +646,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
                     void* d_scratch, int64_t scratch_bytes, int32_t* d_status, void* stream,
                     int mode,
                     const float* ac_ext = nullptr, float* lam_host = nullptr,
-                    int32_t* stage_prefix = nullptr, float* stage_taps = nullptr) {
+                    int32_t* stage_prefix = nullptr, float* stage_taps = nullptr,
+                    int stage = 0, float* d_stage = nullptr) {
   if (n_frames == 0) return CGB_OK;
   if (!frames || n_frames < 0 || !ac_taps || !dc_taps || !prm || !d_scratch ||
       ((mode & kLaunch) && (!d_v || !d_dmg || !d_aihc || !d_lam || !d_status)))
@@ -651,6 +662,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
     const int rc = check_host_mirror(lam_host, "cgb_ihc_lambda_dev: h_lam");
     if (rc) return rc;
   }
+  if (stage != 0 && (stage < 9 || stage > 12 || ((mode & kLaunch) && !d_stage)))
+    return fail(CGB_ERR_ARG, "cgb_ihc_lambda_stage_dev: stage must be 9-12 with an output buffer");
   if (v_rows > INT32_MAX)
     return fail(CGB_ERR_RANGE, "cgb_ihc_lambda_dev: more than 2^31-1 velocity rows");
   // host staging of the tile prefix and the taps: a vector, or the caller's
@@ -754,6 +767,8 @@ int ihc_lambda_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frame
   A.status = d_status;
   A.ac_ext = ac_ext;
   A.skip_first_copy = g_fault_skip_copy;
+  A.stage = stage == 12 ? 11 : stage;  // the reference's 12 ("Shigh") is dS too
+  A.stage_out = d_stage;
   A.run = run;
   A.dc_uniform = 1;
   for (int i = 1; i < n_dc; ++i) A.dc_uniform &= dc_taps[i] == dc_taps[0];
@@ -795,6 +810,24 @@ extern "C" int cgb_ihc_lambda_dev(const float* d_v, int64_t v_rows, const cgb_ih
                               d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc,
                               d_scratch, scratch_bytes, d_status, stream,
                               cgb::kUpload | cgb::kLaunch);
+}
+
+extern "C" int cgb_ihc_lambda_stage_dev(const float* d_v, int64_t v_rows,
+                                        const cgb_ihc_frame* frames, int n_frames,
+                                        const float* ac_taps, int n_ac, const float* dc_taps,
+                                        int n_dc, const cgb_ihc_params* prm, const float* d_dmg,
+                                        int n_dmg_profiles, const float* d_aihc, float* d_lam,
+                                        int64_t lam_plane_rows, float* d_ihc, int stage,
+                                        float* d_stage, void* d_scratch, int64_t scratch_bytes,
+                                        int32_t* d_status, void* stream) {
+  if (stage < 9 || stage > 12 || !d_stage)
+    return cgb::fail(CGB_ERR_ARG,
+                     "cgb_ihc_lambda_stage_dev: stage must be 9-12 with an output buffer");
+  return cgb::ihc_lambda_impl(d_v, v_rows, frames, n_frames, ac_taps, n_ac, dc_taps, n_dc, prm,
+                              d_dmg, n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc,
+                              d_scratch, scratch_bytes, d_status, stream,
+                              cgb::kUpload | cgb::kLaunch, nullptr, nullptr, nullptr, nullptr,
+                              stage, d_stage);
 }
 
 extern "C" int cgb_ihc_lambda_upload_dev(const cgb_ihc_frame* frames, int n_frames,
@@ -1006,15 +1039,16 @@ extern "C" int64_t cgb_ihc_lambda_iir_scratch_bytes(const cgb_ihc_frame* frames,
          (int64_t)(align256(segs * sizeof(IIRSeg)) + align256((size_t)2 * n_iir * 8));
 }
 
-extern "C" int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows,
-                                      const cgb_ihc_frame* frames, int n_frames,
-                                      const float* b_taps, const float* a_taps, int n_iir,
-                                      const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
-                                      const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
-                                      float* d_lam, int64_t lam_plane_rows, float* d_ihc,
-                                      float* d_ac, void* d_scratch, int64_t scratch_bytes,
-                                      int32_t* d_status, void* stream) {
-  using namespace cgb;
+namespace cgb {
+namespace {
+
+int ihc_lambda_iir_impl(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                        int n_frames, const float* b_taps, const float* a_taps, int n_iir,
+                        const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+                        const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
+                        float* d_lam, int64_t lam_plane_rows, float* d_ihc, float* d_ac,
+                        void* d_scratch, int64_t scratch_bytes, int32_t* d_status, void* stream,
+                        int stage, float* d_stage) {
   if (n_frames == 0) return CGB_OK;
   if (!frames || n_frames < 0 || !b_taps || !a_taps || !d_ac || !d_v || !prm || !d_scratch)
     return fail(CGB_ERR_ARG, "cgb_ihc_lambda_iir_dev: null pointer argument");
@@ -1062,5 +1096,42 @@ extern "C" int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows,
   }
   return ihc_lambda_impl(d_v, v_rows, frames, n_frames, &one, 1, dc_taps, n_dc, prm, d_dmg,
                          n_dmg_profiles, d_aihc, d_lam, lam_plane_rows, d_ihc, d_scratch,
-                         base_bytes, d_status, stream, kLaunch, d_ac);
+                         base_bytes, d_status, stream, kLaunch, d_ac, nullptr, nullptr, nullptr,
+                         stage, d_stage);
+}
+
+}  // namespace
+}  // namespace cgb
+
+extern "C" int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows,
+                                      const cgb_ihc_frame* frames, int n_frames,
+                                      const float* b_taps, const float* a_taps, int n_iir,
+                                      const float* dc_taps, int n_dc, const cgb_ihc_params* prm,
+                                      const float* d_dmg, int n_dmg_profiles, const float* d_aihc,
+                                      float* d_lam, int64_t lam_plane_rows, float* d_ihc,
+                                      float* d_ac, void* d_scratch, int64_t scratch_bytes,
+                                      int32_t* d_status, void* stream) {
+  return cgb::ihc_lambda_iir_impl(d_v, v_rows, frames, n_frames, b_taps, a_taps, n_iir, dc_taps,
+                                  n_dc, prm, d_dmg, n_dmg_profiles, d_aihc, d_lam,
+                                  lam_plane_rows, d_ihc, d_ac, d_scratch, scratch_bytes,
+                                  d_status, stream, 0, nullptr);
+}
+
+extern "C" int cgb_ihc_lambda_iir_stage_dev(const float* d_v, int64_t v_rows,
+                                            const cgb_ihc_frame* frames, int n_frames,
+                                            const float* b_taps, const float* a_taps, int n_iir,
+                                            const float* dc_taps, int n_dc,
+                                            const cgb_ihc_params* prm, const float* d_dmg,
+                                            int n_dmg_profiles, const float* d_aihc,
+                                            float* d_lam, int64_t lam_plane_rows, float* d_ihc,
+                                            float* d_ac, int stage, float* d_stage,
+                                            void* d_scratch, int64_t scratch_bytes,
+                                            int32_t* d_status, void* stream) {
+  if (stage < 9 || stage > 12 || !d_stage)
+    return cgb::fail(CGB_ERR_ARG,
+                     "cgb_ihc_lambda_iir_stage_dev: stage must be 9-12 with an output buffer");
+  return cgb::ihc_lambda_iir_impl(d_v, v_rows, frames, n_frames, b_taps, a_taps, n_iir, dc_taps,
+                                  n_dc, prm, d_dmg, n_dmg_profiles, d_aihc, d_lam,
+                                  lam_plane_rows, d_ihc, d_ac, d_scratch, scratch_bytes,
+                                  d_status, stream, stage, d_stage);
 }

@@ -308,7 +308,35 @@ int main(int argc, char** argv) {
     // harness-only test key (not a reference key): make the IHC kernel's
     // staging wait run out, to exercise the drop-in's error path
     if (P.num("Test_Fault_IHC_Staging", 0) != 0) cgb_ihc_set_fault_injection(1);
-    RunIHCKernel(nullptr, 0, 1, -1, 0, log);
+    // the reference's stage dump (TEST_File_Target + Type_TEST_Output,
+    // src/AudioGramCreator.cpp:877-892,913-919; stage names
+    // src/params.cpp:182-187): RunIHCKernel's backup of AC (9), DC (10), dS
+    // (11), Shigh (12, dS as well), IHC (13) or PRE_IHC (14) is written as
+    // write_time x 256 raw floats, the first run of a set truncating the
+    // file.  The JND-side test outputs (MeanRate, dLambda, JND_Lambda, ...)
+    // are not served.
+    const std::string test_target = P.str("TEST_File_Target", "");
+    int backup_stage = -1;
+    if (!test_target.empty()) {
+      const std::string type = P.str("Type_TEST_Output", "MeanRate");
+      const char* names[] = {"AC", "DC", "dS", "Shigh", "IHC", "PRE_IHC"};
+      for (int k = 0; k < 6; ++k)
+        if (type == names[k]) backup_stage = 9 + k;
+      if (backup_stage < 0)
+        throw std::runtime_error("Type_TEST_Output " + type +
+                                 " is not served (only the IHC stages AC, DC, dS, Shigh, IHC, "
+                                 "PRE_IHC)");
+    }
+    std::vector<float> backup(backup_stage > 0 ? (size_t)calc_time * 256 : 0);
+    RunIHCKernel(backup_stage > 0 ? backup.data() : nullptr, 0, 1, backup_stage, 0, log);
+    if (backup_stage > 0) {
+      FILE* tf = std::fopen(test_target.c_str(), "wb");
+      if (!tf) throw std::runtime_error("cannot open TEST_File_Target " + test_target);
+      const size_t n = (size_t)write_time * 256;
+      const bool ok = std::fwrite(backup.data(), sizeof(float), n, tf) == n;
+      std::fclose(tf);
+      if (!ok) throw std::runtime_error("short write to TEST_File_Target " + test_target);
+    }
     std::vector<float> lam((size_t)LAMBDA_COUNT * calc_time * 256);
     BMOHCKernel_Copy_Lambda(lam.data(), lam.size(), 0);
     const int lam_rows = N * TB;

@@ -193,17 +193,25 @@ class IHCStage:
                                              device=self.device)
         return self._scratch
 
-    def run_dev(self, v, frames: np.ndarray, lam, ihc=None, stream=None) -> None:
+    def run_dev(self, v, frames: np.ndarray, lam, ihc=None, stream=None, stage: int = 0,
+                stage_out=None) -> None:
+        """stage 9-12 (with stage_out shaped like ihc): RunIHCKernel's debug
+        stage of every lambda row, 9 AC, 10 DC, 11 and 12 dS."""
         frames = np.ascontiguousarray(frames).view(FRAME_DTYPE)
         st = stream if stream is not None else self.torch.cuda.current_stream(self.device)
         sc = self.scratch(len(frames))
-        native.check(self.lib.cgb_ihc_lambda_dev(
-            native.ptr(v), int(v.shape[0]), native.ptr(frames), len(frames),
-            native.ptr(self.ac), len(self.ac), native.ptr(self.dc), len(self.dc),
-            C.byref(self.prm), native.ptr(self.dmg), int(self.dmg.shape[0]),
-            native.ptr(self.aihc), native.ptr(lam), int(lam.shape[1]), native.ptr(ihc),
-            native.ptr(sc), int(sc.numel()), native.ptr(self.status),
-            C.c_void_p(st.cuda_stream)), "cgb_ihc_lambda_dev")
+        head = (native.ptr(v), int(v.shape[0]), native.ptr(frames), len(frames),
+                native.ptr(self.ac), len(self.ac), native.ptr(self.dc), len(self.dc),
+                C.byref(self.prm), native.ptr(self.dmg), int(self.dmg.shape[0]),
+                native.ptr(self.aihc), native.ptr(lam), int(lam.shape[1]), native.ptr(ihc))
+        tail = (native.ptr(sc), int(sc.numel()), native.ptr(self.status),
+                C.c_void_p(st.cuda_stream))
+        if stage:
+            native.check(self.lib.cgb_ihc_lambda_stage_dev(*head, int(stage),
+                                                           native.ptr(stage_out), *tail),
+                         "cgb_ihc_lambda_stage_dev")
+        else:
+            native.check(self.lib.cgb_ihc_lambda_dev(*head, *tail), "cgb_ihc_lambda_dev")
 
     def upload_chunks(self, frame_groups, v_rows: int, lam_rows: int, stream=None):
         """Per-call tables (frames, tile prefix, taps) of each group of frames
@@ -276,16 +284,22 @@ class IHCStage:
             raise native.CGBError("IHC stage: a staged copy did not complete")
         return lam.cpu().numpy(), (ihc.cpu().numpy() if want_ihc else None), ac.cpu().numpy()
 
-    def run(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, want_ihc: bool = False):
-        """Host-buffer call; returns (lambda float32[3][lam_rows][256], ihc or None)."""
+    def run(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, want_ihc: bool = False,
+            stage: int = 0):
+        """Host-buffer call; returns (lambda float32[3][lam_rows][256], ihc or
+        None), and with stage 9-12 also that debug stage's [lam_rows][256]
+        plane as a third element."""
         torch = self.torch
         d_v = torch.from_numpy(np.require(v, np.float32, ["C", "W"])).to(self.device)
         lam = torch.zeros((3, lam_rows, 256), dtype=torch.float32, device=self.device)
         ihc = torch.zeros((lam_rows, 256), dtype=torch.float32, device=self.device) \
             if want_ihc else None
+        out = torch.zeros((lam_rows, 256), dtype=torch.float32, device=self.device) \
+            if stage else None
         self.status.zero_()
-        self.run_dev(d_v, frames, lam, ihc)
+        self.run_dev(d_v, frames, lam, ihc, stage=stage, stage_out=out)
         torch.cuda.synchronize(self.device)
         if int(self.status[0].item()) != 0:
             raise native.CGBError("IHC stage: a staged copy did not complete")
-        return lam.cpu().numpy(), (ihc.cpu().numpy() if want_ihc else None)
+        res = (lam.cpu().numpy(), (ihc.cpu().numpy() if want_ihc else None))
+        return res + (out.cpu().numpy(),) if stage else res

@@ -79,6 +79,10 @@ _SIGS = {
     "cgb_ihc_lambda_iir_scratch_bytes": (_i64, [_p, _i, _i, _i]),
     "cgb_ihc_lambda_iir_dev": (_i, [_p, _i64, _p, _i, _p, _p, _i, _p, _i, _p, _p, _i, _p, _p,
                                     _i64, _p, _p, _p, _i64, _p, _p]),
+    "cgb_ihc_lambda_iir_stage_dev": (_i, [_p, _i64, _p, _i, _p, _p, _i, _p, _i, _p, _p, _i, _p,
+                                          _p, _i64, _p, _p, _i, _p, _p, _i64, _p, _p]),
+    "cgb_ihc_lambda_stage_dev": (_i, [_p, _i64, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p,
+                                      _i64, _p, _i, _p, _p, _i64, _p, _p]),
     "cgb_hearing_aid_dev": (_i, [_p, _i, _i, _p, _i, _p, _i, _p, _p]),
     "cgb_design_equiripple_lowpass": (_i, [_i, _d, _d, _d, _d, _p, _p, _p]),
     "cgb_complex_jnd": (_i, [_p, _i, _p, _p, _i, _i, _i, C.c_float, _p, _p, _p]),

@@ -313,6 +313,33 @@ int cgb_ihc_lambda_iir_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame
                            void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
                            void* stream);
 
+/* RunIHCKernel's debug stages (backup_stage 9-12 of CudaUnifiedCalcIHC,
+ * src/cochlea.cu:3431-3506): cgb_ihc_lambda_dev and cgb_ihc_lambda_iir_dev
+ * that also store one intermediate plane of every lambda row into d_stage,
+ * laid out as d_ihc ([lam_plane_rows][256] floats):
+ *   stage 9   AC, the AC filter's output
+ *   stage 10  DC, the DC filter's output
+ *   stage 11, 12  dS = (scale v - AC)^2 (the reference's "dS" and "Shigh"
+ *             stages both copy dS)
+ * The values are the kernel's own (the AC and dS that feed lambda, the DC
+ * of the pre-synaptic sum); lambda and IHC are computed as without a stage.
+ * Other stage values, or a null d_stage, return CGB_ERR_ARG. */
+int cgb_ihc_lambda_stage_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                             int n_frames, const float* ac_taps, int n_ac, const float* dc_taps,
+                             int n_dc, const cgb_ihc_params* prm, const float* d_dmg,
+                             int n_dmg_profiles, const float* d_aihc, float* d_lam,
+                             int64_t lam_plane_rows, float* d_ihc, int stage, float* d_stage,
+                             void* d_scratch, int64_t scratch_bytes, int32_t* d_status,
+                             void* stream);
+int cgb_ihc_lambda_iir_stage_dev(const float* d_v, int64_t v_rows, const cgb_ihc_frame* frames,
+                                 int n_frames, const float* b_taps, const float* a_taps,
+                                 int n_iir, const float* dc_taps, int n_dc,
+                                 const cgb_ihc_params* prm, const float* d_dmg,
+                                 int n_dmg_profiles, const float* d_aihc, float* d_lam,
+                                 int64_t lam_plane_rows, float* d_ihc, float* d_ac, int stage,
+                                 float* d_stage, void* d_scratch, int64_t scratch_bytes,
+                                 int32_t* d_status, void* stream);
+
 /* Tiles each IHC/lambda CTA walks in a run (the DC look-back is recomputed
  * once per run): 0 restores the automatic choice (32 or 16 tiles while at
  * least two CTAs per SM remain, else 8); 1-64 forces that run length.  It

@@ -691,7 +691,12 @@ static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int tot
                             const double* ac_taps, int n_ac, const double* dc_taps, int n_dc,
                             double scale, double eta_ac, double eta_dc, const double* ihc_damage,
                             const float* aihc, const float* spont, double lambda_sat, float* ihc,
-                            float* lam, int64_t lam_stride, int mode, const float* ac_in) {
+                            float* lam, int64_t lam_stride, int mode, const float* ac_in,
+                            int stage = 0, float* stage_out = nullptr) {
+  // stage 9 AC, 10 DC, 11 dS of every lambda row into stage_out [rows][256]
+  auto put_stage = [&](int which, int k, int s, double val) {
+    if (stage_out && stage == which && k < lam_rows) stage_out[(size_t)k * NS + s] = (float)val;
+  };
   if (mode == 2) {
     // The GB300 kernel's arithmetic: float taps (AC taps pre-scaled), each
     // FIR summed over taps in order with the compensated dot product Dot2
@@ -752,6 +757,8 @@ static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int tot
         acf[(size_t)k * NS + s] = acc;
         float ms = fmaf(v[(size_t)k * NS + s], sc, -acc);
         dsf[(size_t)k * NS + s] = ms * ms;
+        put_stage(9, k, s, acc);
+        put_stage(11, k, s, dsf[(size_t)k * NS + s]);
       }
     }
     // DC with uniform taps d: d * (window sum), the window re-summed at
@@ -790,6 +797,7 @@ static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int tot
         } else {
           acc = dot2(dt.data(), dsf.data() + (size_t)k * NS + s, tu);
         }
+        put_stage(10, k, s, acc);
         float pre = fmaf(acf[(size_t)k * NS + s], ea, acc * ed);
         float y = (float)ihc_damage[s] * pre;
         float lg = own_log10f(fmaxf(y, 0.0f) + 1e-20f);
@@ -825,6 +833,8 @@ static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int tot
         float ms = fmaf(v[(size_t)k * NS + s], (float)scale, -acf);
         ds[(size_t)k * NS + s] = (double)(ms * ms);
       }
+      put_stage(9, k, s, ac[(size_t)k * NS + s]);
+      put_stage(11, k, s, ds[(size_t)k * NS + s]);
     }
   }
   for (int k = 0; k < rows; ++k) {
@@ -832,6 +842,7 @@ static void ihc_lambda_impl(const float* v, int rows, int seg, int frdp, int tot
     for (int s = 0; s < NS; ++s) {
       double acc = 0.0;
       for (int i = 0; i < tu; ++i) acc = acc + dc_taps[i] * ds[(size_t)(k - i) * NS + s];
+      put_stage(10, k, s, acc);
       double pre;
       if (fp64) {
         pre = ac[(size_t)k * NS + s] * eta_ac + acc * eta_dc;
@@ -929,6 +940,20 @@ void orc_ihc_lambda_iir(const float* v, int rows, int seg, int frdp, int total, 
   ihc_lambda_impl(v, rows, seg, frdp, total, lam_rows, b, n_iir, dc_taps, n_dc, scale, eta_ac,
                   eta_dc, ihc_damage, aihc, spont, lambda_sat, ihc, lam, lam_stride, mode,
                   ac.data());
+}
+
+// orc_ihc_lambda that also stores one intermediate plane of every lambda row
+// into stage_out [lam_rows][256]: stage 9 AC, 10 DC, 11 dS (RunIHCKernel's
+// backup stages, src/cochlea.cu:3431-3506), in `mode`'s arithmetic.
+void orc_ihc_lambda_stage(const float* v, int rows, int seg, int frdp, int total, int lam_rows,
+                          const double* ac_taps, int n_ac, const double* dc_taps, int n_dc,
+                          double scale, double eta_ac, double eta_dc, const double* ihc_damage,
+                          const float* aihc, const float* spont, double lambda_sat, float* ihc,
+                          float* lam, int64_t lam_stride, int mode, int stage,
+                          float* stage_out) {
+  ihc_lambda_impl(v, rows, seg, frdp, total, lam_rows, ac_taps, n_ac, dc_taps, n_dc, scale,
+                  eta_ac, eta_dc, ihc_damage, aihc, spont, lambda_sat, ihc, lam, lam_stride, mode,
+                  nullptr, stage, stage_out);
 }
 
 // IHC + lambda from a given AC stage (ac: rows x 256 floats) in place of the

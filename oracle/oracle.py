@@ -77,6 +77,10 @@ def load():
                                            _p, C.c_int, _p, C.c_int, C.c_double, C.c_double,
                                            C.c_double, _p, _p, _p, C.c_double, _p, _p, C.c_int64,
                                            C.c_int, _p]
+        lib.orc_ihc_lambda_stage.argtypes = [_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             _p, C.c_int, _p, C.c_int, C.c_double, C.c_double,
+                                             C.c_double, _p, _p, _p, C.c_double, _p, _p,
+                                             C.c_int64, C.c_int, C.c_int, _p]
         lib.orc_ihc_lambda_ac.argtypes = [_p, _p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                           _p, C.c_int, C.c_double, C.c_double, C.c_double, _p,
                                           _p, _p, C.c_double, _p, _p, C.c_int64, C.c_int]
@@ -215,6 +219,26 @@ def ws_forward_backward(params, feat, target, s_out, round_bf16=True, want_grad=
     load().orc_ws_forward_backward(_ptr(params), _ptr(feat), _ptr(target), n, s_out,
                                    1 if round_bf16 else 0, _ptr(out), _ptr(loss), _ptr(grad))
     return out, float(loss[0]), grad
+
+
+def ihc_lambda_stage(v, seg, frdp, total, lam_rows, ac_taps, dc_taps, scale, eta_ac, eta_dc,
+                     ihc_damage, aihc, spont, lambda_sat, stage, mode=0):
+    """One intermediate plane of the IHC stage for every lambda row: stage 9
+    AC, 10 DC, 11 dS, in `mode`'s arithmetic (as ihc_lambda).  Returns
+    float32 [lam_rows][256]."""
+    v = np.ascontiguousarray(v, np.float32)
+    rows = v.shape[0]
+    lam = np.zeros((3, lam_rows, 256), np.float32)
+    out = np.zeros((lam_rows, 256), np.float32)
+    ac = np.ascontiguousarray(ac_taps, np.float64)
+    dc = np.ascontiguousarray(dc_taps, np.float64)
+    load().orc_ihc_lambda_stage(_ptr(v), rows, seg, frdp, total, lam_rows, _ptr(ac), len(ac),
+                                _ptr(dc), len(dc), scale, eta_ac, eta_dc,
+                                _ptr(np.ascontiguousarray(ihc_damage, np.float64)),
+                                _ptr(np.ascontiguousarray(aihc, np.float32)),
+                                _ptr(np.ascontiguousarray(spont, np.float32)), lambda_sat,
+                                None, _ptr(lam), lam_rows, mode, stage, _ptr(out))
+    return out
 
 
 def ihc_lambda_ac(v, ac, seg, frdp, total, lam_rows, dc_taps, scale, eta_ac, eta_dc,

@@ -25,7 +25,7 @@ def declared_symbols():
 
 def test_library_loads():
     lib = native.load()
-    assert lib.cgb_abi_version() == 3
+    assert lib.cgb_abi_version() == 4
 
 
 # C++ templates of the reference API (include/cochlea_common.h:186-191) with the

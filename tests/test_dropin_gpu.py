@@ -202,6 +202,56 @@ def test_harness_writes_the_reference_output_files(tmp_path, mv):
     assert np.array_equal(jnd, np.concatenate([_transpose(ai, cols), _transpose(rate, cols)]))
 
 
+def test_harness_writes_the_ihc_stage_file(tmp_path, mv):
+    """TEST_File_Target with Type_TEST_Output AC, DC, dS, Shigh or IHC: the
+    harness writes RunIHCKernel's backup of that stage, write_time x 256 raw
+    floats, as the reference's AudioGramCreator does.  Each file equals the
+    stage plane of the IHC kernel on the same velocity (bit for bit); a
+    JND-side test output is refused."""
+    import torch
+    noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
+    ac = ihc.design_ac_lowpass()
+    (tmp_path / "ac.f32").write_bytes(ac.tobytes())
+    (tmp_path / "noise.f32").write_bytes(noise.tobytes())
+    build.build()
+    cfg = model.RunConfig(Time_Block_Length=0.002, Decouple_Filter=2, Overlap_Time=0.001,
+                          OHC_Vector=np.array([0.5, 0.3, 0.1], np.float32),
+                          IHC_Vector=np.array([8.0, 6.0], np.float32))
+    sweep = ProfileSweep(frequencies=[1000.0, 3000.0], powers=[40.0, 80.0],
+                         noises=[1111.0, 30.0], calculate_jnd=True)
+    run = ProfileRun("cuda:0", cfg, sweep, noise=noise, mv=mv, ac_taps=ac,
+                     jnd=JNDWindow(head=0.001, tail=0.0005))
+    run.step()
+    torch.cuda.synchronize()
+    nodes = run.N * cfg.Time_Blocks
+    v = run.d_v.cpu().numpy()
+    lam_rows = int(run.d_lam.shape[1])
+    for name, stage in (("AC", 9), ("DC", 10), ("dS", 11), ("Shigh", 12), ("IHC", 13)):
+        target = tmp_path / f"stage_{name}.bin"
+        par = tmp_path / f"run_{name}.par"
+        par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
+                                  out=tmp_path / f"out_{name}.bin") +
+                       f'TEST_File_Target = "{target}"\nType_TEST_Output = "{name}"\n')
+        res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True,
+                             text=True, timeout=300)
+        assert res.returncode == 0, res.stderr
+        got = np.fromfile(target, np.float32)
+        assert got.size % 256 == 0 and got.size // 256 >= nodes
+        got = got.reshape(-1, 256)
+        if stage == 13:
+            _, want = run.ihc.run(v, run.frames, lam_rows, want_ihc=True)
+        else:
+            _, _, want = run.ihc.run(v, run.frames, lam_rows, stage=stage)
+        assert np.array_equal(got[:nodes].view(np.uint32), want[:nodes].view(np.uint32)), name
+    par = tmp_path / "run_mr.par"
+    par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
+                              out=tmp_path / "out_mr.bin") +
+                   f'TEST_File_Target = "{tmp_path / "mr.bin"}"\nType_TEST_Output = "MeanRate"\n')
+    res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode != 0 and "not served" in res.stderr
+
+
 def test_unbuilt_kernel_selectors_raise(tmp_path, mv):
     """BMOHCNewKernel raises for Run_Fast_BM_Calculation values, cache hints
     and enable flags it does not build, instead of running another solver."""

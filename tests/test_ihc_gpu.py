@@ -4,7 +4,7 @@ arithmetic (double taps and accumulators), the lambda bar."""
 import numpy as np
 import pytest
 
-from cochlearmodel_gb300 import ihc
+from cochlearmodel_gb300 import ihc, native
 from oracle import oracle as orc
 from tests import cases
 
@@ -180,3 +180,42 @@ def test_staging_wait_runs_out_and_reports(stage):
         native.check(lib.cgb_ihc_set_fault_injection(0), "fault injection")
     again, _ = stage.run(v, frames, 600)
     assert np.array_equal(again.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("stage", [9, 10, 11, 12])
+def test_debug_stages(mv, stage):
+    """RunIHCKernel's debug stages (9 AC, 10 DC, 11 and 12 dS): the plane the
+    kernel stores is bit-exact against the oracle's kernel arithmetic, within
+    the lambda bar of the reference arithmetic, and the lambda planes equal a
+    run without a stage."""
+    st = ihc.IHCStage("cuda:0")
+    case = cases.decoupled_sweep(mv, n_signals=2, decouple=2, block_ms=1.5, overlap_ms=0.5)
+    cfg, sc, gamma, units, x, rows = case
+    v, _, _ = orc.bm_run(mv.section_params(), gamma, sc, units, x, rows)
+    fr = ihc.reference_frame(cfg)
+    v = v[:int(fr["rows"][0])]
+    n = int(fr["lam_rows"][0])
+    lam0, _ = st.run(v, fr, n)
+    lam, _, plane = st.run(v, fr, n, stage=stage)
+    assert np.array_equal(lam.view(np.uint32), lam0.view(np.uint32))
+    o_stage = 11 if stage == 12 else stage
+    args = (v, int(fr["seg"][0]), int(fr["frdp"][0]), int(fr["total"][0]), n,
+            st.ac.astype(np.float64), st.dc.astype(np.float64), st.nerve.scale,
+            st.nerve.eta_AC, st.nerve.eta_DC, st.dmg_host[0].astype(np.float64),
+            st.nerve.aihc(), np.asarray(st.nerve.spontRate, np.float32), st.nerve.Lambda_SAT,
+            o_stage)
+    want = orc.ihc_lambda_stage(*args, mode=2)
+    assert np.array_equal(plane.view(np.uint32), want.view(np.uint32))
+    ref = orc.ihc_lambda_stage(*args, mode=0)
+    assert np.abs(plane - ref).max() <= REL * np.abs(ref).max()
+    assert np.abs(plane).max() > 0
+
+
+def test_debug_stage_rejected():
+    st = ihc.IHCStage("cuda:0")
+    v = np.zeros((600, 256), np.float32)
+    fr = np.zeros(1, ihc.FRAME_DTYPE)
+    fr[0] = (0, 0, 600, 512, 600, 600, ihc.round64(600), 0)
+    for bad in (8, 13):
+        with pytest.raises(native.CGBError):
+            st.run(v, fr, 512, stage=bad)
