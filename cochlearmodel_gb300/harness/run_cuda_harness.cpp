@@ -308,25 +308,30 @@ int main(int argc, char** argv) {
     // harness-only test key (not a reference key): make the IHC kernel's
     // staging wait run out, to exercise the drop-in's error path
     if (P.num("Test_Fault_IHC_Staging", 0) != 0) cgb_ihc_set_fault_injection(1);
-    // the reference's stage dump (TEST_File_Target + Type_TEST_Output,
-    // src/AudioGramCreator.cpp:877-892,913-919; stage names
-    // src/params.cpp:182-187): RunIHCKernel's backup of AC (9), DC (10), dS
-    // (11), Shigh (12, dS as well), IHC (13) or PRE_IHC (14) is written as
-    // write_time x 256 raw floats, the first run of a set truncating the
-    // file.  The JND-side test outputs (MeanRate, dLambda, JND_Lambda, ...)
-    // are not served.
+    // the reference's test output (TEST_File_Target + Type_TEST_Output,
+    // default MeanRate; src/AudioGramCreator.cpp:877-892,913-970, stage
+    // names src/params.cpp:165-187), written as raw floats, the first run of
+    // a set truncating the file:
+    //  - an IHC stage, RunIHCKernel's backup of AC (9), DC (10), dS (11),
+    //    Shigh (12, dS as well), IHC (13) or PRE_IHC (14): write_time x 256;
+    //  - MeanRate, the JND's mean rates [3][intervals][256] (getCudaMeanRate).
+    // The other JND-side outputs (dMeanRate, dLambda, JND_Lambda, CRLB_RA,
+    // ...) are not served.
     const std::string test_target = P.str("TEST_File_Target", "");
+    const std::string test_type = P.str("Type_TEST_Output", "MeanRate");
     int backup_stage = -1;
-    if (!test_target.empty()) {
-      const std::string type = P.str("Type_TEST_Output", "MeanRate");
+    const bool test_mean_rate = !test_target.empty() && test_type == "MeanRate";
+    if (!test_target.empty() && !test_mean_rate) {
       const char* names[] = {"AC", "DC", "dS", "Shigh", "IHC", "PRE_IHC"};
       for (int k = 0; k < 6; ++k)
-        if (type == names[k]) backup_stage = 9 + k;
+        if (test_type == names[k]) backup_stage = 9 + k;
       if (backup_stage < 0)
-        throw std::runtime_error("Type_TEST_Output " + type +
-                                 " is not served (only the IHC stages AC, DC, dS, Shigh, IHC, "
-                                 "PRE_IHC)");
+        throw std::runtime_error("Type_TEST_Output " + test_type +
+                                 " is not served (only MeanRate and the IHC stages AC, DC, dS, "
+                                 "Shigh, IHC, PRE_IHC)");
     }
+    if (test_mean_rate && !calc_jnd)
+      throw std::runtime_error("Type_TEST_Output MeanRate needs Calculate_JND");
     std::vector<float> backup(backup_stage > 0 ? (size_t)calc_time * 256 : 0);
     RunIHCKernel(backup_stage > 0 ? backup.data() : nullptr, 0, 1, backup_stage, 0, log);
     if (backup_stage > 0) {
@@ -384,6 +389,16 @@ int main(int argc, char** argv) {
         };
         jr[i] = db(ra);
         ja[i] = db(ai);
+      }
+      if (test_mean_rate) {
+        const size_t n = (size_t)3 * n_int * 256;  // getMeanNodes()
+        std::vector<float> mr(n);
+        GeneralKernel_Copy_Results_Template<float>(mr.data(), getCudaMeanRate(), n);
+        FILE* tf = std::fopen(test_target.c_str(), "wb");
+        if (!tf) throw std::runtime_error("cannot open TEST_File_Target " + test_target);
+        const bool ok = std::fwrite(mr.data(), sizeof(float), n, tf) == n;
+        std::fclose(tf);
+        if (!ok) throw std::runtime_error("short write to TEST_File_Target " + test_target);
       }
     }
 

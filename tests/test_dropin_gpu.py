@@ -206,8 +206,9 @@ def test_harness_writes_the_ihc_stage_file(tmp_path, mv):
     """TEST_File_Target with Type_TEST_Output AC, DC, dS, Shigh or IHC: the
     harness writes RunIHCKernel's backup of that stage, write_time x 256 raw
     floats, as the reference's AudioGramCreator does.  Each file equals the
-    stage plane of the IHC kernel on the same velocity (bit for bit); a
-    JND-side test output is refused."""
+    stage plane of the IHC kernel on the same velocity (bit for bit).  The
+    default type, MeanRate, writes the JND's mean rates; the other JND-side
+    test outputs are refused."""
     import torch
     noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
     ac = ihc.design_ac_lowpass()
@@ -243,10 +244,23 @@ def test_harness_writes_the_ihc_stage_file(tmp_path, mv):
         else:
             _, _, want = run.ihc.run(v, run.frames, lam_rows, stage=stage)
         assert np.array_equal(got[:nodes].view(np.uint32), want[:nodes].view(np.uint32)), name
+    # MeanRate, the default type: the JND's mean rates, [3][intervals][256]
     par = tmp_path / "run_mr.par"
     par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
                               out=tmp_path / "out_mr.bin") +
-                   f'TEST_File_Target = "{tmp_path / "mr.bin"}"\nType_TEST_Output = "MeanRate"\n')
+                   f'TEST_File_Target = "{tmp_path / "mr.bin"}"\n')
+    res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stderr
+    mr = np.fromfile(tmp_path / "mr.bin", np.float32).reshape(3, run.n_int, 256)
+    lam = run.d_lam.cpu().numpy()
+    for i in range(run.n_int):
+        w = lam[:, i * run.L + run.head:i * run.L + run.head + run.len].astype(np.float64)
+        want = w.mean(axis=1)
+        assert np.abs(mr[:, i] - want).max() <= 1e-6 * np.abs(want).max()
+    par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
+                              out=tmp_path / "out_mr.bin") +
+                   f'TEST_File_Target = "{tmp_path / "x.bin"}"\nType_TEST_Output = "dLambda"\n')
     res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
                          timeout=300)
     assert res.returncode != 0 and "not served" in res.stderr
