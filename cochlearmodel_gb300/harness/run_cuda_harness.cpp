@@ -314,14 +314,26 @@ int main(int argc, char** argv) {
     // a set truncating the file:
     //  - an IHC stage, RunIHCKernel's backup of AC (9), DC (10), dS (11),
     //    Shigh (12, dS as well), IHC (13) or PRE_IHC (14): write_time x 256;
-    //  - MeanRate, the JND's mean rates [3][intervals][256] (getCudaMeanRate).
-    // The other JND-side outputs (dMeanRate, dLambda, JND_Lambda, CRLB_RA,
-    // ...) are not served.
+    //  - MeanRate, the JND's mean rates [3][intervals][256] (getCudaMeanRate);
+    //  - JND_Lambda, the three lambda planes (3 x calc_time x 256), or
+    //    JND_Lambda(k) plane k alone (calc_time x 256).
+    // The other JND-side outputs (dMeanRate, dLambda, CRLB_RA, ...) are not
+    // served.
     const std::string test_target = P.str("TEST_File_Target", "");
     const std::string test_type = P.str("Type_TEST_Output", "MeanRate");
     int backup_stage = -1;
     const bool test_mean_rate = !test_target.empty() && test_type == "MeanRate";
-    if (!test_target.empty() && !test_mean_rate) {
+    int test_lambda = -2;  // -1: all planes, 0..: one plane
+    std::smatch lam_m;
+    if (!test_target.empty() && test_type == "JND_Lambda") test_lambda = -1;
+    if (!test_target.empty() &&
+        std::regex_match(test_type, lam_m, std::regex("JND_Lambda\\(([[:digit:]])\\)"))) {
+      test_lambda = std::stoi(lam_m[1]);
+      if (test_lambda >= LAMBDA_COUNT)
+        throw std::runtime_error("index of lambda must be smaller than 3, you chose " +
+                                 lam_m[1].str());
+    }
+    if (!test_target.empty() && !test_mean_rate && test_lambda == -2) {
       const char* names[] = {"AC", "DC", "dS", "Shigh", "IHC", "PRE_IHC"};
       for (int k = 0; k < 6; ++k)
         if (test_type == names[k]) backup_stage = 9 + k;
@@ -344,6 +356,16 @@ int main(int argc, char** argv) {
     }
     std::vector<float> lam((size_t)LAMBDA_COUNT * calc_time * 256);
     BMOHCKernel_Copy_Lambda(lam.data(), lam.size(), 0);
+    if (test_lambda != -2) {
+      const size_t plane = (size_t)calc_time * 256;
+      const float* src = lam.data() + (test_lambda < 0 ? 0 : (size_t)test_lambda * plane);
+      const size_t n = test_lambda < 0 ? (size_t)LAMBDA_COUNT * plane : plane;
+      FILE* tf = std::fopen(test_target.c_str(), "wb");
+      if (!tf) throw std::runtime_error("cannot open TEST_File_Target " + test_target);
+      const bool ok = std::fwrite(src, sizeof(float), n, tf) == n;
+      std::fclose(tf);
+      if (!ok) throw std::runtime_error("short write to TEST_File_Target " + test_target);
+    }
     const int lam_rows = N * TB;
 
     // JND (AudioGramCreator::calcJND / calcJNDFinal)

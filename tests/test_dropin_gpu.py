@@ -207,8 +207,8 @@ def test_harness_writes_the_ihc_stage_file(tmp_path, mv):
     harness writes RunIHCKernel's backup of that stage, write_time x 256 raw
     floats, as the reference's AudioGramCreator does.  Each file equals the
     stage plane of the IHC kernel on the same velocity (bit for bit).  The
-    default type, MeanRate, writes the JND's mean rates; the other JND-side
-    test outputs are refused."""
+    default type, MeanRate, writes the JND's mean rates, JND_Lambda the
+    lambda planes; the other JND-side test outputs are refused."""
     import torch
     noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
     ac = ihc.design_ac_lowpass()
@@ -258,6 +258,18 @@ def test_harness_writes_the_ihc_stage_file(tmp_path, mv):
         w = lam[:, i * run.L + run.head:i * run.L + run.head + run.len].astype(np.float64)
         want = w.mean(axis=1)
         assert np.abs(mr[:, i] - want).max() <= 1e-6 * np.abs(want).max()
+    # JND_Lambda: the three lambda planes; JND_Lambda(k): plane k
+    for name, planes in (("JND_Lambda", [0, 1, 2]), ("JND_Lambda(1)", [1])):
+        target = tmp_path / "jl.bin"
+        par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
+                                  out=tmp_path / "out_mr.bin") +
+                       f'TEST_File_Target = "{target}"\nType_TEST_Output = "{name}"\n')
+        res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True,
+                             text=True, timeout=300)
+        assert res.returncode == 0, res.stderr
+        got = np.fromfile(target, np.float32).reshape(len(planes), -1, 256)
+        for k, j in enumerate(planes):
+            assert np.array_equal(got[k, :nodes].view(np.uint32), lam[j, :nodes].view(np.uint32))
     par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
                               out=tmp_path / "out_mr.bin") +
                    f'TEST_File_Target = "{tmp_path / "x.bin"}"\nType_TEST_Output = "dLambda"\n')
