@@ -114,6 +114,57 @@ __global__ void fix_lambda_kernel(T* lam, T* buf, int64_t plane, float s0, float
   }
 }
 
+// The JND's debug stages (GlobalCalculateJND's backup_stage,
+// src/cochlea.cu:3773-3944), written into the stage buffer in the reference's
+// layouts, for interval i of plane j (block (i, j)), section s (thread):
+//   1 AvgMeanRate  out[j n + i] = mean over sections of MR
+//   2 dMeanRate    out[(j n + i) 256 + s] = (MR - MR_ref) / dA
+//   3 dLambda      out[j plane + 256 (i L + head + t) + s] = (l - l_ref) / dA
+//                  (0 where dA <= 0), t < len
+//   4 preFisherAI  same positions: dLambda^2 / (Fs l_ref)
+//   5 preFisherAITimeReduced  out[(j n + i) 256 + s] =
+//                  (T / Tlength) nIHC_s sum_t preFisherAI
+//   6 CRLB_RA      out[(j n + i) 256 + s] = 1 / sqrt(T dMR^2 / MR_ref)
+// MR is the JND kernel's (double) mean rate.  The hot JND kernel keeps its
+// own order; these are for inspection and are computed separately.
+__global__ void jnd_stage_kernel(int stage, const float* lam, int64_t plane, const double* MR,
+                                 const double* dA, const int32_t* ref_of, const double* nihc,
+                                 int n, int L, int head, int len, double Fs, double T,
+                                 float* out) {
+  const int i = blockIdx.x, j = blockIdx.y, s = threadIdx.x;
+  const int r = ref_of[i];
+  const double da = dA[i];
+  const double mr = MR[((size_t)j * n + i) * 256 + s], mrr = MR[((size_t)j * n + r) * 256 + s];
+  const double dmr = (mr - mrr) / da;
+  const size_t mo = ((size_t)j * n + i) * 256 + s;
+  if (stage == 1) {
+    __shared__ double acc[256];
+    acc[s] = mr;
+    for (int t = 128; t >= 1; t >>= 1) {
+      __syncthreads();
+      if (s < t) acc[s] += acc[s + t];
+    }
+    if (s == 0) out[(size_t)j * n + i] = (float)(acc[0] / 256.0);
+  } else if (stage == 2) {
+    out[mo] = (float)dmr;
+  } else if (stage == 6) {
+    out[mo] = (float)(1.0 / sqrt(T * dmr * dmr / mrr));
+  } else {
+    const float* c = lam + (size_t)j * plane + 256 * ((size_t)i * L + head) + s;
+    const float* rf = lam + (size_t)j * plane + 256 * ((size_t)r * L + head) + s;
+    float* o = out + (size_t)j * plane + 256 * ((size_t)i * L + head) + s;
+    double sum = 0.0;
+    for (int t = 0; t < len; ++t) {
+      const double dl = da > 0.0 ? ((double)c[(size_t)t * 256] - rf[(size_t)t * 256]) / da : 0.0;
+      const double pre = dl * dl / (Fs * (double)rf[(size_t)t * 256]);
+      if (stage == 3) o[(size_t)t * 256] = (float)dl;
+      if (stage == 4) o[(size_t)t * 256] = (float)pre;
+      sum += pre;
+    }
+    if (stage == 5) out[mo] = (float)((T / ((double)len / Fs)) * nihc[s] * sum);
+  }
+}
+
 __global__ void to_float_kernel(const double* src, float* dst, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -804,8 +855,11 @@ extern "C" void CudaCalculateJND(
     int overlapNodes, int JNDIntervalNodes, int lengthOffset, int* JND_Serial_Intervals_Positions,
     int* JND_Interval_To_Reference, JNDFloat* F_RA, JNDFloat* FisherAISum, int,
     int calculatedMatrixSize, double JND_Delta_Alpha_Length_Factor, int, int, bool calcdA, bool,
-    int, Log&) {
+    int backup_stage, Log&) {
   if (!H.lam) throw std::runtime_error("cochlea_gb300: CudaCalculateJND before IHCNewKernel");
+  // backup_stage 1-6 are the JND's debug stages (into getCudaBuffer); the
+  // reference's JND kernel writes nothing for the others (8 is JND_Lambda,
+  // read from the lambda buffer; 9-14 belong to RunIHCKernel)
   // reference interval of each interval of this chunk (src/cochlea.cu:3818-3840)
   std::vector<int32_t> ref(JNDIntervals);
   for (int i = 0; i < JNDIntervals; ++i) {
@@ -849,6 +903,19 @@ extern "C" void CudaCalculateJND(
             "JND");
   to_float_kernel<<<256, 256>>>(H.mean_rate, H.mean_rate_f, (int64_t)mean);
   gpu_check(cudaGetLastError(), "mean-rate conversion");
+  if (backup_stage >= 1 && backup_stage <= 6) {
+    const size_t need = (backup_stage == 3 || backup_stage == 4)
+                            ? (size_t)LAMBDA_COUNT * plane_rows * 256
+                            : (backup_stage == 1 ? (size_t)LAMBDA_COUNT * JNDIntervals : mean);
+    ensure(H.buffer1, H.buffer1_n, need, "JND stage buffer");
+    if (backup_stage == 3 || backup_stage == 4)
+      gpu_check(cudaMemset(H.buffer1, 0, need * sizeof(float)), "clear JND stage buffer");
+    const double T = JND_Delta_Alpha_Length_Factor / Fs;
+    jnd_stage_kernel<<<dim3((unsigned)JNDIntervals, LAMBDA_COUNT), 256>>>(
+        backup_stage, H.lam, (int64_t)plane_rows * 256, H.mean_rate, H.dA, H.ref_of, H.nihc,
+        JNDIntervals, JNDIntervalNodes, JNDIntervalHeadNodes, lengthOffset, Fs, T, H.buffer1);
+    gpu_check(cudaGetLastError(), "JND stage kernel");
+  }
   std::vector<double> Fh((size_t)6 * JNDIntervals);
   gpu_check(cudaMemcpy(Fh.data(), H.F, Fh.size() * sizeof(double), cudaMemcpyDeviceToHost),
             "read Fisher sums");

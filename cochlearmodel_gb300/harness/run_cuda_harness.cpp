@@ -316,15 +316,37 @@ int main(int argc, char** argv) {
     //    Shigh (12, dS as well), IHC (13) or PRE_IHC (14): write_time x 256;
     //  - MeanRate, the JND's mean rates [3][intervals][256] (getCudaMeanRate);
     //  - JND_Lambda, the three lambda planes (3 x calc_time x 256), or
-    //    JND_Lambda(k) plane k alone (calc_time x 256).
-    // The other JND-side outputs (dMeanRate, dLambda, CRLB_RA, ...) are not
-    // served.
+    //    JND_Lambda(k) plane k alone (calc_time x 256);
+    //  - the JND's debug stages, passed to CudaCalculateJND as backup_stage
+    //    and read from getCudaBuffer: AvgMeanRate (1, 3 x intervals),
+    //    dMeanRate (2) and CRLB_RA (6) and preFisherAITimeReduced (5)
+    //    [3][intervals][256], dLambda (3) and preFisherAI (4) 3 x calc_time x
+    //    256, dLambda(k) plane k.  (The reference writes a stage buffer for
+    //    dMeanRate, dLambda and CRLB_RA; for 1, 4 and 5 it writes the buffer it
+    //    last filled, so these files are this build's.)
     const std::string test_target = P.str("TEST_File_Target", "");
     const std::string test_type = P.str("Type_TEST_Output", "MeanRate");
     int backup_stage = -1;
     const bool test_mean_rate = !test_target.empty() && test_type == "MeanRate";
     int test_lambda = -2;  // -1: all planes, 0..: one plane
+    int jnd_stage = -1, jnd_plane = -1;
     std::smatch lam_m;
+    {
+      const char* jnames[] = {"AvgMeanRate", "dMeanRate", "dLambda", "preFisherAI",
+                              "preFisherAITimeReduced", "CRLB_RA"};
+      for (int k = 0; k < 6; ++k)
+        if (!test_target.empty() && test_type == jnames[k]) jnd_stage = 1 + k;
+      if (!test_target.empty() &&
+          std::regex_match(test_type, lam_m, std::regex("dLambda\\(([[:digit:]])\\)"))) {
+        jnd_stage = 3;
+        jnd_plane = std::stoi(lam_m[1]);
+        if (jnd_plane >= LAMBDA_COUNT)
+          throw std::runtime_error("index of lambda must be smaller than 3, you chose " +
+                                   lam_m[1].str());
+      }
+      if (jnd_stage > 0 && !calc_jnd)
+        throw std::runtime_error("Type_TEST_Output " + test_type + " needs Calculate_JND");
+    }
     if (!test_target.empty() && test_type == "JND_Lambda") test_lambda = -1;
     if (!test_target.empty() &&
         std::regex_match(test_type, lam_m, std::regex("JND_Lambda\\(([[:digit:]])\\)"))) {
@@ -333,14 +355,13 @@ int main(int argc, char** argv) {
         throw std::runtime_error("index of lambda must be smaller than 3, you chose " +
                                  lam_m[1].str());
     }
-    if (!test_target.empty() && !test_mean_rate && test_lambda == -2) {
+    if (!test_target.empty() && !test_mean_rate && test_lambda == -2 && jnd_stage < 0) {
       const char* names[] = {"AC", "DC", "dS", "Shigh", "IHC", "PRE_IHC"};
       for (int k = 0; k < 6; ++k)
         if (test_type == names[k]) backup_stage = 9 + k;
       if (backup_stage < 0)
         throw std::runtime_error("Type_TEST_Output " + test_type +
-                                 " is not served (only MeanRate and the IHC stages AC, DC, dS, "
-                                 "Shigh, IHC, PRE_IHC)");
+                                 " is not served");
     }
     if (test_mean_rate && !calc_jnd)
       throw std::runtime_error("Type_TEST_Output MeanRate needs Calculate_JND");
@@ -394,7 +415,8 @@ int main(int argc, char** argv) {
                        nihc.data(), calc_pos.data(), (int)calc_pos.size(), ref_pos.data(),
                        (int)ref_pos.size(), 0, n_int, n_int, head, overlap, L, len,
                        serial.data(), to_ref.data(), FRA.data(), FAI.data(), write_time * 256,
-                       calc_time * 256, 0.2 * (double)Fs, 1, 0, false, false, -1, log);
+                       calc_time * 256, 0.2 * (double)Fs, 1, 0, false, false,
+                       jnd_stage > 0 ? jnd_stage : backup_stage, log);
       for (int i = 0; i < n_int; ++i) {
         bool isref = false;
         for (int r : ref_pos) isref |= r == i;
@@ -411,6 +433,23 @@ int main(int argc, char** argv) {
         };
         jr[i] = db(ra);
         ja[i] = db(ai);
+      }
+      if (jnd_stage > 0) {
+        const size_t plane = (size_t)calc_time * 256, mean = (size_t)3 * n_int * 256;
+        size_t n = mean, off = 0;
+        if (jnd_stage == 1) n = (size_t)3 * n_int;
+        if (jnd_stage == 3 || jnd_stage == 4) n = 3 * plane;
+        if (jnd_plane >= 0) {
+          n = plane;
+          off = (size_t)jnd_plane * plane;
+        }
+        std::vector<float> st(n);
+        GeneralKernel_Copy_Results_Template<float>(st.data(), getCudaBuffer(), n, off);
+        FILE* tf = std::fopen(test_target.c_str(), "wb");
+        if (!tf) throw std::runtime_error("cannot open TEST_File_Target " + test_target);
+        const bool ok = std::fwrite(st.data(), sizeof(float), n, tf) == n;
+        std::fclose(tf);
+        if (!ok) throw std::runtime_error("short write to TEST_File_Target " + test_target);
       }
       if (test_mean_rate) {
         const size_t n = (size_t)3 * n_int * 256;  // getMeanNodes()

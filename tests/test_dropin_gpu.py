@@ -208,7 +208,9 @@ def test_harness_writes_the_ihc_stage_file(tmp_path, mv):
     floats, as the reference's AudioGramCreator does.  Each file equals the
     stage plane of the IHC kernel on the same velocity (bit for bit).  The
     default type, MeanRate, writes the JND's mean rates, JND_Lambda the
-    lambda planes; the other JND-side test outputs are refused."""
+    lambda planes, and the JND's debug stages (AvgMeanRate, dMeanRate,
+    dLambda, preFisherAI, preFisherAITimeReduced, CRLB_RA) their values; an
+    unknown type is refused."""
     import torch
     noise = np.random.default_rng(11).standard_normal(402).astype(np.float32)
     ac = ihc.design_ac_lowpass()
@@ -270,9 +272,46 @@ def test_harness_writes_the_ihc_stage_file(tmp_path, mv):
         got = np.fromfile(target, np.float32).reshape(len(planes), -1, 256)
         for k, j in enumerate(planes):
             assert np.array_equal(got[k, :nodes].view(np.uint32), lam[j, :nodes].view(np.uint32))
+    # the JND's debug stages, against the same quantities formed here from lambda
+    L, head, ln, n = run.L, run.head, run.len, run.n_int
+    dA = run.prof["dA"].astype(np.float64)
+    win = np.stack([lam[:, i * L + head:i * L + head + ln].astype(np.float64) for i in range(n)],
+                   axis=1)                                  # [3][n][len][256]
+    MR = win.mean(axis=2)                                   # [3][n][256]
+    ref = run.ref_of
+    with np.errstate(divide="ignore", invalid="ignore"):
+        dmr = (MR - MR[:, ref]) / dA[None, :, None]   # NaN where dA = 0, as the reference
+    T, Fs = 0.2, 100000.0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        dl = np.where(dA[None, :, None, None] > 0,
+                      (win - win[:, ref]) / dA[None, :, None, None], 0.0)
+    pre = dl * dl / (Fs * win[:, ref])
+    nihc = np.full(256, float(np.float32(30000.0 / 256.0)))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        want = {"AvgMeanRate": MR.mean(axis=2), "dMeanRate": dmr,
+                "CRLB_RA": 1.0 / np.sqrt(T * dmr * dmr / MR[:, ref]),
+                "preFisherAITimeReduced": (T / (ln / Fs)) * nihc * pre.sum(axis=2),
+                "dLambda": dl, "dLambda(2)": dl[2:], "preFisherAI": pre}
+    for name, w in want.items():
+        target = tmp_path / "js.bin"
+        par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
+                                  out=tmp_path / "out_mr.bin") +
+                       f'TEST_File_Target = "{target}"\nType_TEST_Output = "{name}"\n')
+        res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True,
+                             text=True, timeout=300)
+        assert res.returncode == 0, (name, res.stderr)
+        got = np.fromfile(target, np.float32).astype(np.float64)
+        if name.startswith(("dLambda", "preFisherAI")) and name != "preFisherAITimeReduced":
+            planes = got.reshape(w.shape[0], -1, 256)
+            got = np.stack([planes[:, i * L + head:i * L + head + ln] for i in range(n)], axis=1)
+        got = got.reshape(w.shape)
+        fin = np.isfinite(w)
+        assert np.array_equal(np.isfinite(got), fin), name
+        scale = np.abs(w[fin]).max()
+        assert np.abs(got[fin] - w[fin]).max() <= 1e-5 * scale, name
     par.write_text(PAR.format(ac=tmp_path / "ac.f32", noise=tmp_path / "noise.f32",
                               out=tmp_path / "out_mr.bin") +
-                   f'TEST_File_Target = "{tmp_path / "x.bin"}"\nType_TEST_Output = "dLambda"\n')
+                   f'TEST_File_Target = "{tmp_path / "x.bin"}"\nType_TEST_Output = "Nonsense"\n')
     res = subprocess.run([str(build.harness_path()), str(par)], capture_output=True, text=True,
                          timeout=300)
     assert res.returncode != 0 and "not served" in res.stderr
