@@ -255,8 +255,10 @@ class IHCStage:
                 "cgb_ihc_lambda_launch_mirror_dev")
 
     def run_iir(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, b, a,
-                want_ihc: bool = False):
-        """Host-buffer call of the IIR AC path; returns (lambda, ihc or None, ac)."""
+                want_ihc: bool = False, stage: int = 0):
+        """Host-buffer call of the IIR AC path; returns (lambda, ihc or None,
+        ac), and with stage 9-12 also that debug stage's [lam_rows][256]
+        plane as a fourth element."""
         torch = self.torch
         frames = np.ascontiguousarray(frames).view(FRAME_DTYPE)
         b = np.ascontiguousarray(b, np.float32)
@@ -266,6 +268,8 @@ class IHCStage:
         ihc = torch.zeros((lam_rows, 256), dtype=torch.float32, device=self.device) \
             if want_ihc else None
         ac = torch.zeros_like(d_v)
+        out = torch.zeros((lam_rows, 256), dtype=torch.float32, device=self.device) \
+            if stage else None
         need = self.lib.cgb_ihc_lambda_iir_scratch_bytes(native.ptr(frames), len(frames), len(b),
                                                          len(self.dc))
         if need < 0:
@@ -273,16 +277,24 @@ class IHCStage:
         sc = torch.empty(int(need), dtype=torch.uint8, device=self.device)
         self.status.zero_()
         st = torch.cuda.current_stream(self.device)
-        native.check(self.lib.cgb_ihc_lambda_iir_dev(
-            native.ptr(d_v), int(d_v.shape[0]), native.ptr(frames), len(frames), native.ptr(b),
-            native.ptr(a), len(b), native.ptr(self.dc), len(self.dc), C.byref(self.prm),
-            native.ptr(self.dmg), int(self.dmg.shape[0]), native.ptr(self.aihc), native.ptr(lam),
-            lam_rows, native.ptr(ihc), native.ptr(ac), native.ptr(sc), int(sc.numel()),
-            native.ptr(self.status), C.c_void_p(st.cuda_stream)), "cgb_ihc_lambda_iir_dev")
+        head = (native.ptr(d_v), int(d_v.shape[0]), native.ptr(frames), len(frames),
+                native.ptr(b), native.ptr(a), len(b), native.ptr(self.dc), len(self.dc),
+                C.byref(self.prm), native.ptr(self.dmg), int(self.dmg.shape[0]),
+                native.ptr(self.aihc), native.ptr(lam), lam_rows, native.ptr(ihc),
+                native.ptr(ac))
+        tail = (native.ptr(sc), int(sc.numel()), native.ptr(self.status),
+                C.c_void_p(st.cuda_stream))
+        if stage:
+            native.check(self.lib.cgb_ihc_lambda_iir_stage_dev(*head, int(stage),
+                                                               native.ptr(out), *tail),
+                         "cgb_ihc_lambda_iir_stage_dev")
+        else:
+            native.check(self.lib.cgb_ihc_lambda_iir_dev(*head, *tail), "cgb_ihc_lambda_iir_dev")
         torch.cuda.synchronize(self.device)
         if int(self.status[0].item()) != 0:
             raise native.CGBError("IHC stage: a staged copy did not complete")
-        return lam.cpu().numpy(), (ihc.cpu().numpy() if want_ihc else None), ac.cpu().numpy()
+        res = (lam.cpu().numpy(), (ihc.cpu().numpy() if want_ihc else None), ac.cpu().numpy())
+        return res + (out.cpu().numpy(),) if stage else res
 
     def run(self, v: np.ndarray, frames: np.ndarray, lam_rows: int, want_ihc: bool = False,
             stage: int = 0):

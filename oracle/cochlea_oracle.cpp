@@ -958,15 +958,18 @@ void orc_ihc_lambda_stage(const float* v, int rows, int seg, int frdp, int total
 
 // IHC + lambda from a given AC stage (ac: rows x 256 floats) in place of the
 // FIR; everything after the AC stage as orc_ihc_lambda in `mode`.  Accuracy
-// studies of other AC arithmetic feed their AC through it.
+// studies of other AC arithmetic feed their AC through it, and the IIR path's
+// debug stages are checked with it (stage / stage_out as orc_ihc_lambda_stage;
+// stage 0 for none).
 void orc_ihc_lambda_ac(const float* v, const float* ac, int rows, int seg, int frdp, int total,
                        int lam_rows, const double* dc_taps, int n_dc, double scale,
                        double eta_ac, double eta_dc, const double* ihc_damage, const float* aihc,
                        const float* spont, double lambda_sat, float* ihc, float* lam,
-                       int64_t lam_stride, int mode) {
+                       int64_t lam_stride, int mode, int stage, float* stage_out) {
   const double one = 1.0;
   ihc_lambda_impl(v, rows, seg, frdp, total, lam_rows, &one, 1, dc_taps, n_dc, scale, eta_ac,
-                  eta_dc, ihc_damage, aihc, spont, lambda_sat, ihc, lam, lam_stride, mode, ac);
+                  eta_dc, ihc_damage, aihc, spont, lambda_sat, ihc, lam, lam_stride, mode, ac,
+                  stage, stage_out);
 }
 
 // ---------------------------------------------------------------------------

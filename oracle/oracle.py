@@ -83,7 +83,8 @@ def load():
                                              C.c_int64, C.c_int, C.c_int, _p]
         lib.orc_ihc_lambda_ac.argtypes = [_p, _p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                           _p, C.c_int, C.c_double, C.c_double, C.c_double, _p,
-                                          _p, _p, C.c_double, _p, _p, C.c_int64, C.c_int]
+                                          _p, _p, C.c_double, _p, _p, C.c_int64, C.c_int,
+                                          C.c_int, _p]
         lib.orc_hearing_aid.argtypes = [_p, C.c_int, C.c_int, _p, C.c_int, _p, C.c_int, _p]
         lib.orc_ws_param_count.restype = C.c_int
         lib.orc_ws_forward_backward.argtypes = [_p, _p, _p, C.c_int, C.c_float, C.c_int, _p, _p,
@@ -242,23 +243,26 @@ def ihc_lambda_stage(v, seg, frdp, total, lam_rows, ac_taps, dc_taps, scale, eta
 
 
 def ihc_lambda_ac(v, ac, seg, frdp, total, lam_rows, dc_taps, scale, eta_ac, eta_dc,
-                  ihc_damage, aihc, spont, lambda_sat, mode=0):
+                  ihc_damage, aihc, spont, lambda_sat, mode=0, stage=0):
     """IHC/lambda with the AC stage given (rows x 256 floats) in place of the
-    FIR; the rest in `mode` as ihc_lambda.  Returns (ihc, lambda)."""
+    FIR; the rest in `mode` as ihc_lambda.  Returns (ihc, lambda), and with
+    stage 9-11 (as ihc_lambda_stage) also that plane [lam_rows][256]."""
     v = np.ascontiguousarray(v, np.float32)
     ac = np.ascontiguousarray(ac, np.float32)
     assert ac.shape == v.shape
     rows = v.shape[0]
     ihc = np.zeros((rows, 256), np.float32)
     lam = np.zeros((3, lam_rows, 256), np.float32)
+    out = np.zeros((lam_rows, 256), np.float32) if stage else None
     dc = np.ascontiguousarray(dc_taps, np.float64)
     load().orc_ihc_lambda_ac(_ptr(v), _ptr(ac), rows, seg, frdp, total, lam_rows, _ptr(dc),
                              len(dc), scale, eta_ac, eta_dc,
                              _ptr(np.ascontiguousarray(ihc_damage, np.float64)),
                              _ptr(np.ascontiguousarray(aihc, np.float32)),
                              _ptr(np.ascontiguousarray(spont, np.float32)), lambda_sat,
-                             _ptr(ihc), _ptr(lam), lam_rows, mode)
-    return ihc, lam
+                             _ptr(ihc), _ptr(lam), lam_rows, mode, stage,
+                             _ptr(out) if stage else None)
+    return (ihc, lam, out) if stage else (ihc, lam)
 
 
 def ihc_lambda_iir(v, seg, frdp, total, lam_rows, b, a, dc_taps, scale, eta_ac, eta_dc,

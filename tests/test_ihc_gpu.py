@@ -219,3 +219,30 @@ def test_debug_stage_rejected():
     for bad in (8, 13):
         with pytest.raises(native.CGBError):
             st.run(v, fr, 512, stage=bad)
+
+
+@pytest.mark.parametrize("stage_n", [9, 10, 11])
+def test_iir_debug_stages(mv, stage, stage_n):
+    """The debug stages on the IIR AC path: AC is the IIR's output; DC and dS
+    bit-exact against the oracle fed the same AC (kernel arithmetic)."""
+    case = cases.decoupled_sweep(mv, n_signals=2, decouple=2, block_ms=1.5, overlap_ms=0.5)
+    cfg, sc, gamma, units, x, rows = case
+    v, _, _ = orc.bm_run(mv.section_params(), gamma, sc, units, x, rows)
+    fr = ihc.reference_frame(cfg)
+    v = v[:int(fr["rows"][0])]
+    n = int(fr["lam_rows"][0])
+    b, a = ihc.design_ac_iir_lowpass(order=2)
+    lam0, _, ac0 = stage.run_iir(v, fr, n, b, a)
+    lam, _, ac, plane = stage.run_iir(v, fr, n, b, a, stage=stage_n)
+    assert np.array_equal(lam.view(np.uint32), lam0.view(np.uint32))
+    assert np.array_equal(ac.view(np.uint32), ac0.view(np.uint32))
+    f = fr[0]
+    _, _, want = orc.ihc_lambda_ac(v, ac, int(f["seg"]), int(f["frdp"]), int(f["total"]), n,
+                                   stage.dc.astype(np.float64), stage.nerve.scale,
+                                   stage.nerve.eta_AC, stage.nerve.eta_DC,
+                                   stage.dmg_host[0].astype(np.float64), stage.nerve.aihc(),
+                                   np.asarray(stage.nerve.spontRate, np.float32),
+                                   stage.nerve.Lambda_SAT, mode=2, stage=stage_n)
+    assert np.array_equal(plane.view(np.uint32), want.view(np.uint32))
+    if stage_n == 9:
+        assert np.array_equal(plane.view(np.uint32), ac[:n].view(np.uint32))
