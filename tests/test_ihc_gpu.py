@@ -70,6 +70,20 @@ def test_many_tiles_and_frames(stage):
                      ihc.round64(n), i % 2)
         lam0 += frames[i]["lam_rows"]
     _check(stage, v, frames, lam0)
+    # a debug stage over the same frames: each frame's rows land at its
+    # lambda rows, bit-exact against the oracle's kernel arithmetic
+    for st_n in (9, 10, 11):
+        _, _, plane = stage.run(v, frames, lam0, stage=st_n)
+        for fr in frames:
+            r0, n = int(fr["lam_row0"]), int(fr["lam_rows"])
+            want = orc.ihc_lambda_stage(
+                v[fr["v_row0"]:fr["v_row0"] + fr["rows"]], int(fr["seg"]), int(fr["frdp"]),
+                int(fr["total"]), n, stage.ac.astype(np.float64), stage.dc.astype(np.float64),
+                stage.nerve.scale, stage.nerve.eta_AC, stage.nerve.eta_DC,
+                stage.dmg_host[fr["ihc_profile"]].astype(np.float64), stage.nerve.aihc(),
+                np.asarray(stage.nerve.spontRate, np.float32), stage.nerve.Lambda_SAT, st_n,
+                mode=2)
+            assert np.array_equal(plane[r0:r0 + n].view(np.uint32), want.view(np.uint32)), st_n
 
 
 @pytest.mark.parametrize("kind", ["asymmetric", "even_symmetric"])
