@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from cochlearmodel_gb300 import batch, model
-from cochlearmodel_gb300.pipeline import JNDWindow, ProfileRun, ProfileSweep
+from cochlearmodel_gb300.pipeline import ProfileRun, ProfileSweep
 from oracle import oracle as orc
 from tests import cases
 

@@ -1,6 +1,5 @@
 """Known-answer and property tests of the CPU oracle itself."""
 import numpy as np
-import pytest
 
 from cochlearmodel_gb300 import model
 from oracle import oracle as orc
