@@ -28,9 +28,10 @@
 //   1  BMOHC_NEW_kernel's own operation order: its fmaf placement, CUDA's
 //      tanhf, __fdividef where it divides, its shared-memory tree order for
 //      the velocity-error sum and one Jacobi sweep at a time; checked bit for
-//      bit against the reference's compiled kernel.
-//   Both keep simulated time in a float accumulator, as the reference does.  (CUDA's tanhf gives the same bits under --fmad=false as under
-//      the reference's default --fmad=true, checked on every float input.)
+//      bit against the reference's compiled kernel.  (CUDA's tanhf gives the
+//      same bits under --fmad=false as under the reference's default
+//      --fmad=true, checked on every float input.)
+//   Both keep simulated time in a float accumulator, as the reference does.
 //
 // Floating-point order is fixed: the file is compiled with --fmad=false and
 // every fused multiply-add is an explicit __fmaf_rn.
