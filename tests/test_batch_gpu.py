@@ -127,3 +127,32 @@ def test_host_mirror_rejects_bad_buffers(sweep):
             C.cast(C.byref(ex), C.c_void_p), None)
         assert rc != 0 and msg in lib.cgb_last_error()
     torch.cuda.synchronize()
+
+
+def test_jnd_table_order_does_not_change_the_sums(sweep):
+    """cgb_jnd_batch_dev writes each descriptor's sums to its own output slot,
+    so the table's order (longest windows first, as BatchSweep builds it, or
+    any other) changes nothing; an empty table enqueues nothing."""
+    import torch
+    from cochlearmodel_gb300 import native
+    b, _ = sweep
+    lens = b.jnd_iv["len"]
+    assert (np.diff(lens) <= 0).all()           # longest first
+    b.jnd_sums()
+    torch.cuda.synchronize()
+    F0, A0 = b.d_FRA.clone(), b.d_FAI.clone()
+    perm = np.random.default_rng(5).permutation(len(b.jnd_iv))
+    shuffled = torch.from_numpy(b.jnd_iv[perm].view(np.uint8).copy()).to(b.d_jnd_iv.device)
+    lib = native.load()
+    b.d_FRA.zero_()
+    b.d_FAI.zero_()
+    native.check(lib.cgb_jnd_batch_dev(
+        native.ptr(b.d_lam), b.lam_rows, native.ptr(shuffled), len(b.jnd_iv), len(b.jnd_iv),
+        native.ptr(b.d_nihc), native.ptr(b.W), float(b.Fs), b.jnd_win.delta_alpha_time_factor * b.Fs,
+        native.ptr(b.d_FRA), native.ptr(b.d_FAI), None, None), "cgb_jnd_batch_dev")
+    torch.cuda.synchronize()
+    assert torch.equal(b.d_FRA, F0) and torch.equal(b.d_FAI, A0)
+    native.check(lib.cgb_jnd_batch_dev(
+        native.ptr(b.d_lam), b.lam_rows, native.ptr(shuffled), 0, 1,
+        native.ptr(b.d_nihc), native.ptr(b.W), float(b.Fs), b.jnd_win.delta_alpha_time_factor * b.Fs,
+        native.ptr(b.d_FRA), native.ptr(b.d_FAI), None, None), "cgb_jnd_batch_dev")
