@@ -24,6 +24,9 @@ Workloads (--workload):
 --jacobi selects the pressure solve: reference (the reference's fixed
 20/2 sweep schedule, default), or the tolerance mode (|dp| <= 1e-6 |p|)
 started from the previous pressure, its extrapolation, or the learned guess.
+--bm-kernel 0 runs the reference's default BM kernel (BMOHC_NEW_kernel's
+fault-count controller in the reference's operation order, bit-exact with its
+compiled kernel) in place of kernel 17's semantics.
 
 Every step recomputes everything from the profile table in HBM.  Reported
 beside the batched value: the same kernels run one signal at a time ("plain
@@ -444,6 +447,7 @@ def plain_single_signal(run, device, n_sample=12):
                                         powers=[20 * math.log10(p["dA"] / (10 * 2e-5))],
                                         noises=[noise_db]))]
         one = batch.BatchSweep(device, spec, mv=run.mv)
+        one.sc.controller, one.sc.arith = run.sc.controller, run.sc.arith
         for _ in range(2):
             one.generate_input()
             one.solve_bm()
@@ -474,6 +478,9 @@ def run_reference(args, rank, world):
     if args.workload != "jnd_sweep":
         return {"impl": "reference", "unavailable": "the host-core arm is built for the "
                                                     "default workload (jnd_sweep)"}
+    if args.bm_kernel != 17:
+        return {"impl": "reference", "unavailable": "the host-core arm evaluates kernel 17's "
+                                                    "semantics (--bm-kernel 17)"}
     cores = os.cpu_count() or 1
     ref = RefSweepCPU(n_seeds=args.n_seeds)
     value, ms, desc = ref_cpu_timed(ref, args.steps, args.warmup, cores)
@@ -489,12 +496,17 @@ def run_reference(args, rank, world):
                     "d2h_bytes_per_step": 0}}
 
 
-def base_config(kind, signals, units, audio, jacobi):
+def base_config(kind, signals, units, audio, jacobi, bm_kernel=17):
     """The workload description both arms print (the GPU arm adds its details)."""
+    if bm_kernel == 0:
+        sem = ("BMOHC_NEW_kernel (the reference default, Run_Fast_BM_Calculation 0) in the "
+               "reference's operation order, reference schedule (20/2 Jacobi sweeps)")
+    elif jacobi == "reference":
+        sem = "kernel 17, reference schedule (20/2 Jacobi sweeps)"
+    else:
+        sem = f"tolerance mode 1e-6, {jacobi} guess"
     return {"workload": kind, "signals": signals, "units": units, "audio_s_per_step": audio,
-            "fs": 100000,
-            "bm_semantics": "kernel 17, reference schedule (20/2 Jacobi sweeps)"
-            if jacobi == "reference" else f"tolerance mode 1e-6, {jacobi} guess"}
+            "fs": 100000, "bm_semantics": sem}
 
 
 def run_ours(args, rank, world, device):
@@ -503,8 +515,14 @@ def run_ours(args, rank, world, device):
 
     run = make_workload(args.workload, device, args.n_freq, args.n_seeds, args.n_signals)
     set_jacobi(run, args.jacobi, device)
+    if args.bm_kernel == 0:
+        # BMOHC_NEW_kernel's fault-count controller in the reference's operation
+        # order (as model.bm_scalars sets it for Run_Fast_BM_Calculation 0); it
+        # runs one launch shape of its own
+        run.sc.controller = run.sc.arith = 1
     tuning = None
-    if args.tune != "off" and hasattr(run, "tune") and args.jacobi == "reference":
+    if (args.tune != "off" and hasattr(run, "tune") and args.jacobi == "reference"
+            and args.bm_kernel == 17):
         choice, source = run.tune(use_cache=args.tune == "cache")
         tuning = {"bm_shape": choice.bm_shape, "ihc_run": choice.ihc_run, "source": source}
         args.shape = choice.bm_shape
@@ -606,7 +624,7 @@ def run_ours(args, rank, world, device):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": base_config(run.kind, n_signals(run), len(run.units), run.audio_seconds,
-                              args.jacobi),
+                              args.jacobi, args.bm_kernel),
         "details": {"l2": "flushed between timed steps (256 MB write)",
                     "path": " -> ".join(nm for nm, _ in stages(run)),
                     "cuda_graph": use_graph, "launch_shape": args.shape, "stage_ms": stage_ms,
@@ -628,7 +646,8 @@ def run_ours(args, rank, world, device):
     if plain is not None:
         line["plain_single_signal"] = plain
         line["speedup_vs_plain"] = value / plain["value"]
-    if rank == 0 and run.kind == "jnd_sweep" and args.jacobi == "reference" and not args.no_learned:
+    if (rank == 0 and run.kind == "jnd_sweep" and args.jacobi == "reference"
+            and args.bm_kernel == 17 and not args.no_learned):
         line["learned"] = learned_record(device, run.mv)
     return line, run
 
@@ -690,6 +709,10 @@ def main():
     ap.add_argument("--n-signals", type=int, default=1024, help="mixed_batch signals")
     ap.add_argument("--jacobi", default="reference", choices=list(JACOBI),
                     help="pressure solve: reference schedule or tolerance-mode guess")
+    ap.add_argument("--bm-kernel", type=int, default=17, choices=[17, 0],
+                    help="BM semantics (Run_Fast_BM_Calculation): 17 kernel 17 in the own "
+                         "order (default), 0 the reference default BMOHC_NEW_kernel in the "
+                         "reference's operation order")
     ap.add_argument("--cpu-seconds", type=float, default=20.0,
                     help="tone_sweep: seconds of the CPU baseline sample")
     ap.add_argument("--cpu-steps", type=int, default=4,

@@ -27,6 +27,7 @@ namespace {
 
 std::string g_err;
 CUmodule g_mod = nullptr;
+float g_bm_ms = 0.0f;  // device time of the last BM launch (CUDA events)
 CUcontext g_ctx = nullptr;
 
 int fail(const std::string& m) {
@@ -120,6 +121,10 @@ typedef struct {
 } refgpu_bm_params;
 
 const char* refgpu_last_error(void) { return g_err.c_str(); }
+
+// Device time in ms of the last refgpu_bm_run launch, taken by CUDA events
+// recorded on the launch stream on either side of the kernel.
+float refgpu_last_bm_ms(void) { return g_bm_ms; }
 
 // Loads the reference cubin into the primary context of device 0.
 int refgpu_load(const char* cubin_path) {
@@ -277,10 +282,18 @@ int refgpu_bm_run(int variant, const refgpu_bm_params* p, const float* const* se
                      &s_e1, &s_e2, &s_len, &s_ov, &s_dtmin, &s_dtmax};
     for (void* e : extra) args.push_back(e);
   }
+  CUevent ev[2] = {nullptr, nullptr};
+  RG_TRY(cuEventCreate(&ev[0], CU_EVENT_DEFAULT), "cuEventCreate");
+  RG_TRY(cuEventCreate(&ev[1], CU_EVENT_DEFAULT), "cuEventCreate");
+  RG_TRY(cuEventRecord(ev[0], nullptr), "cuEventRecord");
   RG_TRY(cuLaunchKernel(fn, (unsigned)TB, 1, 1, kSections, 1, 1, 0, nullptr, args.data(),
                         nullptr),
          "cuLaunchKernel (reference BM)");
+  RG_TRY(cuEventRecord(ev[1], nullptr), "cuEventRecord");
   RG_TRY(cuCtxSynchronize(), "reference BM kernel");
+  RG_TRY(cuEventElapsedTime(&g_bm_ms, ev[0], ev[1]), "cuEventElapsedTime");
+  cuEventDestroy(ev[0]);
+  cuEventDestroy(ev[1]);
   if (d_out.down(saved_speeds, (size_t)out_rows * kSections * 4)) return 1;
   if (failed_nodes && d_fn.down(failed_nodes, (size_t)out_rows * 4)) return 1;
   if (failed_blocks && d_fb.down(failed_blocks, (size_t)TB * 4)) return 1;

@@ -55,6 +55,7 @@ def load():
             subprocess.run(["sh", str(HERE / "build.sh")], check=True)
         lib = C.CDLL(str(LIB))
         lib.refgpu_last_error.restype = C.c_char_p
+        lib.refgpu_last_bm_ms.restype = C.c_float
         lib.refgpu_load.argtypes = [C.c_char_p]
         lib.refgpu_bm_run.argtypes = [C.c_int, C.POINTER(RefBMParams), _p, _p, _p, _p,
                                       C.c_longlong, _p, C.c_longlong, _p, _p]
@@ -132,6 +133,11 @@ def bm_run(variant: int, params: RefBMParams, sections, mtt, mmspt, inp, out_row
     if rc:
         raise RuntimeError(lib.refgpu_last_error().decode())
     return out, fn, fb
+
+
+def last_bm_ms() -> float:
+    """Device time (ms, CUDA events around the launch) of the last bm_run."""
+    return float(load().refgpu_last_bm_ms())
 
 
 def ihc_lambda(v, calc_time, interval, time_blocks, decouple, ac, dc, scale, eta_ac, eta_dc,

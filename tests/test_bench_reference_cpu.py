@@ -43,3 +43,14 @@ def test_reference_arm_workload_matches_the_gpu_arm():
     assert r.units_total == units == 3025
     assert np.isclose(r.audio_seconds, audio)
     assert len(r.specs) == 24 and sum(len(s["sweep"].powers) + 1 for s in r.specs) == 264
+
+
+def test_reference_arm_declines_kernel_0_semantics():
+    """The host-core arm evaluates kernel 17's semantics only; asked for the
+    reference default BM kernel it prints its unavailable line and exits 0."""
+    import json
+    res = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--bm-kernel", "0"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr
+    line = json.loads(res.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and "unavailable" in line
