@@ -30,7 +30,9 @@ compiled kernel) in place of kernel 17's semantics.
 
 Every step recomputes everything from the profile table in HBM.  Reported
 beside the batched value: the same kernels run one signal at a time ("plain
-single-signal"), and the CPU restatement on the host cores.
+single-signal"), the CPU restatement on the host cores, and (JND sweep,
+reference schedule) max_rel_vs_fp64: the step's velocity, lambda and JND error
+against the FP64 oracle on the shortest group, after the timed region.
 
 Arms:
   default            the GB300 kernels (value: device time; e2e: host tables in,
@@ -612,6 +614,14 @@ def run_ours(args, rank, world, device):
 
     plain = plain_single_signal(run, device) \
         if rank == 0 and not args.no_plain and run.kind != "mixed_batch" else None
+    accuracy = None
+    if rank == 0 and run.kind == "jnd_sweep" and args.jacobi == "reference" \
+            and not args.no_accuracy:
+        t_acc = time.perf_counter()
+        run.step()
+        torch.cuda.synchronize(device)
+        accuracy = accuracy_record(run)
+        accuracy["seconds"] = time.perf_counter() - t_acc
 
     peaks, peak_kind = measured_peaks()
     clock_mhz = peaks.get("sm_max_mhz", 2070.0)
@@ -646,10 +656,95 @@ def run_ours(args, rank, world, device):
     if plain is not None:
         line["plain_single_signal"] = plain
         line["speedup_vs_plain"] = value / plain["value"]
+    if accuracy is not None:
+        line["max_rel_vs_fp64"] = accuracy
     if (rank == 0 and run.kind == "jnd_sweep" and args.jacobi == "reference"
             and args.bm_kernel == 17 and not args.no_learned):
         line["learned"] = learned_record(device, run.mv)
     return line, run
+
+
+def accuracy_record(run):
+    """The step's error against the FP64 method on a bounded sample: the
+    shortest group of a batched JND sweep (a noise-only reference interval and
+    ten tones, all its blocks), from the run's device results of its last step.
+    Per interval:
+    - velocity against the FP64 oracle with the same step controller and
+      Jacobi schedule, and against the FP64 oracle with an exact tridiagonal
+      solve (the Jacobi schedule's truncation added);
+    - lambda (the worst of the three planes) against the FP64 IHC/lambda of
+      the FP64 velocity, the whole chain up to lambda;
+    - JND: |dB difference| of rate and all-info against the FP64 Fisher sums
+      of that lambda (tested intervals).
+    Errors are max |a - b| / max |b| over the interval's rows, and the
+    relative L2 norm |a - b|_2 / |b|_2.  The max measure of lambda is set by
+    the few rows where the IHC pre-potential crosses zero: the IHC stage
+    takes log10 of the rectified value plus 1e-20, so a small velocity
+    difference there moves the log between -20 and a finite value.  The
+    oracle runs on the host cores."""
+    from oracle import oracle as orc
+    gi = int(np.argmin([g.L for g in run.groups]))
+    g, fr = run.groups[gi], run.frames[gi]
+    rows = g.cfg.total_time_nodes_p1() + 4
+    units = run.units[run.units["out_base"] == g.v_row0].copy()
+    units["in_base"] -= g.in_base
+    units["out_base"] -= g.v_row0
+    x = run.d_in[g.in_base:g.in_base + rows].cpu().numpy()
+    v = run.d_v[g.v_row0:g.v_row0 + rows].cpu().numpy()
+    n_lam = int(fr["lam_rows"])
+    lam = run.d_lam[:, g.lam_row0:g.lam_row0 + n_lam].cpu().numpy()
+    rate_db, ai_db = run.jnd_db()[gi][:2]
+    gamma = run.d_gamma.cpu().numpy()
+    secp = run.mv.section_params()
+    cores = os.cpu_count() or 1
+
+    def max_rel(a, b):
+        return float(np.abs(np.asarray(a, np.float64) - b).max() / max(np.abs(b).max(), 1e-300))
+
+    def rel_l2(a, b):
+        b = np.asarray(b, np.float64)
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) /
+                     max(np.linalg.norm(b), 1e-300))
+
+    v64, _, _ = orc.bm_run(secp, gamma, run.sc, units, x, rows, fp64=True, threads=cores)
+    vex, _, _ = orc.bm_run(secp, gamma, run.sc, units, x, rows, fp64=True, threads=cores,
+                           jacobi_mode=1)
+    st, nv = run.ihc, run.nerve
+    _, lam64 = orc.ihc_lambda(v64[:int(fr["rows"])], int(fr["seg"]), int(fr["frdp"]),
+                              int(fr["total"]), n_lam, st.ac.astype(np.float64),
+                              st.dc.astype(np.float64), nv.scale, nv.eta_AC, nv.eta_DC,
+                              st.dmg_host[int(fr["ihc_profile"])].astype(np.float64), nv.aihc(),
+                              np.asarray(nv.spontRate, np.float32), nv.Lambda_SAT, mode=1)
+    n_int = len(g.prof)
+    head, length = run.jnd_win.nodes(g.cfg.Fs, g.L)
+    ra, ai = orc.jnd(lam64, n_int, g.L, head, length, g.prof["dA"], g.ref_of, nv.nihc(),
+                     np.asarray(nv.W, np.float32), float(g.cfg.Fs),
+                     run.jnd_win.delta_alpha_time_factor * g.cfg.Fs, fp64=True)
+    tested = g.ref_of != np.arange(n_int)
+    jnd_err = np.zeros(n_int)
+    for got, ref in ((rate_db, ra), (ai_db, ai)):
+        want = np.array([orc.jnd_db(ref[:, i].sum()) for i in range(n_int)])
+        jnd_err[tested] = np.maximum(jnd_err[tested], np.abs(got[tested] - want[tested]))
+    per = []
+    for k in range(n_int):
+        r = slice(k * g.L, (k + 1) * g.L)
+        dA = float(g.prof["dA"][k])
+        per.append({"signal": f"{20 * math.log10(dA / (10 * 2e-5)):.0f} dB tone"
+                    if tested[k] else "noise only",
+                    "velocity": max_rel(v[r], v64[r]), "velocity_rel_l2": rel_l2(v[r], v64[r]),
+                    "velocity_vs_exact_solve": max_rel(v[r], vex[r]),
+                    "lambda": max(max_rel(lam[j, r], lam64[j, r]) for j in range(3)),
+                    "lambda_rel_l2": max(rel_l2(lam[j, r], lam64[j, r]) for j in range(3)),
+                    "jnd_db_abs": float(jnd_err[k]) if tested[k] else None})
+    worst = {k: max(p[k] for p in per)
+             for k in ("velocity", "velocity_rel_l2", "velocity_vs_exact_solve", "lambda",
+                       "lambda_rel_l2")}
+    return {"sample": f"the shortest JND-sweep group ({n_int} intervals of {g.L} samples, "
+                      f"{len(units)} blocks), the run's own results; per interval "
+                      f"max |a - b| / max |b| and |a - b|_2 / |b|_2 over its rows "
+                      f"(lambda: the worst plane); the top level is the worst interval",
+            **worst, "jnd_db_abs": float(jnd_err.max()), "per_interval": per,
+            "oracle_threads": cores}
 
 
 def learned_record(device, mv, n_groups=3):
@@ -720,6 +815,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the max_rel_vs_fp64 record (FP64 oracle on one group)")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--shape", type=int, default=0, help="BM kernel launch shape (--tune off)")
     ap.add_argument("--tune", default="cache", choices=["cache", "search", "off"],
