@@ -5,10 +5,11 @@
 //
 // GB300 layout: one WARP owns one unit (one time block of one signal); lane l
 // holds sections 8l..8l+7 of every state vector in registers, as four
-// two-wide FP32 pairs.  Two Jacobi sweeps take four two-wide adds and four
-// two-wide fmas each per lane plus one round of four shuffles for a two-section
-// halo -- no shared-memory round trip and no block barrier, where the
-// reference spends two __syncthreads per sweep across 256 threads.  The
+// two-wide FP32 pairs.  Two Jacobi sweeps take one round of four shuffles
+// for a two-section halo and, in the own order with four or more sweeps, one
+// update over the second neighbours (three two-wide fmas per pair) -- no
+// shared-memory round trip and no block barrier, where the reference spends
+// two __syncthreads per sweep across 256 threads.  The
 // Lipschitz/fault reductions are xor-butterflies, so every lane holds the
 // full result and takes the same step decision.  Units come from a device
 // work queue, so a persistent grid of warps drains batches of uneven-length
@@ -24,7 +25,10 @@
 // Arithmetic (ARITH):
 //   0  own fixed order, reproduced bit for bit by the CPU oracle: explicit
 //      __fmaf_rn, own tanh and reciprocal, the step-size tests as products
-//      (no division).
+//      (no division), and an iteration's four or more Jacobi sweeps taken
+//      two at a time as one update over the second neighbours (the same
+//      iterates in exact arithmetic, three roundings per section instead
+//      of four).
 //   1  BMOHC_NEW_kernel's own operation order: its fmaf placement, CUDA's
 //      tanhf, __fdividef where it divides, its shared-memory tree order for
 //      the velocity-error sum and one Jacobi sweep at a time; checked bit for
@@ -575,6 +579,46 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
 #pragma unroll
         for (int k = 0; k < 4; ++k) p[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
       };
+      // Own order, four or more sweeps: pairs of sweeps as one update over
+      // the second neighbours, p''_s = C_s + a_s p_{s-2} + b_s p_s + c_s p_{s+2}
+      // (C = one sweep applied to Y/m; the coefficient rows are built per CTA
+      // in bm_body).  Three fmas per section instead of two sweeps' four
+      // operations, no halo sections, and one dependent fma after the
+      // shuffles.  On the mirror pairs both second neighbours are whole
+      // pairs: p[k-2] (the halos H2, H for k = 0, 1) holds the lower one of
+      // the pair's x section and the upper one of its y section, p[k+2]
+      // (p[3], p[2] swapped for k = 2, 3) the other two.  Row 8 multiplies
+      // the first, row 9 the second, which is added first: sections
+      // 8l..8l+3 add the upper term before the lower, 8l+4..8l+7 the lower
+      // before the upper.  Beyond the ends the wrapped and clamped shuffles
+      // deliver p_254, p_255 (below sections 0, 1) and p_248, p_249 (above
+      // 254, 255), each times a zero coefficient.
+      float2 C2[4], KL[4], KH[4], KB[4];
+      auto two_step_setup = [&]() {
+        load8q(sp + 8 * 256 + qb, KL);
+        load8q(sp + 9 * 256 + qb, KH);
+        load8q(sp + 10 * 256 + qb, KB);
+        float2 T[4];
+        T[0] = add2(Yrmh, Yrm[1]);
+        T[1] = fma2(lo1, Yrm[2], Yrm[0]);
+        T[2] = add2(Yrm[1], Yrm[3]);
+        T[3] = f2(__fadd_rn(Yrm[2].x, Yrm[3].y), __fadd_rn(Yrm[2].y, Yrm[3].x));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) C2[k] = fma2(neg2(T[k]), rm[k], Yrm[k]);
+      };
+      auto two_step = [&]() {
+        const float2 H =
+            f2(__shfl_sync(kFull, p[0].y, src_l), __shfl_down_sync(kFull, p[0].x, 1));
+        const float2 H2 =
+            f2(__shfl_sync(kFull, p[1].y, src_l), __shfl_down_sync(kFull, p[1].x, 1));
+        float2 r[4];
+        r[0] = fma2(KL[0], H2, fma2(KH[0], p[2], fma2(KB[0], p[0], C2[0])));
+        r[1] = fma2(KL[1], H, fma2(KH[1], p[3], fma2(KB[1], p[1], C2[1])));
+        r[2] = fma2(KL[2], p[0], fma2(KH[2], f2(p[3].y, p[3].x), fma2(KB[2], p[2], C2[2])));
+        r[3] = fma2(KL[3], p[1], fma2(KH[3], f2(p[2].y, p[2].x), fma2(KB[3], p[3], C2[3])));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) p[k] = r[k];
+      };
       int it = 0;
       if (ARITH) {
         // BMOHC_NEW_kernel's sweep, one at a time: p_s <- (Y_s - t_s) / m_s
@@ -598,13 +642,17 @@ __device__ __forceinline__ void run_unit(const BMArgs& A, const cgb_unit& un,
         }
       } else if (!TOL && J == 20) {
         // the reference schedule's slow count, fully unrolled
+        two_step_setup();
 #pragma unroll
-        for (int r = 0; r < 10; ++r) sweep_pair();
+        for (int r = 0; r < 10; ++r) two_step();
         it = 20;
       } else if (!TOL && J == 2) {
         // and its fast count, one pair without the loop
         sweep_pair();
         it = 2;
+      } else if (!TOL && J >= 4) {
+        two_step_setup();
+        for (; it + 1 < J; it += 2) two_step();
       } else {
 #pragma unroll 2
         for (; it + 1 < J; it += 2) {
@@ -784,12 +832,36 @@ constexpr int bm_dyn_smem() {
 
 template <int WARPS, bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __device__ __forceinline__ void bm_body(const BMArgs& A) {
-  __shared__ __align__(16) float s_par[8 * 256];
+  // rows 0-7: the section vectors of d_secp; 8-10: the two-step sweep
+  // coefficients derived from row 1 (1/m)
+  __shared__ __align__(16) float s_par[11 * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
   __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 9 * 256 : 4];
   extern __shared__ __align__(16) unsigned char s_dyn[];
   for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
     s_par[(i & ~255) | smem_pos(i & 255)] = A.secp[i];
+  __syncthreads();
+  // Two-step sweep coefficients (run_unit), each one FP32 product of 1/m
+  // values: a_s = rm_s rm_{s-1} (2 <= s <= 253), c_s = rm_s rm_{s+1}
+  // (s <= 253), b_s = rm_s (l_s rm_{s-1} + l_{s+1} rm_{s+1}) with l_s = 0 on
+  // sections 254, 255 and rm_{-1} = rm_256 = 0.  Row 8 multiplies the
+  // neighbour pair p[k-2], which holds the lower second neighbour of an x
+  // section (s mod 8 < 4: a_s) and the upper one of a y section (c_s); row 9
+  // the other one; row 10 b_s.
+  for (int s = threadIdx.x; s < 256; s += blockDim.x) {
+    const float r = s_par[256 + smem_pos(s)];
+    const float rl = s >= 1 ? s_par[256 + smem_pos(s - 1)] : 0.0f;
+    const float ru = s <= 254 ? s_par[256 + smem_pos(s + 1)] : 0.0f;
+    const float a = (s >= 2 && s <= 253) ? __fmul_rn(r, rl) : 0.0f;
+    const float c = s <= 253 ? __fmul_rn(r, ru) : 0.0f;
+    const float b =
+        __fmul_rn(r, __fadd_rn((s >= 1 && s <= 253) ? rl : 0.0f, s <= 252 ? ru : 0.0f));
+    const bool x_half = (s & 7) < 4;
+    const int q = smem_pos(s);
+    s_par[8 * 256 + q] = x_half ? a : c;
+    s_par[9 * 256 + q] = x_half ? c : a;
+    s_par[10 * 256 + q] = b;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float* hist = nullptr;
   unsigned char* wblob = nullptr;

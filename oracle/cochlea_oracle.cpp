@@ -292,7 +292,33 @@ namespace {
 template <typename T>
 struct BMModel {
   T invM[NS], rm[NS], R[NS], S[NS], Q[NS], S_ohc[NS], S_tm[NS], R_tm[NS];
+  // two-step sweep coefficients (FP32 own order): the lower / upper
+  // neighbour's coefficient a_s / c_s and the centre's b_s
+  T k2a[NS], k2c[NS], k2b[NS];
 };
+
+// Two sweeps p -> q -> p'' (q_s = Yrm_s - rm_s (l_s p_{s-1} + p_{s+1}), with
+// l_s = 0 on sections 254 and 255 and the boundary values p_{-1} = p_256 =
+// q_{-1} = q_256 = 0) fold into one update over the second neighbours:
+//   p''_s = C_s + a_s p_{s-2} + b_s p_s + c_s p_{s+2},
+//   C_s = Yrm_s - rm_s (l_s Yrm_{s-1} + Yrm_{s+1})   (one sweep applied to Y/m),
+//   a_s = rm_s rm_{s-1}                 for 2 <= s <= 253, else 0,
+//   c_s = rm_s rm_{s+1}                 for s <= 253, else 0,
+//   b_s = rm_s (l_s rm_{s-1} + l_{s+1} rm_{s+1})  (rm_{-1} = rm_256 = 0).
+// Each coefficient is one FP32 product (b_s of an FP32 sum).  In exact
+// arithmetic p'' is the result of the two sweeps; in FP32 it takes three
+// roundings per section instead of four.
+template <typename T>
+void two_step_coefficients(BMModel<T>& md) {
+  for (int s = 0; s < NS; ++s) {
+    const T r = md.rm[s];
+    md.k2a[s] = (s >= 2 && s <= NS - 3) ? r * md.rm[s - 1] : (T)0;
+    md.k2c[s] = s <= NS - 3 ? r * md.rm[s + 1] : (T)0;
+    const T lo = (s >= 1 && s <= NS - 3) ? md.rm[s - 1] : (T)0;
+    const T up = s + 1 <= NS - 3 ? md.rm[s + 1] : (T)0;
+    md.k2b[s] = r * (lo + up);
+  }
+}
 
 template <typename T>
 T pair_sum(const T* t, int n) {
@@ -482,6 +508,41 @@ void bm_unit(const BMModel<T>& md, const T* gam, const T* gs, const orc_bm_scala
           if (dmax <= tol * pmax) break;
         }
         S.sweeps += done;
+      } else if (kF32 && J >= 4) {
+        // Own FP32 order with four or more sweeps: C = one sweep applied to
+        // Y/m, then J/2 two-step updates (two_step_coefficients), then a
+        // last single sweep if J is odd.  The kernel holds sections 8l+j and
+        // 8l+7-j (j < 4) of lane l as one register pair and adds the two
+        // neighbour terms in the pair's order: sections with s mod 8 < 4 add
+        // the upper term, then the lower; the others the lower, then the
+        // upper.  Beyond the ends the neighbour values are those the warp
+        // shuffles deliver, each times a zero coefficient: p_254, p_255 below
+        // sections 0 and 1, p_248, p_249 above sections 254 and 255.
+        for (int s = 0; s < NS; ++s) Yrm[s] = Y[s] * md.rm[s];
+        T C2[NS];
+        jacobi_sweep<T>(Yrm, C2, Yrm, md.rm);
+        int it = 0;
+        for (; it + 1 < J; it += 2) {
+          for (int s = 0; s < NS; ++s) {
+            const T lo = s >= 2 ? p[s - 2] : p[s + NS - 2];
+            const T hi = s <= NS - 3 ? p[s + 2] : p[s - 6];
+            T r = A::fma(md.k2b[s], p[s], C2[s]);
+            if ((s & 7) < 4) {
+              r = A::fma(md.k2c[s], hi, r);
+              r = A::fma(md.k2a[s], lo, r);
+            } else {
+              r = A::fma(md.k2a[s], lo, r);
+              r = A::fma(md.k2c[s], hi, r);
+            }
+            tmp[s] = r;
+          }
+          for (int s = 0; s < NS; ++s) p[s] = tmp[s];
+        }
+        if (it < J) {
+          jacobi_sweep<T>(p, tmp, Yrm, md.rm);
+          for (int s = 0; s < NS; ++s) p[s] = tmp[s];
+        }
+        S.sweeps += J;
       } else {
         // p_s <- (Y_s - (l_s p_{s-1} + p_{s+1})) / m_s, evaluated as
         // fma(-t, 1/m_s, Y_s/m_s) with Y_s/m_s formed once per iteration.
@@ -627,6 +688,7 @@ void bm_run(const float* secp, const float* gamma, const orc_bm_scalars* sc,
     md.S_tm[s] = (T)secp[6 * NS + s];
     md.R_tm[s] = (T)secp[7 * NS + s];
   }
+  two_step_coefficients(md);
   std::atomic<int> next(0);
   auto worker = [&]() {
     T gam[NS], gs[NS];
