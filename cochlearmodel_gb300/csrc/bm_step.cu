@@ -832,9 +832,10 @@ constexpr int bm_dyn_smem() {
 
 template <int WARPS, bool PREV_SMEM, int TOL, int CTL, int ARITH>
 __device__ __forceinline__ void bm_body(const BMArgs& A) {
-  // rows 0-7: the section vectors of d_secp; 8-10: the two-step sweep
-  // coefficients derived from row 1 (1/m)
-  __shared__ __align__(16) float s_par[11 * 256];
+  // rows 0-7: the section vectors of d_secp; 8-10 (own order, fixed sweep
+  // counts only): the two-step sweep coefficients derived from row 1 (1/m)
+  constexpr bool kTwoStep = TOL == 0 && ARITH == 0;
+  __shared__ __align__(16) float s_par[(kTwoStep ? 11 : 8) * 256];
   __shared__ __align__(16) float s_gam[WARPS][2][256];
   __shared__ __align__(16) float s_prev[PREV_SMEM ? WARPS : 1][PREV_SMEM ? 9 * 256 : 4];
   extern __shared__ __align__(16) unsigned char s_dyn[];
@@ -848,7 +849,7 @@ __device__ __forceinline__ void bm_body(const BMArgs& A) {
   // neighbour pair p[k-2], which holds the lower second neighbour of an x
   // section (s mod 8 < 4: a_s) and the upper one of a y section (c_s); row 9
   // the other one; row 10 b_s.
-  for (int s = threadIdx.x; s < 256; s += blockDim.x) {
+  for (int s = threadIdx.x; kTwoStep && s < 256; s += blockDim.x) {
     const float r = s_par[256 + smem_pos(s)];
     const float rl = s >= 1 ? s_par[256 + smem_pos(s - 1)] : 0.0f;
     const float ru = s <= 254 ? s_par[256 + smem_pos(s + 1)] : 0.0f;
