@@ -2,7 +2,7 @@
 # Builds oracle/_ref/cochlea_ref.cubin: the REFERENCE's own device code
 # (src/cochlea.cu, which includes include/cochlea.cuh), compiled unmodified
 # for sm_103a from the reference tree with the reference's default nvcc
-# settings.  Test infrastructure only: it is the parity judge loaded by
+# settings.  Test infrastructure only: it is the parity reference loaded by
 # oracle/ref_gpu.cpp; the product never loads it.
 #
 # The reference is written for MSVC and the CUDA Samples; oracle/ref_shim/

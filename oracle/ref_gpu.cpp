@@ -6,7 +6,7 @@
 // it loads that cubin through the CUDA driver API, fills the reference's
 // __constant__ symbols and launch arguments the way the reference's host
 // functions do (each step cites the lines it restates), launches the
-// reference's kernels and copies their results back.  It is the parity judge
+// reference's kernels and copies their results back.  It is the parity reference
 // for the product's reference-arithmetic BM mode and reports the reference's
 // FP32 results for the error tables; nothing in the product links or loads it.
 //
