@@ -45,56 +45,66 @@ def _events_ms(torch, fn, reps=1):
     return s.elapsed_time(e) / reps
 
 
-def main():
+def compare_group(sp, mv, md, dev="cuda:0", Fs=100000):
+    """One JND-sweep group (a jnd_sweep_spec entry) through the product's BM
+    (controller 1, arith 1) and, when no unit stopped on the substep guard,
+    through the reference's BMOHC_NEW_kernel on the same input.  Returns the
+    group's record: blocks, audio seconds, substeps, the product's ms, and the
+    reference's ms and bit-exactness on the owned rows (or why it was
+    skipped)."""
     import torch
     from cochlearmodel_gb300 import batch, model, native
     from cochlearmodel_gb300.pipeline import ProfileRun
-    from oracle import oracle as orc
     from oracle import ref_gpu
+
+    N, D = batch.block_nodes_for(sp["length"], 1000, Fs)
+    cfg = model.RunConfig(Fs=Fs, Time_Block_Length=N / Fs, Decouple_Filter=D,
+                          Overlap_Time=0.005, OHC_Vector=batch.hearing_loss_ohc(),
+                          IHC_Vector=batch.hearing_loss_ihc(), Run_Fast_BM_Calculation=0)
+    run = ProfileRun(dev, cfg, sp["sweep"], noise=sp["noise"], mv=mv, want_lambda=False)
+    assert run.sc.controller == 1 and run.sc.arith == 1
+    run.generate_input()
+    run.solve_bm()  # warm-up
+    ours_ms = _events_ms(torch, run.solve_bm)
+    st = run.d_stats.cpu().numpy().view(native.STATS_DTYPE).ravel()
+    g = {"length": int(sp["length"]), "blocks": len(run.units), "audio_s": run.audio_seconds,
+         "substeps": int(st["substeps"].sum()), "ours_ms": ours_ms}
+    if (st["status"] != 0).any():
+        g["reference"] = "skipped: a unit stopped on the substep guard"
+        return g
+    x = run.d_in.cpu().numpy()
+    v = run.d_v.cpu().numpy()
+    p = ref_gpu.params_from(run.cfg, run.sc)
+    secs = ref_gpu.sections_from(md, run.cfg.gamma())
+    mtt = np.full(run.cfg.Time_Blocks, run.cfg.Max_Tolerance, np.float32)
+    mmspt = np.full(run.cfg.Time_Blocks, run.cfg.Max_M1_SP_Error, np.float32)
+    r_v, _, _ = ref_gpu.bm_run(0, p, secs, mtt, mmspt, x, run.rows)
+    g["reference_ms"] = ref_gpu.last_bm_ms()
+    mask = _owned(run.units, run.rows)
+    g["owned_rows"] = int(mask.sum())
+    g["bit_exact"] = bool(np.array_equal(v[mask].view(np.uint32), r_v[mask].view(np.uint32)))
+    return g
+
+
+def main():
+    import torch
+    from cochlearmodel_gb300 import batch, model
+    from oracle import oracle as orc
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--seeds", type=int, default=4)
     args = ap.parse_args()
     dev = "cuda:0"
-    Fs = 100000
     mv = model.ModelVectors.build()
     specs = batch.jnd_sweep_spec(n_seeds=args.seeds)
-    ohc, ihc_vec = batch.hearing_loss_ohc(), batch.hearing_loss_ihc()
     md = orc.model_setup()
     groups = []
     for gi, sp in enumerate(specs):
-        N, D = batch.block_nodes_for(sp["length"], 1000, Fs)
-        cfg = model.RunConfig(Fs=Fs, Time_Block_Length=N / Fs, Decouple_Filter=D,
-                              Overlap_Time=0.005, OHC_Vector=ohc, IHC_Vector=ihc_vec,
-                              Run_Fast_BM_Calculation=0)
-        run = ProfileRun(dev, cfg, sp["sweep"], noise=sp["noise"], mv=mv, want_lambda=False)
-        assert run.sc.controller == 1 and run.sc.arith == 1
-        run.generate_input()
-        run.solve_bm()  # warm-up
-        ours_ms = _events_ms(torch, run.solve_bm)
-        st = run.d_stats.cpu().numpy().view(native.STATS_DTYPE).ravel()
-        g = {"group": gi, "length": int(sp["length"]), "blocks": len(run.units),
-             "audio_s": run.audio_seconds, "substeps": int(st["substeps"].sum()),
-             "ours_ms": ours_ms}
-        if (st["status"] != 0).any():
-            g["reference"] = "skipped: a unit stopped on the substep guard"
-            groups.append(g)
-            continue
-        x = run.d_in.cpu().numpy()
-        v = run.d_v.cpu().numpy()
-        p = ref_gpu.params_from(run.cfg, run.sc)
-        secs = ref_gpu.sections_from(md, run.cfg.gamma())
-        mtt = np.full(run.cfg.Time_Blocks, run.cfg.Max_Tolerance, np.float32)
-        mmspt = np.full(run.cfg.Time_Blocks, run.cfg.Max_M1_SP_Error, np.float32)
         if gi == 0:
-            ref_gpu.bm_run(0, p, secs, mtt, mmspt, x, run.rows)  # module warm-up
-        r_v, _, _ = ref_gpu.bm_run(0, p, secs, mtt, mmspt, x, run.rows)
-        g["reference_ms"] = ref_gpu.last_bm_ms()
-        mask = _owned(run.units, run.rows)
-        g["bit_exact"] = bool(np.array_equal(v[mask].view(np.uint32),
-                                             r_v[mask].view(np.uint32)))
+            compare_group(sp, mv, md, dev)  # module and kernel warm-up
+        g = compare_group(sp, mv, md, dev)
+        g["group"] = gi
         groups.append(g)
-        del run
         torch.cuda.empty_cache()
 
     sweep = batch.BatchSweep(dev, specs, mv=mv)

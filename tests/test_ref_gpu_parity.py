@@ -245,3 +245,22 @@ def test_whole_profile_path_on_the_reference_default(mv):
         want_db = np.array([orc.jnd_db(ref[:, i].astype(np.float64).sum())
                             for i in range(run.n_int)])
         assert np.abs(got_db[tested] - want_db[tested]).max() <= JND_DB_TOL
+
+
+def test_jnd_sweep_groups_bit_exact_against_the_reference_default(mv):
+    """Whole groups of the JND sweep (hearing-loss profile, seeded noise,
+    10-100 dB tones and the noise-only reference) through the reference's
+    compiled BMOHC_NEW_kernel as Run_Cuda launches it, and through the
+    product's reference-arithmetic mode: bit-exact on every owned row.  The
+    shortest group (44 blocks) and the longest (220 blocks, 196 ms signals)."""
+    from cochlearmodel_gb300 import batch
+    from oracle import ref_gpu_sweep
+    specs = batch.jnd_sweep_spec(n_seeds=4)
+    md = orc.model_setup()
+    order = np.argsort([sp["length"] for sp in specs])
+    for gi in (order[0], order[-1]):
+        g = ref_gpu_sweep.compare_group(specs[gi], mv, md)
+        print(f"JND-sweep group {gi}: {g['blocks']} blocks, {g['owned_rows']} owned rows, "
+              f"bit-exact {g['bit_exact']}")
+        assert "reference_ms" in g, g.get("reference")
+        assert g["owned_rows"] > 0 and g["bit_exact"]
