@@ -18,18 +18,22 @@
 //   * input generation         src/cochlea.cu:4070-4103, 4165-4254
 //
 // Parity pinning: the reference publishes no tests, fixtures or golden
-// vectors, and its own path cannot be built here (Windows/MFC/MATLAB host,
-// GPU-only kernels).  Its Thomas solve (src/tridiag.cpp) and constants
-// header (include/const.h) DO compile on their own; oracle/build_ref.sh
-// builds them into oracle/_ref/ and tests/test_oracle_pins.py checks this
-// restatement against them.  The BM step, IHC, lambda and JND stages are
-// pinned only by this restatement ("parity pinned for the model constants
-// and the tridiagonal solve; restatement-only for the time stepping").
+// vectors, and its host path cannot be built here (Windows/MFC/MATLAB).  Its
+// Thomas solve (src/tridiag.cpp) and constants header (include/const.h)
+// compile on their own; oracle/build_ref.sh builds them into oracle/_ref/ and
+// tests/test_oracle_pins.py checks this restatement against them.  Its device
+// code compiles too (oracle/build_ref_gpu.sh, launched by oracle/ref_gpu.cpp):
+// on a GPU the IHC/lambda restatement in the reference's mixed precision
+// equals the reference's own kernels bit for bit, the JND sums agree with
+// them, and the product's reference-order BM mode equals BMOHC_NEW_kernel bit
+// for bit (tests/test_ref_gpu_parity.py).
 //
 // FP32 mode fixes the order of every floating-point operation (explicit
-// fmaf, IEEE division, a fixed reduction tree) so that the CUDA kernels,
+// fmaf, IEEE division, a fixed reduction tree, the own-order pairs of Jacobi
+// sweeps as one update over the second neighbours) so that the CUDA kernels,
 // which follow the same order, agree with it bit for bit.  FP64 mode runs the
-// same algorithm in double and is the accuracy yardstick.
+// reference algorithm (plain sweeps) in double and is the accuracy
+// yardstick.
 //
 // Build: oracle/build.sh (g++ -O2 -ffp-contract=off, no fast-math).
 
